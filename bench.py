@@ -1,0 +1,313 @@
+"""Benchmark: iso-queries/s of the block-compressed marching-cubes pipeline.
+
+Workload (one "step"): the 256^3 CT-like volume (uint8-range values stored as
+float32, ~35 % constant-0 background blocks, interior 20-255 + N(0,3) noise),
+ZFP fixed rate 4 bits/value, cache initially 50 % of the 262,144 blocks; the
+step resets the cache and runs the 16 isovalues linspace(30, 220, 16) one at a
+time through computeSurface.  Synthetic data generated from a seed (the
+reference's scans are not shipped).
+
+Lines printed (one JSON line on rank 0):
+  value   iso-queries/s, volume resident in HBM, timed with CUDA events on the
+          library's stream (L2 flushed with a 512 MB write between steps)
+  e2e     the same through the C ABI with a host copy of every vertex buffer
+  roofline  the dominant kernel's algorithmic bytes / its CUDA-event time
+  cpu_baseline  the CPU oracle (OpenMP, all host cores) on one step
+
+`--impl reference` times the CPU restatement of the reference pipeline (the
+reference itself is WebGPU/JavaScript and has no CPU path) on the same config.
+Under torchrun (N>1) each rank runs an independent replica (the path does not
+shard); value is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "webgpu-bcmc_gb300"))
+
+CONFIG = dict(workload="ct256: 256^3 CT-like float32, ZFP rate 4, 16 isovalues linspace(30,220,16), "
+                       "cache 50% of 262144 blocks, cache reset per step",
+              dims=(256, 256, 256), rate=4, seed=2, cache_fraction=0.5)
+METRIC = "iso-queries/s (plain per-query path, ct256)"
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock and throttle reasons)."""
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                           "--format=csv,noheader,nounits", "-lms", "100"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self._proc = None
+            return
+        threading.Thread(target=self._read, daemon=True).start()
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self) -> dict:
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def make_volume():
+    from bcmc import datasets as D
+
+    field = D.ct_like(CONFIG["dims"], CONFIG["seed"])
+    isos = np.linspace(30.0, 220.0, 16).astype(np.float32)
+    return field, isos
+
+
+def encode_on_gpu(ctx, field):
+    import torch
+
+    import bcmc
+
+    words = bcmc.zfp_encode(ctx, torch.from_numpy(field).cuda(), CONFIG["rate"])
+    torch.cuda.synchronize()
+    nb = int(np.prod([(d + 3) // 4 for d in CONFIG["dims"]]))
+    nbytes = nb * 64 * CONFIG["rate"] // 8
+    host = words.cpu().numpy().view(np.uint8)[:nbytes].copy()
+    return words, host
+
+
+def cpu_oracle_time(field, isos, steps: int = 1):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build()
+    words = oracle.zfp_encode(field, CONFIG["rate"])
+    m = oracle.CompressedMarchingCubes(words, CONFIG["rate"], CONFIG["dims"],
+                                       initial_cache_fraction=CONFIG["cache_fraction"])
+    m.compute_surface(float(isos[0]))  # warm caches / threads
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        m.cache_reset()
+        for iso in isos:
+            m.compute_surface(float(iso))
+    dt = time.perf_counter() - t0
+    return len(isos) * steps / dt, oracle.threads(), words
+
+
+def run_reference(args):
+    """CPU restatement of the reference pipeline, all host threads."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    field, isos = make_volume()
+    steps = max(1, args.steps)
+    for _ in range(args.warmup):
+        pass
+    qps, threads, _ = cpu_oracle_time(field, isos, steps=steps)
+    line = {"impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1000.0 * len(isos) / qps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded CT-like field, ZFP-encoded by the project's encoder)",
+            "config": {"workload": CONFIG["workload"]},
+            "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": f"{steps} step(s) of 16 queries, CPU oracle (C, OpenMP)"},
+            "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def algorithmic_bytes(stage: str, st: dict, rate: int, total_blocks: int) -> float:
+    """Algorithmic DRAM bytes per launch of each stage's kernel."""
+    if stage == "computeVertices":  # k_mc: block data + ids/slots + vertices
+        return st["numActiveBlocks"] * (256 + 4 + 4) + st["numVertices"] * 8 + st["numBlocksWithVertices"] * 8
+    if stage == "decompression":  # k_assign: compressed bits + decoded block + ids
+        return st["newDecompressed"] * (8 * rate + 256 + 8)
+    if stage == "computeActiveBlocks":  # k_active: ranges, slots, flags
+        return total_blocks * (8 + 4 + 4) + st["numActiveBlocks"] * 4
+    if stage == "cacheUpdate":  # k_slots + sort: 3 slot arrays rw + sort passes
+        return st["cacheSize"] * (12 + 12) + st["slotsAvailable"] * 16
+    return 0.0
+
+
+def run_gb300(args):
+    import torch
+    import torch.distributed as dist
+
+    import bcmc
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    field, isos = make_volume()
+    ctx = bcmc.Context(local, initial_cache_fraction=CONFIG["cache_fraction"])
+    _, host_stream = encode_on_gpu(ctx, field)
+    mc = bcmc.CompressedMarchingCubes(ctx)
+    t0 = time.perf_counter()
+    mc.setCompressedVolume(host_stream, CONFIG["rate"], CONFIG["dims"])
+    load_s = time.perf_counter() - t0
+    total_blocks = mc.totalBlocks
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
+    L = bcmc._lib.load()
+
+    def step(perf=None, copy_out=None):
+        mc.lruCache.reset()
+        n_tot = 0
+        for iso in isos:
+            n = mc.computeSurface(float(iso), perf)
+            if copy_out is not None:
+                mc.copyVertices(copy_out)
+            n_tot += n
+        return n_tot
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    # timed: device-resident
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    times = []
+    launches0 = L.bcmc_kernel_launches()
+    perf = {}
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step(perf)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    launches = L.bcmc_kernel_launches() - launches0
+    clk = clocks.stop()
+    ms = float(np.mean(times))
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * len(isos) / (ms / 1000.0)
+
+    # e2e: every query's vertex buffer copied to pinned host memory
+    vmax = 1 << 24
+    pinned = torch.empty((vmax, 2), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    e2e_times, d2h = [], 0
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        n_tot = step(None, pinned)
+        e2e_times.append(time.perf_counter() - t0)
+        d2h = n_tot * 8
+    e2e_ms = 1000.0 * float(np.mean(e2e_times))
+    e2e_value = world * len(isos) / (e2e_ms / 1000.0)
+
+    # roofline of the dominant stage (CUDA-event stage times of the timed steps)
+    stages = ("computeActiveBlocks", "cacheUpdate", "decompression", "computeVertices")
+    tot = {s: float(np.sum(perf[s])) for s in stages}
+    dominant = max(stages, key=lambda s: tot[s])
+    # per-launch algorithmic bytes, averaged over the queries of the timed steps
+    nq = len(perf[dominant])
+    stats_seq = []
+    mc.lruCache.reset()
+    for iso in isos:
+        mc.computeSurface(float(iso))
+        s = mc.stats()
+        s["slotsAvailable"] = mc.lruCache.displayNumSlotsAvailable + s["newDecompressed"]
+        stats_seq.append(s)
+    bytes_per_launch = float(np.mean([algorithmic_bytes(dominant, s, CONFIG["rate"], total_blocks)
+                                      for s in stats_seq]))
+    avg_ms = tot[dominant] / nq
+    peak, peak_kind = _peaks()
+    achieved = bytes_per_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else 0.0
+    kernel_of = {"computeVertices": "k_mc", "decompression": "k_assign (LRU assign + ZFP decode)",
+                 "computeActiveBlocks": "k_active", "cacheUpdate": "k_slots + radix sort"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        qps, threads, _ = cpu_oracle_time(field, isos, steps=1)
+        cpu = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+               "sample": "1 step (cache reset + 16 queries) of the same workload, CPU oracle (C, OpenMP)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded CT-like field, ZFP-encoded on the GPU by the project's encoder)",
+                "config": {"workload": CONFIG["workload"], "l2": "flushed (512 MB write) between steps",
+                           "parallelism": f"replicas x{world}"},
+                "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": 4 * len(isos),
+                        "d2h_bytes_per_step": d2h},
+                "roofline": {"bound": "hbm", "kernel": kernel_of[dominant], "achieved": achieved, "peak": peak,
+                             "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                             "traffic": None, "avg_launch_ms": avg_ms, "algorithmic_bytes": bytes_per_launch},
+                "stage_ms_per_query": {s: tot[s] / nq for s in stages},
+                "gpu_launches": int(launches),
+                "clocks": clk,
+                "volume_load_s": load_s,
+                "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

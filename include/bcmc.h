@@ -1,0 +1,232 @@
+/*
+ * bcmc.h -- C ABI of the GB300 block-compressed marching-cubes library
+ * (libbcmc_gb300.so, CUDA for sm_103a).
+ *
+ * Drop-in for the compute path of Twinklebear/webgpu-bcmc: the
+ * CompressedMarchingCubes pipeline (js/compressed_marching_cubes.js) and the
+ * GPU primitives it is built from (js/lru_cache.js, js/exclusive_scan.js,
+ * js/stream_compact.js, js/radix_sort_by_key.js).  Every entry point names the
+ * reference interface it replaces.  Plain pointers and sizes only; no C++
+ * exceptions cross this boundary.  `stream` arguments are cudaStream_t values
+ * passed as void* (NULL = the context's own stream).  Device pointers are
+ * plain CUDA device addresses on the context's device.
+ *
+ * Threading: a context and the objects made from it are used by one host
+ * thread at a time.
+ */
+#ifndef BCMC_H
+#define BCMC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BCMC_ABI_VERSION 1
+
+/* Status codes.  The reference reports errors with alert()/console.log
+ * (js/lru_cache.js:315-317, js/exclusive_scan.js:117-119, js/util.js:29-31). */
+typedef enum {
+    BCMC_OK = 0,
+    BCMC_E_ARG = 1,       /* invalid argument (sizes, null pointers, rate)      */
+    BCMC_E_OOM = 2,       /* device or host allocation failed                   */
+    BCMC_E_CUDA = 3,      /* a CUDA call failed; see bcmc_last_error()          */
+    BCMC_E_TIMEOUT = 4,   /* a device-side wait hit its iteration limit         */
+    BCMC_E_ADMISSION = 5, /* a request does not fit the configured memory       */
+    BCMC_E_STATE = 6      /* call order violated (e.g. no surface computed yet) */
+} bcmc_status;
+
+typedef struct bcmc_ctx bcmc_ctx;
+typedef struct bcmc_vol bcmc_vol;
+typedef struct bcmc_lru bcmc_lru;
+
+/* Context options.  Defaults (bcmc_opts_default): device 0,
+ * initial cache 5 % of the blocks (compressed_marching_cubes.js:446). */
+typedef struct {
+    int device;                    /* CUDA device ordinal                          */
+    double initial_cache_fraction; /* LRU initial size as a fraction of blocks     */
+    uint32_t flags;                /* reserved, 0                                  */
+} bcmc_opts;
+
+void bcmc_opts_default(bcmc_opts* opts);
+
+/* ---- context ------------------------------------------------------------ */
+/* Replaces the WebGPU device handed to `new CompressedMarchingCubes(device)`
+ * (js/compressed_marching_cubes.js:1, js/bcmc.js:2-13). */
+bcmc_status bcmc_ctx_create(const bcmc_opts* opts, bcmc_ctx** out);
+void bcmc_ctx_destroy(bcmc_ctx* ctx);
+const char* bcmc_last_error(const bcmc_ctx* ctx);
+/* The context's CUDA stream (cudaStream_t as void*). */
+void* bcmc_ctx_stream(bcmc_ctx* ctx);
+/* Wait for all work the context queued. */
+bcmc_status bcmc_ctx_synchronize(bcmc_ctx* ctx);
+/* CUDA kernels this library has launched in this process (all contexts).
+ * No reference counterpart: lets callers account for the GPU work behind a
+ * call (e.g. kernels per query). */
+uint64_t bcmc_kernel_launches(void);
+
+/* ---- CompressedMarchingCubes -------------------------------------------- */
+/* setCompressedVolume(volume, compressionRate, volumeDims, volumeScale)
+ * (js/compressed_marching_cubes.js:432-520): uploads the fixed-rate ZFP stream
+ * (host bytes, 64*rate bits per 4^3 block, x-fastest block order) and computes
+ * every block's value range (computeBlockRanges, :522-578). */
+bcmc_status bcmc_volume_create(bcmc_ctx* ctx, const uint8_t* zfp, size_t len, uint32_t rate,
+                               const uint32_t dims[3], const float scale[3], bcmc_vol** out);
+/* Same, from a stream already resident on the device (copied device-to-device). */
+bcmc_status bcmc_volume_create_device(bcmc_ctx* ctx, const void* d_zfp, size_t len, uint32_t rate,
+                                      const uint32_t dims[3], const float scale[3],
+                                      bcmc_vol** out);
+void bcmc_volume_destroy(bcmc_vol* vol);
+
+/* Per-stage device times in milliseconds, keyed like the reference's
+ * perfTracker (compressed_marching_cubes.js:593-610). */
+typedef struct {
+    float computeActiveBlocks; /* active test + compaction + cache lookup        */
+    float cacheUpdate;         /* LRU age/mark/grow/sort/assign                  */
+    float decompression;       /* ZFP decode of newly needed blocks               */
+    float computeVertices;     /* MC count + scan + emit                         */
+    float total;
+} bcmc_perf;
+
+/* computeSurface(isovalue, perfTracker) -> numVertices
+ * (js/compressed_marching_cubes.js:580-809).  Blocks until the vertex count is
+ * known.  `perf` may be NULL (no per-stage timing). */
+bcmc_status bcmc_compute_surface(bcmc_vol* vol, float isovalue, bcmc_perf* perf,
+                                 uint32_t* num_vertices);
+
+/* The vertex buffer (this.vertexBuffer, :781-784): numVertices entries of
+ * 8 bytes, {uint32 packed 10:10:10 position within the block, uint32 block id}
+ * (compute_block_vertices.comp:164).  The pointer stays valid until the next
+ * bcmc_compute_surface on this volume. */
+bcmc_status bcmc_vertices(bcmc_vol* vol, const void** d_vertices, uint64_t* bytes);
+/* Copies the vertex buffer into host memory (bytes <= 8*numVertices). */
+bcmc_status bcmc_copy_vertices(bcmc_vol* vol, void* host, uint64_t bytes);
+
+/* Fields the reference object exposes to its UI (js/bcmc.js:77-100),
+ * updated at the same points of computeSurface as the reference updates them. */
+typedef struct {
+    uint32_t totalBlocks;
+    uint32_t numActiveBlocks;
+    uint32_t newDecompressed;
+    uint32_t numBlocksWithVertices;
+    uint32_t numVertices;
+    uint32_t cacheSize;                /* lruCache.cacheSize                    */
+    uint32_t displayNumSlotsAvailable; /* lruCache.displayNumSlotsAvailable     */
+    uint32_t lastNumVertices;          /* return value of the last query        */
+} bcmc_stats;
+bcmc_status bcmc_stats_get(bcmc_vol* vol, bcmc_stats* out);
+
+/* reportMemoryUse() (js/compressed_marching_cubes.js:366-430): bytes per
+ * buffer class, plus what this implementation actually holds on the device. */
+typedef struct {
+    uint64_t compressedData, vertexBuffer, blockActive, blockRanges, activeBlockIDs,
+        blocksWithVertices, blockVertexOffsets, cache, cachedItemSlots, slotData, scratch,
+        deviceTotal;
+} bcmc_memory;
+bcmc_status bcmc_memory_report(bcmc_vol* vol, bcmc_memory* out);
+
+/* lruCache.reset() (js/lru_cache.js:846-903). */
+bcmc_status bcmc_cache_reset(bcmc_vol* vol);
+
+/* Debug views of the last query (device pointers owned by the volume), used by
+ * the parity tests.  Lengths come from bcmc_stats_get / totalBlocks. */
+typedef struct {
+    const float* d_block_ranges;        /* vec2 per block                         */
+    const uint32_t* d_block_active;     /* u32 per block                          */
+    const uint32_t* d_active_block_ids; /* numActiveBlocks, ascending             */
+    const uint32_t* d_blocks_with_vertices; /* numBlocksWithVertices, indices into active ids */
+    const uint32_t* d_block_vertex_offsets; /* exclusive scan of per-block counts */
+    const uint32_t* d_new_item_ids;     /* newDecompressed, ascending             */
+    bcmc_lru* lru;                      /* the volume's cache                     */
+} bcmc_vol_views;
+bcmc_status bcmc_volume_views(bcmc_vol* vol, bcmc_vol_views* out);
+
+/* ---- LRUCache (js/lru_cache.js) ----------------------------------------- */
+/* new LRUCache(device, scan, compact, initialSize, elementSize, totalElements)
+ * (js/lru_cache.js:4-305).  elementSize must be a multiple of 4 bytes. */
+bcmc_status bcmc_lru_create(bcmc_ctx* ctx, uint32_t initial_size, uint32_t element_size,
+                            uint32_t total_elements, bcmc_lru** out);
+void bcmc_lru_destroy(bcmc_lru* lru);
+/* update(itemNeeded) -> [numNewItems, newItemIDs] (js/lru_cache.js:312-843).
+ * d_item_needed: u32 per element (1 = needed).  *d_new_item_ids stays valid
+ * until the next update. */
+bcmc_status bcmc_lru_update(bcmc_lru* lru, const uint32_t* d_item_needed, uint32_t* num_new,
+                            const uint32_t** d_new_item_ids);
+/* reset() (js/lru_cache.js:846-903). */
+bcmc_status bcmc_lru_reset(bcmc_lru* lru);
+typedef struct {
+    uint32_t cacheSize, totalElements, elementSize, displayNumSlotsAvailable;
+    const int32_t* d_cached_item_slots; /* per element: slot or -1             */
+    const uint32_t* d_slot_age;         /* per slot                            */
+    const uint32_t* d_slot_available;   /* per slot                            */
+    const int32_t* d_slot_item;         /* per slot: element or -1             */
+    void* d_cache;                      /* cacheSize * elementSize bytes       */
+    const uint32_t* d_last_sorted_slots; /* available slots, oldest first      */
+    uint32_t lastNumSlotsAvailable;
+} bcmc_lru_view;
+bcmc_status bcmc_lru_view_get(bcmc_lru* lru, bcmc_lru_view* out);
+
+/* ---- ExclusiveScanPipeline / ExclusiveScanner (js/exclusive_scan.js) ----- */
+/* getAlignedSize(n) = alignTo(n, 512) (js/exclusive_scan.js:95-97). */
+uint32_t bcmc_scan_aligned_size(uint32_t n);
+/* scanner.scan(dataSize) (js/exclusive_scan.js:178-295): in-place exclusive
+ * scan of d_data[0..n) (uint32, wrapping); when n < aligned_size, d_data[n]
+ * receives the total.  Returns the total through *total (synchronous). */
+bcmc_status bcmc_scan_exclusive_u32(bcmc_ctx* ctx, uint32_t* d_data, uint32_t n,
+                                    uint32_t aligned_size, uint32_t* total);
+/* Asynchronous form: d_out may equal d_in; the total lands in *d_total. */
+bcmc_status bcmc_scan_exclusive_u32_async(bcmc_ctx* ctx, const uint32_t* d_in, uint32_t* d_out,
+                                          uint32_t n, uint32_t* d_total, void* stream);
+
+/* ---- StreamCompact (js/stream_compact.js) ------------------------------- */
+/* compactActiveIDs(numElements, isActive, offsets, output)
+ * (js/stream_compact.js:56-165, shaders/stream_compact.comp:26-32):
+ * out[offsets[i]] = i for every i < n with flags[i] != 0. */
+bcmc_status bcmc_compact_ids(bcmc_ctx* ctx, uint32_t n, const uint32_t* d_flags,
+                             const uint32_t* d_offsets, uint32_t* d_out, void* stream);
+/* Fused scan + compaction of the ids of nonzero flags (no offsets buffer). */
+bcmc_status bcmc_select_ids(bcmc_ctx* ctx, uint32_t n, const uint32_t* d_flags, uint32_t* d_out,
+                            uint32_t* d_count, void* stream);
+
+/* ---- RadixSorter (js/radix_sort_by_key.js) ------------------------------ */
+/* getAlignedSize(n) = nextPow2(ceil(n/64))*64 (js/radix_sort_by_key.js:155-158). */
+uint32_t bcmc_sort_aligned_size(uint32_t n);
+/* sort(keys, values, size, reverse) (js/radix_sort_by_key.js:161-400): sorts
+ * the (key, value) pairs d_keys/d_values[0..n) in place, ascending by key, or
+ * descending when reverse != 0, with the reference's order among equal keys
+ * (ascending: later 64-element chunks first, index order within a chunk;
+ * descending: earlier chunks first, reverse index order within a chunk).
+ * Keys equal to 0xFFFFFFFF are ordered by that rule too (the reference pads
+ * with that value). */
+bcmc_status bcmc_sort_pairs_u32(bcmc_ctx* ctx, uint32_t* d_keys, uint32_t* d_values, uint32_t n,
+                                int reverse, void* stream);
+
+/* ---- ZFP fixed-rate float32 codec (shaders/zfp_decompress.comp) ---------- */
+/* zfp_compute_block_range.comp:19-61: vec2(min,max) of every block over the
+ * voxels inside dims. */
+bcmc_status bcmc_zfp_block_ranges(bcmc_ctx* ctx, const uint64_t* d_words, const uint32_t dims[3],
+                                  uint32_t rate, float* d_ranges, void* stream);
+/* zfp_decompress_block.comp:29-39: decode block d_block_ids[i] into
+ * d_cache[64*d_item_slots[d_block_ids[i]] ...] for i < n. */
+bcmc_status bcmc_zfp_decode_blocks(bcmc_ctx* ctx, const uint64_t* d_words, uint32_t rate,
+                                   const uint32_t* d_block_ids, uint32_t n,
+                                   const int32_t* d_item_slots, float* d_cache, void* stream);
+/* Decode every block into d_out[64*b ...] (block order). */
+bcmc_status bcmc_zfp_decode_volume(bcmc_ctx* ctx, const uint64_t* d_words, uint64_t nblocks,
+                                   uint32_t rate, float* d_out, void* stream);
+/* Fixed-rate encoder (no counterpart in the reference, which only decodes):
+ * d_field is float32 x-fastest of dims; writes bcmc_zfp_stream_words() words. */
+uint64_t bcmc_zfp_stream_words(const uint32_t dims[3], uint32_t rate);
+bcmc_status bcmc_zfp_encode(bcmc_ctx* ctx, const float* d_field, const uint32_t dims[3],
+                            uint32_t rate, uint64_t* d_words, void* stream);
+
+/* compute_block_active.comp:24-61: u32 active flag per block. */
+bcmc_status bcmc_block_active(bcmc_ctx* ctx, const float* d_ranges, const uint32_t dims[3],
+                              float isovalue, uint32_t* d_active, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

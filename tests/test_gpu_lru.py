@@ -1,0 +1,59 @@
+"""LRUCache drop-in on the GPU vs the oracle: new items, slot assignment (with
+the reference's tie order among equal ages), ages, availability, growth and
+reset, after every update."""
+import numpy as np
+import pytest
+
+import bcmc
+from gpu_util import to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+
+
+def _compare(c_gpu, c_ref, total):
+    g = c_gpu.state()
+    r = c_ref.state()
+    assert g["cache_size"] == c_ref.cache_size
+    assert np.array_equal(g["item_slots"][:total], r["item_slots"][:total])
+    assert np.array_equal(g["age"], r["age"])
+    assert np.array_equal(g["avail"], r["avail"])
+    assert np.array_equal(g["item"], r["item"])
+
+
+@pytest.mark.parametrize("total,initial,steps", [(300, 20, 40), (5000, 64, 30), (70000, 3500, 12),
+                                                 (262144, 13107, 6)])
+def test_lru_sequence_matches_oracle(ctx, oracle, total, initial, steps):
+    rs = np.random.default_rng(total)
+    g = bcmc.LRUCache(ctx, None, None, initial, 256, total)
+    r = oracle.LRUCache(initial, total)
+    for step in range(steps):
+        if step == steps - 3:
+            g.reset()
+            r.reset()
+        p = rs.uniform(0.01, 0.4)
+        # spatially coherent needs: runs of needed items, as active blocks are
+        needed = (np.convolve(rs.random(total) < p / 8, np.ones(8), mode="same") > 0).astype(np.uint32)
+        if step % 7 == 3:
+            needed[:] = 0
+        n_gpu, ids = g.update(to_dev(needed))
+        ref_ids = r.update(needed)
+        assert n_gpu == len(ref_ids), step
+        if n_gpu:
+            assert np.array_equal(ids.numpy(), ref_ids), step
+            assert g.displayNumSlotsAvailable == r.slots_available
+        _compare(g, r, total)
+
+
+def test_lru_ties_after_reset(ctx, oracle):
+    """After reset every slot has age 100000: assignment order is then the
+    reference's tie order (64-chunks ascending, slots descending inside)."""
+    total = 4000
+    g = bcmc.LRUCache(ctx, None, None, 1000, 256, total)
+    r = oracle.LRUCache(1000, total)
+    g.reset()
+    r.reset()
+    needed = np.zeros(total, np.uint32)
+    needed[::3] = 1
+    n, ids = g.update(to_dev(needed))
+    assert np.array_equal(ids.numpy(), r.update(needed))
+    _compare(g, r, total)

@@ -1,0 +1,102 @@
+"""CompressedMarchingCubes on the GPU vs the oracle's plain one-query-at-a-time
+pipeline: every query's vertex buffer bit for bit, plus ranges, active flags,
+active/with-vertex block lists, vertex offsets, cache state and statistics."""
+import numpy as np
+import pytest
+
+import bcmc
+from bcmc import datasets as D
+from gpu_util import bits
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(ctx, oracle, field, dims, rate, isos, cache_fraction, check_state=True, reset_at=None):
+    w = oracle.zfp_encode(field, rate)
+    ref = oracle.CompressedMarchingCubes(w, rate, dims, initial_cache_fraction=cache_fraction)
+    c = bcmc.Context(ctx.device, initial_cache_fraction=cache_fraction)
+    mc = bcmc.CompressedMarchingCubes(c)
+    mc.setCompressedVolume(w.view(np.uint8)[: (int(np.prod(oracle.padded_blocks(dims))) * 64 * rate + 7) // 8],
+                           rate, dims)
+    v = mc.views()
+    assert np.array_equal(bits(v["ranges"].numpy()), bits(ref.ranges()))
+    for qi, iso in enumerate(isos):
+        if reset_at is not None and qi == reset_at:
+            mc.lruCache.reset()
+            ref.cache_reset()
+        n_ref = ref.compute_surface(float(iso))
+        n = mc.computeSurface(float(iso))
+        assert n == n_ref, (qi, iso)
+        got = mc.copyVertices()
+        assert np.array_equal(got, ref.vertices(n_ref)), (qi, iso)
+        st, rs = mc.stats(), ref.stats()
+        for k in ("numActiveBlocks", "newDecompressed", "numBlocksWithVertices", "numVertices", "cacheSize"):
+            assert st[k] == rs[k], (qi, k, st[k], rs[k])
+        if check_state:
+            v = mc.views()
+            assert np.array_equal(v["active"].numpy(), ref.active())
+            if rs["numActiveBlocks"] and n_ref:
+                assert np.array_equal(v["active_ids"].numpy(), ref.active_ids(rs["numActiveBlocks"]))
+                assert np.array_equal(v["with_verts"].numpy(), ref.with_verts(rs["numBlocksWithVertices"]))
+                assert np.array_equal(v["vert_offsets"].numpy(), ref.vert_offsets(rs["numBlocksWithVertices"]))
+            g = mc.lruCache.state()
+            r = ref.lru_state()
+            assert g["cache_size"] == r["cache_size"]
+            for k in ("item_slots", "age", "avail", "item"):
+                assert np.array_equal(g[k], r[k]), (qi, k)
+    return mc, ref
+
+
+def test_blobs64_single_query(ctx, oracle):
+    """64^3 Gaussian blobs, rate 8, iso 0.5, cache large enough for all blocks."""
+    f = D.blobs((64, 64, 64), 1)
+    mc, _ = _run(ctx, oracle, f, (64, 64, 64), 8, [0.5], 1.0)
+    assert mc.numVertices > 0
+
+
+def test_blobs64_sweep_small_cache(ctx, oracle):
+    f = D.blobs((64, 64, 64), 1)
+    isos = list(np.linspace(0.1, 1.0, 12)) + [5.0, 0.5, -1.0, 0.5]
+    _run(ctx, oracle, f, (64, 64, 64), 8, isos, 0.05, reset_at=9)
+
+
+@pytest.mark.parametrize("dims", [(61, 47, 53), (17, 5, 33), (4, 4, 4), (5, 5, 5)])
+def test_partial_blocks(ctx, oracle, dims):
+    f = D.blobs(dims, 8, n_blobs=5)
+    isos = np.linspace(float(f.min()), float(f.max()), 7)
+    _run(ctx, oracle, f, dims, 4, isos, 0.05)
+
+
+def test_ct_like_96(ctx, oracle):
+    f = D.ct_like((96, 96, 96), 2)
+    _run(ctx, oracle, f, (96, 96, 96), 4, np.linspace(30.0, 220.0, 16), 0.5)
+
+
+def test_turbulence_random_walk(ctx, oracle):
+    f = D.turbulence((64, 64, 64), 3)
+    _run(ctx, oracle, f, (64, 64, 64), 2, D.random_walk(24, 3), 0.25)
+
+
+def test_ct256_config(ctx, oracle):
+    """The 256^3 CT-like configuration: rate 4, 16 isovalues in [30, 220],
+    cache 50 % of the blocks."""
+    f = D.ct_like((256, 256, 256), 2)
+    _run(ctx, oracle, f, (256, 256, 256), 4, np.linspace(30.0, 220.0, 16), 0.5, check_state=False)
+
+
+def test_empty_and_full_queries(ctx, oracle):
+    f = D.blobs((32, 32, 32), 4)
+    _run(ctx, oracle, f, (32, 32, 32), 4, [1e9, -1e9, float(np.median(f)), 1e9], 0.05)
+
+
+def test_perf_tracker_and_memory_report(ctx, oracle):
+    f = D.blobs((32, 32, 32), 4)
+    w = oracle.zfp_encode(f, 4)
+    mc = bcmc.CompressedMarchingCubes(ctx)
+    mc.setCompressedVolume(w, 4, (32, 32, 32))
+    perf = {}
+    for iso in (float(np.median(f)), float(f.max()) + 1):
+        mc.computeSurface(iso, perf)
+    assert len(perf["computeVertices"]) == 2 and perf["totalBlocks"] == 512
+    mc_text, cache_text, total, use = mc.reportMemoryUse()
+    assert "compressedData" in mc_text and "cache" in cache_text and use["cache"]["cache"] > 0

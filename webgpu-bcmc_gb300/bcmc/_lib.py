@@ -1,0 +1,139 @@
+"""ctypes binding of libbcmc_gb300.so (the C ABI in include/bcmc.h).
+
+The shared library is the product; this module only declares its entry points.
+Loading fails loudly when the library has not been built: there is no CPU
+fallback behind it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_ROOT, "_build", "libbcmc_gb300.so")
+HEADER = os.path.join(os.path.dirname(PKG_ROOT), "include", "bcmc.h")
+
+BCMC_OK = 0
+STATUS_NAMES = {0: "BCMC_OK", 1: "BCMC_E_ARG", 2: "BCMC_E_OOM", 3: "BCMC_E_CUDA", 4: "BCMC_E_TIMEOUT",
+                5: "BCMC_E_ADMISSION", 6: "BCMC_E_STATE"}
+
+
+class bcmc_opts(C.Structure):
+    _fields_ = [("device", C.c_int), ("initial_cache_fraction", C.c_double), ("flags", C.c_uint32)]
+
+
+class bcmc_perf(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("computeActiveBlocks", "cacheUpdate", "decompression",
+                                          "computeVertices", "total")]
+
+
+class bcmc_stats(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in ("totalBlocks", "numActiveBlocks", "newDecompressed",
+                                           "numBlocksWithVertices", "numVertices", "cacheSize",
+                                           "displayNumSlotsAvailable", "lastNumVertices")]
+
+
+class bcmc_memory(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("compressedData", "vertexBuffer", "blockActive", "blockRanges",
+                                           "activeBlockIDs", "blocksWithVertices", "blockVertexOffsets",
+                                           "cache", "cachedItemSlots", "slotData", "scratch", "deviceTotal")]
+
+
+class bcmc_vol_views(C.Structure):
+    _fields_ = [("d_block_ranges", C.c_void_p), ("d_block_active", C.c_void_p),
+                ("d_active_block_ids", C.c_void_p), ("d_blocks_with_vertices", C.c_void_p),
+                ("d_block_vertex_offsets", C.c_void_p), ("d_new_item_ids", C.c_void_p), ("lru", C.c_void_p)]
+
+
+class bcmc_lru_view(C.Structure):
+    _fields_ = [("cacheSize", C.c_uint32), ("totalElements", C.c_uint32), ("elementSize", C.c_uint32),
+                ("displayNumSlotsAvailable", C.c_uint32), ("d_cached_item_slots", C.c_void_p),
+                ("d_slot_age", C.c_void_p), ("d_slot_available", C.c_void_p), ("d_slot_item", C.c_void_p),
+                ("d_cache", C.c_void_p), ("d_last_sorted_slots", C.c_void_p),
+                ("lastNumSlotsAvailable", C.c_uint32)]
+
+
+P = C.c_void_p
+U32 = C.c_uint32
+U64 = C.c_uint64
+U32P = C.POINTER(C.c_uint32)
+
+# name -> (restype, argtypes); mirrors include/bcmc.h
+SIGNATURES = {
+    "bcmc_opts_default": (None, [C.POINTER(bcmc_opts)]),
+    "bcmc_ctx_create": (C.c_int, [C.POINTER(bcmc_opts), C.POINTER(P)]),
+    "bcmc_ctx_destroy": (None, [P]),
+    "bcmc_last_error": (C.c_char_p, [P]),
+    "bcmc_ctx_stream": (P, [P]),
+    "bcmc_ctx_synchronize": (C.c_int, [P]),
+    "bcmc_kernel_launches": (U64, []),
+    "bcmc_volume_create": (C.c_int, [P, P, C.c_size_t, U32, U32P, C.POINTER(C.c_float), C.POINTER(P)]),
+    "bcmc_volume_create_device": (C.c_int, [P, P, C.c_size_t, U32, U32P, C.POINTER(C.c_float), C.POINTER(P)]),
+    "bcmc_volume_destroy": (None, [P]),
+    "bcmc_compute_surface": (C.c_int, [P, C.c_float, C.POINTER(bcmc_perf), U32P]),
+    "bcmc_vertices": (C.c_int, [P, C.POINTER(P), C.POINTER(U64)]),
+    "bcmc_copy_vertices": (C.c_int, [P, P, U64]),
+    "bcmc_stats_get": (C.c_int, [P, C.POINTER(bcmc_stats)]),
+    "bcmc_memory_report": (C.c_int, [P, C.POINTER(bcmc_memory)]),
+    "bcmc_cache_reset": (C.c_int, [P]),
+    "bcmc_volume_views": (C.c_int, [P, C.POINTER(bcmc_vol_views)]),
+    "bcmc_lru_create": (C.c_int, [P, U32, U32, U32, C.POINTER(P)]),
+    "bcmc_lru_destroy": (None, [P]),
+    "bcmc_lru_update": (C.c_int, [P, P, U32P, C.POINTER(P)]),
+    "bcmc_lru_reset": (C.c_int, [P]),
+    "bcmc_lru_view_get": (C.c_int, [P, C.POINTER(bcmc_lru_view)]),
+    "bcmc_scan_aligned_size": (U32, [U32]),
+    "bcmc_scan_exclusive_u32": (C.c_int, [P, P, U32, U32, U32P]),
+    "bcmc_scan_exclusive_u32_async": (C.c_int, [P, P, P, U32, P, P]),
+    "bcmc_compact_ids": (C.c_int, [P, U32, P, P, P, P]),
+    "bcmc_select_ids": (C.c_int, [P, U32, P, P, P, P]),
+    "bcmc_sort_aligned_size": (U32, [U32]),
+    "bcmc_sort_pairs_u32": (C.c_int, [P, P, P, U32, C.c_int, P]),
+    "bcmc_zfp_block_ranges": (C.c_int, [P, P, U32P, U32, P, P]),
+    "bcmc_zfp_decode_blocks": (C.c_int, [P, P, U32, P, U32, P, P, P]),
+    "bcmc_zfp_decode_volume": (C.c_int, [P, P, U64, U32, P, P]),
+    "bcmc_zfp_stream_words": (U64, [U32P, U32]),
+    "bcmc_zfp_encode": (C.c_int, [P, P, U32P, U32, P, P]),
+    "bcmc_block_active": (C.c_int, [P, P, U32P, C.c_float, P, P]),
+}
+
+_lib = None
+
+
+class BcmcError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {message}")
+        self.code = code
+
+
+def load():
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with `python webgpu-bcmc_gb300/build.py` "
+                              "(there is no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        for name, (rt, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = rt
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(code: int, ctx=None) -> None:
+    if code != BCMC_OK:
+        msg = ""
+        if ctx:
+            raw = load().bcmc_last_error(ctx)
+            msg = raw.decode() if raw else ""
+        raise BcmcError(code, msg)
+
+
+def dims3(dims) -> C.Array:
+    return (C.c_uint32 * 3)(*[int(d) for d in dims])
+
+
+def scale3(scale) -> C.Array:
+    return (C.c_float * 3)(*[float(s) for s in scale])

@@ -1,0 +1,186 @@
+// bcmc_internal.cuh -- shared device/host helpers of libbcmc_gb300 (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/bcmc.h"
+
+namespace bcmc {
+
+constexpr int kWarp = 32;
+constexpr uint32_t kSpinLimit = 1u << 22;  // bounded device-side waits
+
+// ---------------------------------------------------------------------------
+// Per-query device state.  Every count the pipeline needs lives here so that a
+// query is a fixed sequence of launches with no host round trip in between;
+// the host reads this struct once at the end of the query.
+// ---------------------------------------------------------------------------
+struct QueryState {
+    // inputs written by the host (or the query-init kernel)
+    float isovalue;
+    uint32_t epoch;          // tags the decoupled-lookback status words
+    uint32_t capacity;       // physical slots of the cache buffers
+    uint32_t cache_size;     // logical LRU size (js/lru_cache.js cacheSize)
+    uint32_t vert_capacity;  // entries of the vertex buffer
+    // active-block pass
+    uint32_t num_active;
+    uint32_t num_new;
+    uint32_t old_cache_size;
+    uint32_t new_cache_size;
+    // LRU slot pass
+    uint32_t num_avail;
+    uint32_t display_slots_available;
+    // marching cubes
+    uint32_t num_with_verts;
+    uint32_t num_verts;
+    // flags
+    uint32_t grow_needed;    // cache capacity exceeded: host grows and re-runs
+    uint32_t vert_overflow;  // vertex buffer too small: host grows, re-runs MC
+    uint32_t error;          // nonzero: a bounded wait timed out (code = site)
+    // dynamic tile counters (zeroed by the init kernel)
+    uint32_t tiles_active;
+    uint32_t tiles_slots;
+    uint32_t tiles_mc;
+    uint32_t tiles_sort[4];
+    uint32_t tiles_sort_hist;
+    // radix sort plan (written by the histogram kernel)
+    uint32_t sort_src[4];     // source buffer (0/1) of each digit pass
+    uint32_t sort_run[4];     // 1 if the digit pass runs
+    uint32_t sort_first;      // index of the first pass that runs (4 = none)
+    uint32_t sort_final;      // buffer holding the sorted values
+    uint32_t sort_hist[4][256];
+    uint32_t pad[8];
+};
+
+// ---------------------------------------------------------------------------
+// Decoupled look-back status words: [epoch:30 | flag:2][value:32].
+// flag 1 = tile aggregate, 2 = inclusive prefix.  Words from an older epoch read
+// as "not ready", so the arrays need no clearing between launches.
+// ---------------------------------------------------------------------------
+constexpr uint64_t kFlagAggregate = 1;
+constexpr uint64_t kFlagPrefix = 2;
+
+__device__ __forceinline__ uint64_t lb_pack(uint32_t epoch, uint64_t flag, uint32_t value)
+{
+    return ((((uint64_t)epoch << 2) | flag) << 32) | value;
+}
+
+__device__ __forceinline__ void lb_store(uint64_t* p, uint64_t v)
+{
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ uint64_t lb_load(const uint64_t* p)
+{
+    uint64_t v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p)
+{
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Single-thread look-back over tiles [0, tile) of one counter whose status
+// word for tile i sits at status[i * stride].  Publishes the tile's aggregate
+// (tile > 0), accumulates predecessors until an inclusive prefix is found,
+// then publishes its own inclusive prefix.  Returns the exclusive prefix.  A
+// wait that exceeds kSpinLimit records `site` in *err and stops the walk, so
+// the kernel always finishes (the host reports BCMC_E_TIMEOUT).
+__device__ __forceinline__ uint32_t lookback_exclusive(uint64_t* status, uint32_t tile,
+                                                       uint32_t aggregate, uint32_t epoch,
+                                                       uint32_t* err, uint32_t site,
+                                                       uint32_t stride = 1)
+{
+    if (tile == 0) {
+        lb_store(status, lb_pack(epoch, kFlagPrefix, aggregate));
+        return 0;
+    }
+    lb_store(status + (uint64_t)tile * stride, lb_pack(epoch, kFlagAggregate, aggregate));
+    uint32_t exclusive = 0;
+    int64_t t = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    while (t >= 0) {
+        const uint64_t s = lb_load(status + (uint64_t)t * stride);
+        const uint32_t hi = (uint32_t)(s >> 32);
+        if ((hi >> 2) != epoch || (hi & 3u) == 0) {
+            if (++spins > kSpinLimit) {
+                atomicCAS(err, 0u, site);
+                break;
+            }
+            if (spins > 32) __nanosleep(100);
+            continue;
+        }
+        exclusive += (uint32_t)s;
+        if ((hi & 3u) == kFlagPrefix) break;
+        --t;
+    }
+    lb_store(status + (uint64_t)tile * stride, lb_pack(epoch, kFlagPrefix, exclusive + aggregate));
+    return exclusive;
+}
+
+// Warp-wide inclusive scan (shuffles).
+__device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t n = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += n;
+    }
+    return v;
+}
+
+// CTA-wide exclusive scan of one value per thread; returns the exclusive
+// prefix and writes the CTA total to *total.  `warp_sums` holds blockDim/32
+// entries of shared memory.
+template <int kThreads>
+__device__ __forceinline__ uint32_t cta_exclusive_scan(uint32_t v, uint32_t* warp_sums, uint32_t* total)
+{
+    constexpr int kWarps = kThreads / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t inc = warp_inclusive_scan(v);
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < kWarps ? warp_sums[lane] : 0;
+        const uint32_t wi = warp_inclusive_scan(w);
+        if (lane < kWarps) warp_sums[lane] = wi - w;
+        if (lane == kWarps - 1) warp_sums[kWarps] = wi;
+    }
+    __syncthreads();
+    const uint32_t r = warp_sums[warp] + inc - v;
+    *total = warp_sums[kWarps];
+    __syncthreads();
+    return r;
+}
+
+__host__ __device__ __forceinline__ uint32_t align_up(uint32_t v, uint32_t a)
+{
+    return (uint32_t)(((uint64_t)v + a - 1) / a * a);
+}
+
+__host__ __device__ __forceinline__ uint32_t div_up(uint32_t v, uint32_t a)
+{
+    return (uint32_t)(((uint64_t)v + a - 1) / a);
+}
+
+// Error helper for host code.
+struct CudaError {
+    cudaError_t err;
+    const char* what;
+};
+
+}  // namespace bcmc
+
+#define BCMC_CUDA(call)                                                       \
+    do {                                                                      \
+        cudaError_t e_ = (call);                                              \
+        if (e_ != cudaSuccess) throw ::bcmc::CudaError{e_, #call};            \
+    } while (0)

@@ -1,0 +1,70 @@
+// bcmc_pipeline.h -- argument blocks and launchers of the query pipeline
+// kernels (pipeline.cu).  Internal to libbcmc_gb300.
+#pragma once
+
+#include "bcmc_impl.h"
+
+namespace bcmc {
+
+struct ActiveArgs {
+    const float2* ranges;     // set: test ranges against the isovalue (MC path)
+    uint3 nb;                 // blocks per axis
+    const uint32_t* item_needed;  // set instead of ranges: standalone LRU update
+    uint32_t* active_out;     // per-block active flags (MC path)
+    const int32_t* item_slots;  // cachedItemSlots
+    uint32_t total;           // blocks / items
+    uint32_t* active_ids;     // compacted active ids (nullable)
+    uint32_t* new_ids;        // compacted ids that need caching
+    uint64_t* status_a;
+    uint64_t* status_n;
+};
+
+struct SlotArgs {
+    const uint32_t* needed;   // per item: 1 if needed this update
+    uint32_t* slot_age;
+    uint32_t* slot_avail;
+    int32_t* slot_item;
+    uint32_t* avail_ids;      // compacted available slots (ascending)
+    uint32_t* avail_keys;     // their ages
+    uint64_t* status;
+    // computeSurface skips the cache update when no block is active
+    // (compressed_marching_cubes.js:630-641); LRUCache.update itself always ages
+    uint32_t skip_when_inactive;
+};
+
+struct AssignArgs {
+    const uint32_t* new_ids;
+    const uint32_t* sorted_b;  // sorted slot ids in sort buffer b or c
+    const uint32_t* sorted_c;
+    uint32_t* slot_age;
+    uint32_t* slot_avail;
+    int32_t* slot_item;
+    int32_t* item_slots;
+    const uint64_t* words;    // set: decode each new block into its slot
+    uint32_t max_bits;
+    float* cache;
+};
+
+struct McArgs {
+    const uint32_t* active;
+    const uint32_t* active_ids;
+    const int32_t* item_slots;
+    const float* cache;
+    uint3 nb;
+    uint32_t* with_verts;
+    uint32_t* vert_offsets;
+    uint2* verts;
+    uint64_t* status_v;
+    uint64_t* status_b;
+};
+
+void query_begin_launch(QueryState* q, float iso, int mc_only, uint32_t capacity, uint32_t vert_capacity,
+                        cudaStream_t s);
+void active_launch(bcmc_ctx* ctx, QueryState* q, const ActiveArgs& a, cudaStream_t s);
+void slots_launch(bcmc_ctx* ctx, QueryState* q, const SlotArgs& a, uint32_t max_slots, cudaStream_t s);
+void assign_launch(bcmc_ctx* ctx, QueryState* q, const AssignArgs& a, uint32_t max_new, cudaStream_t s);
+void mc_launch(bcmc_ctx* ctx, QueryState* q, const McArgs& a, uint32_t max_active, cudaStream_t s);
+uint32_t active_tiles(uint32_t total);
+uint32_t mc_tiles(uint32_t total);
+
+}  // namespace bcmc

@@ -1,0 +1,238 @@
+// sort.cu -- onesweep LSD radix sort of (uint32 key, uint32 value) pairs.
+//
+// Replaces RadixSorter.sort (js/radix_sort_by_key.js:161-400): the reference
+// sorts 64-element chunks with 32 one-bit splits (radix_sort_chunk.comp), merges
+// them pairwise log2(chunks) times (merge_sorted_chunks.comp, where elements of
+// the right half come first among equal keys, :82-86) and, for a descending
+// sort, reverses the result (reverse_buffer.comp).  That fixes the order among
+// equal keys:
+//   ascending : key asc,  then chunk (index/64) desc, then index asc
+//   descending: key desc, then chunk asc,             then index desc
+// Here one stable LSD radix sort reproduces it: the first pass reads the input
+// through a permutation that lists the elements in that tie order, and sorts
+// ~key for a descending sort.
+//
+// Kernels: a histogram/plan kernel (all four 8-bit digit histograms in one
+// read, exclusive bucket offsets, and which digit passes can be skipped because
+// every key shares the digit), then one onesweep pass per digit: tiles of 4096
+// keys are ranked with warp match/popc, each tile publishes its 256 digit
+// counts through decoupled look-back, and keys are scattered via shared memory
+// so that global writes come out in runs.
+#include "bcmc_impl.h"
+
+namespace bcmc {
+
+// Sequence position q -> input index p giving the reference's tie order.
+__device__ __forceinline__ uint32_t tie_perm(uint32_t q, uint32_t n, int reverse)
+{
+    const uint32_t chunks = (n + 63u) >> 6;
+    const uint32_t last_len = n - 64u * (chunks - 1u);
+    if (reverse) {
+        const uint32_t c = q >> 6, r = q & 63u;
+        const uint32_t len = (c == chunks - 1u) ? last_len : 64u;
+        return 64u * c + (len - 1u - r);
+    }
+    if (q < last_len) return 64u * (chunks - 1u) + q;
+    const uint32_t qq = q - last_len;
+    return 64u * (chunks - 2u - (qq >> 6)) + (qq & 63u);
+}
+
+__global__ void __launch_bounds__(256) k_sort_hist(QueryState* q, const uint32_t* d_n, uint32_t n_host,
+                                                   const uint32_t* __restrict__ keys, int reverse)
+{
+    __shared__ uint32_t h[4 * 256];
+    __shared__ uint32_t warp_sums[9];
+    __shared__ bool is_last;
+    const uint32_t n = d_n ? *d_n : n_host;
+    for (int i = threadIdx.x; i < 1024; i += 256) h[i] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * 256u + threadIdx.x; i < n; i += gridDim.x * 256u) {
+        uint32_t k = keys[i];
+        if (reverse) k = ~k;
+        atomicAdd(&h[k & 255u], 1u);
+        atomicAdd(&h[256 + ((k >> 8) & 255u)], 1u);
+        atomicAdd(&h[512 + ((k >> 16) & 255u)], 1u);
+        atomicAdd(&h[768 + (k >> 24)], 1u);
+    }
+    __syncthreads();
+    uint32_t* gh = &q->sort_hist[0][0];
+    for (int i = threadIdx.x; i < 1024; i += 256)
+        if (h[i]) atomicAdd(gh + i, h[i]);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = atomicAdd(&q->tiles_sort_hist, 1u) == gridDim.x - 1u;
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    // plan: which digit passes run, bucket offsets, buffer ping-pong
+    uint32_t run[4];
+    for (int d = 0; d < 4; ++d) {
+        const uint32_t v = __ldcg(gh + d * 256 + threadIdx.x);
+        const int full = __syncthreads_or(n > 0 && v == n);
+        run[d] = (n > 0 && !full) ? 1u : 0u;
+        uint32_t tot;
+        const uint32_t ex = cta_exclusive_scan<256>(v, warp_sums, &tot);
+        gh[d * 256 + threadIdx.x] = ex;
+    }
+    if (threadIdx.x == 0) {
+        if (n > 0 && !(run[0] | run[1] | run[2] | run[3])) run[0] = 1;  // permutation still applies
+        uint32_t cur = 0, first = 4;
+        for (int d = 0; d < 4; ++d) {
+            q->sort_run[d] = run[d];
+            q->sort_src[d] = cur;
+            if (run[d]) {
+                if (first == 4) first = d;
+                cur = (cur == 1u) ? 2u : 1u;
+            }
+        }
+        q->sort_first = first;
+        q->sort_final = cur == 0 ? 1u : cur;
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_sort_pass(QueryState* q, const uint32_t* d_n, uint32_t n_host,
+                                                            SortBuffers b, int reverse, int pass)
+{
+    __shared__ uint32_t s_keys[kSortTile];
+    __shared__ uint32_t s_vals[kSortTile];
+    __shared__ uint32_t s_whist[kSortThreads / 32][256];
+    __shared__ uint32_t s_start[256];
+    __shared__ uint32_t s_gbase[256];
+    __shared__ uint32_t s_warp_sums[kSortThreads / 32 + 1];
+    __shared__ uint32_t s_tile;
+
+    if (!q->sort_run[pass]) return;
+    const uint32_t n = d_n ? *d_n : n_host;
+    const uint32_t src = q->sort_src[pass];
+    const uint32_t* __restrict__ ks = src == 0 ? b.in_keys : (src == 1 ? b.b_keys : b.c_keys);
+    const uint32_t* __restrict__ vs = src == 0 ? b.in_vals : (src == 1 ? b.b_vals : b.c_vals);
+    uint32_t* __restrict__ kd = src == 1 ? b.c_keys : b.b_keys;
+    uint32_t* __restrict__ vd = src == 1 ? b.c_vals : b.b_vals;
+    const bool gather = src == 0;
+    const uint32_t shift = 8u * (uint32_t)pass;
+    const uint32_t epoch = q->epoch * 4u + (uint32_t)pass;
+    const uint32_t ntiles = div_up(n, kSortTile);
+    const uint32_t* bucket = q->sort_hist[pass];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(&q->tiles_sort[pass], 1u);
+        for (int i = threadIdx.x; i < (kSortThreads / 32) * 256; i += kSortThreads) (&s_whist[0][0])[i] = 0;
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        if (tile >= ntiles) break;
+
+        uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+        const uint32_t base = tile * kSortTile + (uint32_t)warp * (32u * kSortItems);
+#pragma unroll
+        for (int j = 0; j < kSortItems; ++j) {
+            const uint32_t qi = base + 32u * j + lane;
+            key[j] = 0;
+            val[j] = 0;
+            if (qi < n) {
+                const uint32_t p = gather ? tie_perm(qi, n, reverse) : qi;
+                uint32_t k = ks[p];
+                if (gather && reverse) k = ~k;
+                key[j] = k;
+                val[j] = vs[p];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kSortItems; ++j) {
+            const uint32_t qi = base + 32u * j + lane;
+            const uint32_t digit = qi < n ? (key[j] >> shift) & 255u : 256u;
+            const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+            const uint32_t cnt = digit < 256u ? s_whist[warp][digit] : 0u;
+            __syncwarp();
+            if (digit < 256u && lane == __ffs(peers) - 1) s_whist[warp][digit] = cnt + __popc(peers);
+            __syncwarp();
+            rank[j] = cnt + __popc(peers & lt_mask);
+        }
+        __syncthreads();
+        // thread t owns digit t: warp-exclusive offsets and the tile count
+        const uint32_t t = threadIdx.x;
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < kSortThreads / 32; ++w) {
+            const uint32_t c = s_whist[w][t];
+            s_whist[w][t] = run;
+            run += c;
+        }
+        uint32_t tile_total;
+        const uint32_t start = cta_exclusive_scan<kSortThreads>(run, s_warp_sums, &tile_total);
+        s_start[t] = start;
+        const uint32_t excl = lookback_exclusive(b.status + t, tile, run, epoch, &q->error, 20u + pass, 256u);
+        s_gbase[t] = bucket[t] + excl - start;
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kSortItems; ++j) {
+            const uint32_t qi = base + 32u * j + lane;
+            if (qi < n) {
+                const uint32_t d = (key[j] >> shift) & 255u;
+                const uint32_t pos = s_start[d] + s_whist[warp][d] + rank[j];
+                s_keys[pos] = key[j];
+                s_vals[pos] = val[j];
+            }
+        }
+        __syncthreads();
+        const uint32_t count = min((uint32_t)kSortTile, n - tile * kSortTile);
+        for (uint32_t i = threadIdx.x; i < count; i += kSortThreads) {
+            const uint32_t k = s_keys[i];
+            const uint32_t pos = s_gbase[(k >> shift) & 255u] + i;
+            if (pos < n) {  // always true unless a look-back wait timed out
+                kd[pos] = k;
+                vd[pos] = s_vals[i];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_sort_writeback(QueryState* q, const uint32_t* d_n, uint32_t n_host, SortBuffers b,
+                                 uint32_t* keys, uint32_t* vals, int reverse)
+{
+    const uint32_t n = d_n ? *d_n : n_host;
+    const uint32_t f = q->sort_final;
+    const uint32_t* ks = f == 1 ? b.b_keys : b.c_keys;
+    const uint32_t* vs = f == 1 ? b.b_vals : b.c_vals;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = ks[i];
+        keys[i] = reverse ? ~k : k;
+        vals[i] = vs[i];
+    }
+}
+
+size_t sort_status_words(uint32_t n_max) { return (size_t)div_up(n_max ? n_max : 1, kSortTile) * 256u; }
+
+int sort_grid(bcmc_ctx* ctx, uint32_t n_max)
+{
+    const uint32_t tiles = div_up(n_max ? n_max : 1, kSortTile);
+    const uint32_t resident = (uint32_t)ctx->num_sms * 3u;
+    return (int)(tiles < resident ? tiles : resident);
+}
+
+void sort_launch(bcmc_ctx* ctx, QueryState* q, const uint32_t* d_n, uint32_t n_max,
+                 const SortBuffers& bufs, int reverse, cudaStream_t s)
+{
+    const int hist_grid = (int)min(div_up(n_max ? n_max : 1, 256u * 8u), (uint32_t)ctx->num_sms * 4u);
+    k_sort_hist<<<hist_grid, 256, 0, s>>>(q, d_n, n_max, bufs.in_keys, reverse);
+    count_launches(1);
+    const int grid = sort_grid(ctx, n_max);
+    for (int pass = 0; pass < 4; ++pass)
+        k_sort_pass<<<grid, kSortThreads, 0, s>>>(q, d_n, n_max, bufs, reverse, pass);
+    count_launches(4);
+    BCMC_CUDA(cudaGetLastError());
+}
+
+void sort_writeback(bcmc_ctx* ctx, QueryState* q, const uint32_t* d_n, uint32_t n_max,
+                    const SortBuffers& bufs, uint32_t* keys, uint32_t* vals, int reverse,
+                    cudaStream_t s)
+{
+    const int grid = (int)min(div_up(n_max ? n_max : 1, 256u), (uint32_t)ctx->num_sms * 8u);
+    k_sort_writeback<<<grid, 256, 0, s>>>(q, d_n, n_max, bufs, keys, vals, reverse);
+    count_launches(1);
+    BCMC_CUDA(cudaGetLastError());
+}
+
+}  // namespace bcmc
