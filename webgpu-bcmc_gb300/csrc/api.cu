@@ -257,8 +257,8 @@ static bcmc_lru* lru_new(bcmc_ctx* ctx, uint32_t initial_size, uint32_t element_
         c->item_slots = (int32_t*)dev_alloc(ctx, (size_t)c->aligned_total * 4);
         c->new_ids = (uint32_t*)dev_alloc(ctx, (size_t)(total ? total : 1) * 4);
         lru_alloc_slots(c, c->cache_size ? c->cache_size : 32u);
-        const size_t wa = active_tiles(total) + 1, ws = active_tiles(c->aligned_total) + 1,
-                     wsort = sort_status_words(c->aligned_total), wm = mc_tiles(total) + 1;
+        const size_t wa = active_tiles(total) + 1, ws = slot_tiles(c->aligned_total) + 1,
+                     wsort = sort_status_words(c->aligned_total), wm = mc_grid(ctx, total) + 1;
         c->status_words = 2 * wa + ws + wsort + 2 * wm;
         c->status = (uint64_t*)dev_alloc(ctx, c->status_words * 8);
         c->st_active_a = c->status;
@@ -357,6 +357,7 @@ struct bcmc_vol {
     uint32_t* active_ids = nullptr;
     uint32_t* with_verts = nullptr;
     uint32_t* vert_offsets = nullptr;
+    uint32_t* block_counts = nullptr;
     uint2* verts = nullptr;
     uint32_t vert_capacity = 0;
     uint32_t verts_storage = 0;  // the reference's numVerticesStorage
@@ -376,6 +377,7 @@ static void vol_free(bcmc_vol* v)
     dev_free(ctx, v->active_ids, (size_t)v->total * 4);
     dev_free(ctx, v->with_verts, (size_t)v->total * 4);
     dev_free(ctx, v->vert_offsets, (size_t)v->total * 4);
+    dev_free(ctx, v->block_counts, (size_t)v->total * 4);
     dev_free(ctx, v->verts, (size_t)v->vert_capacity * 8);
     lru_delete(v->lru);
     for (auto& e : v->ev)
@@ -438,6 +440,7 @@ static bcmc_status vol_create_common(bcmc_ctx* ctx, const void* src, bool src_de
             v->active_ids = (uint32_t*)dev_alloc(ctx, (size_t)total * 4);
             v->with_verts = (uint32_t*)dev_alloc(ctx, (size_t)total * 4);
             v->vert_offsets = (uint32_t*)dev_alloc(ctx, (size_t)total * 4);
+            v->block_counts = (uint32_t*)dev_alloc(ctx, (size_t)total * 4);
             const uint32_t init_slots =
                 (uint32_t)std::min<double>((double)total, std::ceil((double)total * ctx->opts.initial_cache_fraction));
             v->lru = lru_new(ctx, init_slots, 256u, (uint32_t)total);
@@ -555,7 +558,7 @@ bcmc_status bcmc_compute_surface(bcmc_vol* v, float iso, bcmc_perf* perf, uint32
         ActiveArgs aa{reinterpret_cast<const float2*>(v->ranges), nb, nullptr, v->active, c->item_slots, v->total,
                       v->active_ids, c->new_ids, c->st_active_a, c->st_active_n};
         McArgs ma{v->active, v->active_ids, c->item_slots, reinterpret_cast<const float*>(c->cache), nb,
-                  v->with_verts, v->vert_offsets, v->verts, c->st_mc_v, c->st_mc_b};
+                  v->with_verts, v->vert_offsets, v->block_counts, v->verts, c->st_mc_v, c->st_mc_b};
         for (int attempt = 0;; ++attempt) {
             if (perf) BCMC_CUDA(cudaEventRecord(v->ev[0], s));
             lru_begin(c, s, iso, 0, v->vert_capacity);

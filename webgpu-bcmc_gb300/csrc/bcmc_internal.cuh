@@ -125,6 +125,125 @@ __device__ __forceinline__ uint32_t lookback_exclusive(uint64_t* status, uint32_
     return exclusive;
 }
 
+// Warp-cooperative look-back, called by all 32 lanes of one warp: each round
+// reads the status words of 32 predecessors at once, finds the nearest one
+// holding an inclusive prefix with a ballot and sums the window with a warp
+// reduction, so a walk past k unfinished predecessors costs k/32 round trips.
+// Lane 0 publishes the aggregate first and the inclusive prefix at the end.
+// Returns the exclusive prefix in every lane.  A timed-out wait records
+// `site` in *err and stops the walk.
+__device__ __forceinline__ uint32_t warp_lookback(uint64_t* status, uint32_t tile, uint32_t aggregate,
+                                                  uint32_t epoch, uint32_t* err, uint32_t site,
+                                                  uint32_t stride = 1)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    if (tile == 0) {
+        if (lane == 0) lb_store(status, lb_pack(epoch, kFlagPrefix, aggregate));
+        return 0;
+    }
+    if (lane == 0) lb_store(status + (uint64_t)tile * stride, lb_pack(epoch, kFlagAggregate, aggregate));
+    // each lane owns 4 consecutive predecessors per round (nearest first):
+    // 128 status words per round trip
+    constexpr int kPer = 4;
+    uint32_t exclusive = 0;
+    int64_t tail = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    bool timed_out = false;
+    for (;;) {
+        uint32_t flag[kPer], value[kPer];
+        for (;;) {
+            bool ready = true;
+#pragma unroll
+            for (int i = 0; i < kPer; ++i) {
+                const int64_t pred = tail - (int64_t)(kPer * lane + i);
+                flag[i] = (uint32_t)kFlagPrefix;  // before tile 0: prefix 0
+                value[i] = 0;
+                if (pred >= 0) {
+                    const uint64_t s = lb_load(status + (uint64_t)pred * stride);
+                    const uint32_t hi = (uint32_t)(s >> 32);
+                    ready = ready && (hi >> 2) == epoch && (hi & 3u) != 0;
+                    flag[i] = hi & 3u;
+                    value[i] = (uint32_t)s;
+                }
+            }
+            if (__all_sync(0xffffffffu, ready)) break;
+            if (++spins > kSpinLimit) {
+                timed_out = true;
+                break;
+            }
+            if (spins > 8) __nanosleep(100);
+        }
+        if (timed_out) {
+            if (lane == 0) atomicCAS(err, 0u, site);
+            break;
+        }
+        // this lane's sum up to and including its nearest prefix (all 4 if none)
+        uint32_t local = 0;
+        bool has_prefix = false;
+#pragma unroll
+        for (int i = 0; i < kPer; ++i) {
+            if (!has_prefix) local += value[i];
+            has_prefix = has_prefix || flag[i] == (uint32_t)kFlagPrefix;
+        }
+        const uint32_t pmask = __ballot_sync(0xffffffffu, has_prefix);
+        if (pmask) {
+            const uint32_t first = (uint32_t)__ffs(pmask) - 1u;
+            exclusive += __reduce_add_sync(0xffffffffu, lane <= first ? local : 0u);
+            break;
+        }
+        exclusive += __reduce_add_sync(0xffffffffu, local);
+        tail -= 32 * kPer;
+    }
+    if (lane == 0) lb_store(status + (uint64_t)tile * stride, lb_pack(epoch, kFlagPrefix, exclusive + aggregate));
+    return exclusive;
+}
+
+// Per-thread look-back that keeps 8 predecessor loads in flight per round
+// (used where every thread owns its own chain, e.g. one radix digit each).
+__device__ __forceinline__ uint32_t lookback_exclusive_w8(uint64_t* status, uint32_t tile, uint32_t aggregate,
+                                                          uint32_t epoch, uint32_t* err, uint32_t site,
+                                                          uint32_t stride)
+{
+    constexpr int W = 8;
+    if (tile == 0) {
+        lb_store(status, lb_pack(epoch, kFlagPrefix, aggregate));
+        return 0;
+    }
+    lb_store(status + (uint64_t)tile * stride, lb_pack(epoch, kFlagAggregate, aggregate));
+    uint32_t exclusive = 0;
+    int64_t tail = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    bool done = false;
+    while (!done) {
+        uint64_t s[W];
+#pragma unroll
+        for (int i = 0; i < W; ++i)
+            s[i] = (tail - i >= 0) ? lb_load(status + (uint64_t)(tail - i) * stride)
+                                   : lb_pack(epoch, kFlagPrefix, 0u);
+#pragma unroll
+        for (int i = 0; i < W; ++i) {
+            if (done) break;
+            uint32_t hi = (uint32_t)(s[i] >> 32);
+            while ((hi >> 2) != epoch || (hi & 3u) == 0) {
+                if (++spins > kSpinLimit) {
+                    atomicCAS(err, 0u, site);
+                    done = true;
+                    break;
+                }
+                if (spins > 8) __nanosleep(100);
+                s[i] = lb_load(status + (uint64_t)(tail - i) * stride);
+                hi = (uint32_t)(s[i] >> 32);
+            }
+            if (done) break;
+            exclusive += (uint32_t)s[i];
+            if ((hi & 3u) == kFlagPrefix) done = true;
+        }
+        tail -= W;
+    }
+    lb_store(status + (uint64_t)tile * stride, lb_pack(epoch, kFlagPrefix, exclusive + aggregate));
+    return exclusive;
+}
+
 // Warp-wide inclusive scan (shuffles).
 __device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t v)
 {

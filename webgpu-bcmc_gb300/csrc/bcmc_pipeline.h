@@ -53,6 +53,7 @@ struct McArgs {
     uint3 nb;
     uint32_t* with_verts;
     uint32_t* vert_offsets;
+    uint32_t* block_counts;  // vertices of each active block (count pass -> emit pass)
     uint2* verts;
     uint64_t* status_v;
     uint64_t* status_b;
@@ -65,6 +66,7 @@ void slots_launch(bcmc_ctx* ctx, QueryState* q, const SlotArgs& a, uint32_t max_
 void assign_launch(bcmc_ctx* ctx, QueryState* q, const AssignArgs& a, uint32_t max_new, cudaStream_t s);
 void mc_launch(bcmc_ctx* ctx, QueryState* q, const McArgs& a, uint32_t max_active, cudaStream_t s);
 uint32_t active_tiles(uint32_t total);
-uint32_t mc_tiles(uint32_t total);
+uint32_t slot_tiles(uint32_t slots);
+uint32_t mc_grid(bcmc_ctx* ctx, uint32_t max_active);
 
 }  // namespace bcmc

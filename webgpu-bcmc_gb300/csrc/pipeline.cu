@@ -65,39 +65,49 @@ __global__ void k_query_begin(QueryState* q, float iso, int mc_only, uint32_t ca
 // ---------------------------------------------------------------------------
 constexpr int kActThreads = 256;
 constexpr int kActItems = 8;
-constexpr int kActTile = kActThreads * kActItems;
+constexpr int kActTile = kActThreads * kActItems;  // slots per k_slots tile
+constexpr int kActiveItems = 2;
+constexpr int kActiveTile = kActThreads * kActiveItems;  // blocks per k_active tile
 
 __device__ __forceinline__ uint32_t spad8(uint32_t i) { return i + (i >> 5); }
 
-// compute_block_active.comp:24-61
+// compute_block_active.comp:24-61.  The reference tests, for each of the 26
+// neighbours n, iso in [min(lo_b, lo_n), max(hi_b, hi_n)].  With A = (iso >=
+// lo), B = (iso <= hi) that is (A_b || A_n) && (B_b || B_n), so over all
+// neighbours (and b itself, which adds nothing new):
+//   active = (A_b && anyB) || (B_b && anyA) || any(A_n && B_n)
+// -- the same booleans, evaluated without branches or early exits.
 __device__ __forceinline__ uint32_t block_is_active(const float2* __restrict__ ranges, uint3 nb, uint32_t b,
                                                     float iso)
 {
-    const float2 r = ranges[b];
-    if (iso >= r.x && iso <= r.y) return 1u;
+    const float2 r = __ldg(ranges + b);
+    const bool A = iso >= r.x, B = iso <= r.y;
     const int bx = (int)(b % nb.x), by = (int)((b / nb.x) % nb.y), bz = (int)(b / (nb.x * nb.y));
+    bool anyA = false, anyB = false, anyC = false;
+#pragma unroll
     for (int k = -1; k < 2; ++k)
+#pragma unroll
         for (int j = -1; j < 2; ++j)
+#pragma unroll
             for (int i = -1; i < 2; ++i) {
                 const int cx = bx + i, cy = by + j, cz = bz + k;
-                if ((i == 0 && j == 0 && k == 0) || cx < 0 || cy < 0 || cz < 0 || cx >= (int)nb.x ||
-                    cy >= (int)nb.y || cz >= (int)nb.z)
-                    continue;
-                const float2 n = ranges[(uint32_t)cx + nb.x * ((uint32_t)cy + nb.y * (uint32_t)cz)];
-                const float lo = n.x < r.x ? n.x : r.x;  // GLSL min(range.x, n.x)
-                const float hi = r.y < n.y ? n.y : r.y;  // GLSL max(range.y, n.y)
-                if (iso >= lo && iso <= hi) return 1u;
+                if (cx < 0 || cy < 0 || cz < 0 || cx >= (int)nb.x || cy >= (int)nb.y || cz >= (int)nb.z) continue;
+                const float2 n = __ldg(ranges + ((uint32_t)cx + nb.x * ((uint32_t)cy + nb.y * (uint32_t)cz)));
+                const bool an = iso >= n.x, bn = iso <= n.y;
+                anyA |= an;
+                anyB |= bn;
+                anyC |= an && bn;
             }
-    return 0u;
+    return ((A && anyB) || (B && anyA) || anyC) ? 1u : 0u;
 }
 
 __global__ void __launch_bounds__(kActThreads) k_active(QueryState* q, ActiveArgs a)
 {
-    __shared__ uint8_t s_flags[kActTile + kActTile / 32];
+    __shared__ uint8_t s_flags[kActiveTile + kActiveTile / 32];
     __shared__ uint32_t s_warp[kActThreads / 32 + 1];
     __shared__ uint32_t s_tile, s_pa, s_pn;
     const uint32_t total = a.total;
-    const uint32_t ntiles = div_up(total, kActTile);
+    const uint32_t ntiles = div_up(total, kActiveTile);
     const uint32_t epoch = q->epoch;
     const float iso = q->isovalue;
     for (;;) {
@@ -105,9 +115,9 @@ __global__ void __launch_bounds__(kActThreads) k_active(QueryState* q, ActiveArg
         __syncthreads();
         const uint32_t tile = s_tile;
         if (tile >= ntiles) break;
-        const uint32_t base = tile * kActTile;
+        const uint32_t base = tile * kActiveTile;
 #pragma unroll
-        for (int j = 0; j < kActItems; ++j) {
+        for (int j = 0; j < kActiveItems; ++j) {
             const uint32_t local = j * kActThreads + threadIdx.x;
             const uint32_t b = base + local;
             uint32_t f = 0;
@@ -126,21 +136,26 @@ __global__ void __launch_bounds__(kActThreads) k_active(QueryState* q, ActiveArg
         }
         __syncthreads();
         uint32_t cnt = 0;
-        uint8_t fl[kActItems];
+        uint8_t fl[kActiveItems];
 #pragma unroll
-        for (int j = 0; j < kActItems; ++j) {
-            fl[j] = s_flags[spad8(threadIdx.x * kActItems + j)];
+        for (int j = 0; j < kActiveItems; ++j) {
+            fl[j] = s_flags[spad8(threadIdx.x * kActiveItems + j)];
             cnt += (fl[j] & 1u) | ((uint32_t)(fl[j] >> 1) << 16);
         }
         uint32_t tot;
         const uint32_t excl = cta_exclusive_scan<kActThreads>(cnt, s_warp, &tot);
-        if (threadIdx.x == 0) s_pa = lookback_exclusive(a.status_a, tile, tot & 0xffffu, epoch, &q->error, 30u);
-        if (threadIdx.x == 32) s_pn = lookback_exclusive(a.status_n, tile, tot >> 16, epoch, &q->error, 31u);
+        if (threadIdx.x < 32) {
+            const uint32_t p = warp_lookback(a.status_a, tile, tot & 0xffffu, epoch, &q->error, 30u);
+            if (threadIdx.x == 0) s_pa = p;
+        } else if (threadIdx.x < 64) {
+            const uint32_t p = warp_lookback(a.status_n, tile, tot >> 16, epoch, &q->error, 31u);
+            if (threadIdx.x == 32) s_pn = p;
+        }
         __syncthreads();
         uint32_t pa = s_pa + (excl & 0xffffu), pn = s_pn + (excl >> 16);
-        const uint32_t first = base + threadIdx.x * kActItems;
+        const uint32_t first = base + threadIdx.x * kActiveItems;
 #pragma unroll
-        for (int j = 0; j < kActItems; ++j) {
+        for (int j = 0; j < kActiveItems; ++j) {
             if (fl[j] & 1u) {
                 if (a.active_ids) a.active_ids[pa] = first + j;
                 ++pa;
@@ -231,7 +246,10 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
             }
             uint32_t tot;
             const uint32_t excl = cta_exclusive_scan<kActThreads>(cnt, s_warp, &tot);
-            if (threadIdx.x == 0) s_prefix = lookback_exclusive(a.status, tile, tot, epoch, &q->error, 32u);
+            if (threadIdx.x < 32) {
+                const uint32_t p = warp_lookback(a.status, tile, tot, epoch, &q->error, 32u);
+                if (threadIdx.x == 0) s_prefix = p;
+            }
             __syncthreads();
             uint32_t p = s_prefix + excl;
             const uint32_t first = base + threadIdx.x * kActItems;
@@ -282,38 +300,44 @@ __global__ void __launch_bounds__(128) k_assign(QueryState* q, AssignArgs a)
 }
 
 // ---------------------------------------------------------------------------
-// k_mc: marching cubes over the active blocks, 4 blocks (256 cells) per tile.
+// k_mc: marching cubes over the active blocks, 16 blocks per tile.
 // ---------------------------------------------------------------------------
-constexpr int kMcBlocks = 4;
-constexpr int kMcThreads = 64 * kMcBlocks;
+constexpr int kMcBlocks = 16;
+constexpr int kMcThreads = 256;
+constexpr int kMcCells = 64 * kMcBlocks;  // 4 consecutive cells per thread
 
-// ghost voxel positions of a 5^3 block (some coordinate == 4), packed x|y<<4|z<<8
+// Ghost voxels of a block's 5^3 grid (some coordinate == 4): x|y<<4|z<<8 and,
+// in bits 12-14, which +x/+y/+z neighbour holds them (kNb* order below).
 __constant__ uint16_t c_ghost[61] = {
-#define G(x, y, z) (uint16_t)((x) | ((y) << 4) | ((z) << 8))
-    G(4, 0, 0), G(4, 1, 0), G(4, 2, 0), G(4, 3, 0), G(0, 4, 0), G(1, 4, 0), G(2, 4, 0), G(3, 4, 0), G(4, 4, 0),
-    G(4, 0, 1), G(4, 1, 1), G(4, 2, 1), G(4, 3, 1), G(0, 4, 1), G(1, 4, 1), G(2, 4, 1), G(3, 4, 1), G(4, 4, 1),
-    G(4, 0, 2), G(4, 1, 2), G(4, 2, 2), G(4, 3, 2), G(0, 4, 2), G(1, 4, 2), G(2, 4, 2), G(3, 4, 2), G(4, 4, 2),
-    G(4, 0, 3), G(4, 1, 3), G(4, 2, 3), G(4, 3, 3), G(0, 4, 3), G(1, 4, 3), G(2, 4, 3), G(3, 4, 3), G(4, 4, 3),
-    G(0, 0, 4), G(1, 0, 4), G(2, 0, 4), G(3, 0, 4), G(4, 0, 4), G(0, 1, 4), G(1, 1, 4), G(2, 1, 4), G(3, 1, 4),
-    G(4, 1, 4), G(0, 2, 4), G(1, 2, 4), G(2, 2, 4), G(3, 2, 4), G(4, 2, 4), G(0, 3, 4), G(1, 3, 4), G(2, 3, 4),
-    G(3, 3, 4), G(4, 3, 4), G(0, 4, 4), G(1, 4, 4), G(2, 4, 4), G(3, 4, 4), G(4, 4, 4)
+#define G(x, y, z, k) (uint16_t)((x) | ((y) << 4) | ((z) << 8) | ((k) << 12))
+    G(4, 0, 0, 0), G(4, 1, 0, 0), G(4, 2, 0, 0), G(4, 3, 0, 0), G(0, 4, 0, 1), G(1, 4, 0, 1), G(2, 4, 0, 1),
+    G(3, 4, 0, 1), G(4, 4, 0, 3), G(4, 0, 1, 0), G(4, 1, 1, 0), G(4, 2, 1, 0), G(4, 3, 1, 0), G(0, 4, 1, 1),
+    G(1, 4, 1, 1), G(2, 4, 1, 1), G(3, 4, 1, 1), G(4, 4, 1, 3), G(4, 0, 2, 0), G(4, 1, 2, 0), G(4, 2, 2, 0),
+    G(4, 3, 2, 0), G(0, 4, 2, 1), G(1, 4, 2, 1), G(2, 4, 2, 1), G(3, 4, 2, 1), G(4, 4, 2, 3), G(4, 0, 3, 0),
+    G(4, 1, 3, 0), G(4, 2, 3, 0), G(4, 3, 3, 0), G(0, 4, 3, 1), G(1, 4, 3, 1), G(2, 4, 3, 1), G(3, 4, 3, 1),
+    G(4, 4, 3, 3), G(0, 0, 4, 2), G(1, 0, 4, 2), G(2, 0, 4, 2), G(3, 0, 4, 2), G(4, 0, 4, 4), G(0, 1, 4, 2),
+    G(1, 1, 4, 2), G(2, 1, 4, 2), G(3, 1, 4, 2), G(4, 1, 4, 4), G(0, 2, 4, 2), G(1, 2, 4, 2), G(2, 2, 4, 2),
+    G(3, 2, 4, 2), G(4, 2, 4, 4), G(0, 3, 4, 2), G(1, 3, 4, 2), G(2, 3, 4, 2), G(3, 3, 4, 2), G(4, 3, 4, 4),
+    G(0, 4, 4, 5), G(1, 4, 4, 5), G(2, 4, 4, 5), G(3, 4, 4, 5), G(4, 4, 4, 6)
 #undef G
 };
+// neighbour k of a block: +x, +y, +z, +xy, +xz, +yz, +xyz (packed x|y<<1|z<<2)
+__constant__ uint8_t c_nb_off[7] = {1, 2, 4, 3, 5, 6, 7};
+enum { kNbX = 0, kNbY, kNbZ, kNbXY, kNbXZ, kNbYZ, kNbXYZ, kNbSelf };
 
 // compute_vertex_values.comp:96-156: grid extent of the block plus the ghost
 // layer taken from active +x/+y/+z neighbours, tested corner, edges, faces.
-__device__ __forceinline__ uint32_t block_dims_with_ghost(const uint32_t* __restrict__ active, uint3 nb,
-                                                          uint32_t bx, uint32_t by, uint32_t bz)
+// `act` has bit k set when neighbour k exists and is active.
+__device__ __forceinline__ uint32_t block_dims_with_ghost(uint32_t act, bool hx, bool hy, bool hz)
 {
-    auto act = [&](uint32_t x, uint32_t y, uint32_t z) { return active[x + nb.x * (y + nb.y * z)] != 0u; };
-    uint32_t dx = bx + 1 < nb.x ? 5 : 4, dy = by + 1 < nb.y ? 5 : 4, dz = bz + 1 < nb.z ? 5 : 4;
-    if (dx == 5 && dy == 5 && dz == 5 && !act(bx + 1, by + 1, bz + 1)) dx = dy = dz = 4;
-    if (dx == 5 && dy == 5 && !act(bx + 1, by + 1, bz)) dx = dy = 4;
-    if (dx == 5 && dz == 5 && !act(bx + 1, by, bz + 1)) dx = dz = 4;
-    if (dy == 5 && dz == 5 && !act(bx, by + 1, bz + 1)) dy = dz = 4;
-    if (dx == 5 && !act(bx + 1, by, bz)) dx = 4;
-    if (dy == 5 && !act(bx, by + 1, bz)) dy = 4;
-    if (dz == 5 && !act(bx, by, bz + 1)) dz = 4;
+    uint32_t dx = hx ? 5 : 4, dy = hy ? 5 : 4, dz = hz ? 5 : 4;
+    if (dx == 5 && dy == 5 && dz == 5 && !(act >> kNbXYZ & 1u)) dx = dy = dz = 4;
+    if (dx == 5 && dy == 5 && !(act >> kNbXY & 1u)) dx = dy = 4;
+    if (dx == 5 && dz == 5 && !(act >> kNbXZ & 1u)) dx = dz = 4;
+    if (dy == 5 && dz == 5 && !(act >> kNbYZ & 1u)) dy = dz = 4;
+    if (dx == 5 && !(act >> kNbX & 1u)) dx = 4;
+    if (dy == 5 && !(act >> kNbY & 1u)) dy = 4;
+    if (dz == 5 && !(act >> kNbZ & 1u)) dz = 4;
     return dx | (dy << 4) | (dz << 8);
 }
 
@@ -326,132 +350,236 @@ __device__ __forceinline__ uint32_t quantize(float p)
     return __float2uint_rz(f) & 0x3ffu;  // saturating float->uint, as WGSL u32()
 }
 
+// Marching cubes over the active blocks.  Each CTA owns one contiguous range of
+// active blocks (whole 16-block tiles) and makes two passes over it:
+//   count pass: per tile, one parallel round of loads fetches the active flags
+//     and cache slots of every block's 7 +x/+y/+z neighbours and its own slot,
+//     a second round fills each block's 5^3 grid in shared memory (16 B vector
+//     loads of 4 voxels per thread, ghost voxels alongside); one thread per 4
+//     cells finds the case and vertex count; block totals are kept for the
+//     emit pass and summed for the CTA;
+//   one warp-cooperative decoupled look-back per CTA turns the CTA totals into
+//     its global vertex offset and its offset in the blocks-with-vertices list;
+//   emit pass: tiles are reloaded (from L2), blocks without vertices skipped;
+//     a CTA scan gives each cell's offset and the vertices are spread over the
+//     CTA -- thread k takes vertex k of the tile, finds its cell by binary
+//     search -- so lanes stay converged and stores are contiguous.
+// A CTA walks back once per launch, not once per tile, so the look-back never
+// waits on a wave of unfinished tiles.  Output order = the reference's:
+// active-block order, cell order, table order.
 __global__ void __launch_bounds__(kMcThreads) k_mc(QueryState* q, McArgs a)
 {
     __shared__ float s_vol[kMcBlocks][128];
     __shared__ int8_t s_tri[256][16];
-    __shared__ uint32_t s_dims[kMcBlocks], s_id[kMcBlocks];
-    __shared__ uint32_t s_wsum[kMcThreads / 32];
-    __shared__ uint32_t s_tile, s_pv, s_pb;
+    __shared__ uint8_t s_cnt[256];
+    __shared__ uint8_t s_edge[12];  // corner offsets of each edge: o0 | o1 << 3
+    __shared__ __align__(16) uint8_t s_case[kMcCells];  // written 4 cases per 32-bit store
+    __shared__ uint32_t s_off[kMcCells + 1];
+    __shared__ uint32_t s_id[kMcBlocks];
+    __shared__ uint32_t s_slot[kMcBlocks][8];
+    __shared__ uint32_t s_act[kMcBlocks];
+    __shared__ uint32_t s_warp[kMcThreads / 32 + 1];
+    __shared__ uint32_t s_any, s_pv, s_pb, s_cta_v, s_cta_b;
 
     const uint32_t A = q->num_active;
     if (A == 0 || q->grow_needed) return;
-    const uint32_t ntiles = div_up(A, kMcBlocks);
     const uint32_t epoch = q->epoch;
     const float iso = q->isovalue;
     const uint32_t cap = q->vert_capacity;
     const uint32_t slots = q->cache_size;
+    const uint3 nb = a.nb;
+    const uint32_t t = threadIdx.x;
+    const uint32_t G = gridDim.x;
+    const uint32_t range = div_up(div_up(A, G), kMcBlocks) * kMcBlocks;
+    const uint32_t start = min(A, blockIdx.x * range), end = min(A, start + range);
     {
         const uint4* src = reinterpret_cast<const uint4*>(&kTriEdges[0][0]);
         uint4* dst = reinterpret_cast<uint4*>(&s_tri[0][0]);
-        for (int i = threadIdx.x; i < 256; i += kMcThreads) dst[i] = src[i];
-    }
-    const uint32_t j = threadIdx.x >> 6, c = threadIdx.x & 63u;
-    const uint32_t cx = c & 3u, cy = (c >> 2) & 3u, cz = c >> 4;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(&q->tiles_mc, 1u);
-        __syncthreads();
-        const uint32_t tile = s_tile;
-        if (tile >= ntiles) break;
-        const uint32_t idx = tile * kMcBlocks + j;
-        const bool valid = idx < A;
-        if (c == 0) {
-            uint32_t id = 0, dims = 0;
-            if (valid) {
-                id = a.active_ids[idx];
-                dims = block_dims_with_ghost(a.active, a.nb, id % a.nb.x, (id / a.nb.x) % a.nb.y,
-                                             id / (a.nb.x * a.nb.y));
-            }
-            s_id[j] = id;
-            s_dims[j] = dims;
+        for (uint32_t i = t; i < 256; i += kMcThreads) dst[i] = src[i];
+        for (uint32_t i = t; i < 256; i += kMcThreads) {
+            uint32_t n = 0;
+            while (n < 16 && kTriEdges[i][n] != -1) ++n;
+            s_cnt[i] = (uint8_t)n;
         }
-        __syncthreads();
-        const uint32_t id = s_id[j], dims = s_dims[j];
-        const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
-        if (valid) {
-            // every active block is cached; a slot outside the cache would be a
-            // logic error, reported instead of read
-            const uint32_t slot = (uint32_t)a.item_slots[id];
-            if (slot < slots) s_vol[j][cx + 5u * (cy + 5u * cz)] = __ldg(a.cache + (uint64_t)slot * 64u + c);
-            else atomicCAS(&q->error, 0u, 51u);
-            if (c < 61) {
-                const uint32_t g = c_ghost[c];
-                const uint32_t gx = g & 15u, gy = (g >> 4) & 15u, gz = g >> 8;
-                if (gx < dx && gy < dy && gz < dz) {
-                    const uint32_t nid = id + (gx >> 2) + a.nb.x * ((gy >> 2) + a.nb.y * (gz >> 2));
-                    const uint32_t nslot = (uint32_t)a.item_slots[nid];
-                    if (nslot < slots)
-                        s_vol[j][gx + 5u * (gy + 5u * gz)] =
-                            __ldg(a.cache + (uint64_t)nslot * 64u + (gx & 3u) + 4u * ((gy & 3u) + 4u * (gz & 3u)));
-                    else atomicCAS(&q->error, 0u, 52u);
+        if (t < 12) s_edge[t] = (uint8_t)(c_corner[c_edge[t][0]] | (c_corner[c_edge[t][1]] << 3));
+        if (t == 0) s_cta_v = s_cta_b = 0;
+    }
+    // thread -> (block j, cells 4u..4u+3 = the x-row (y, z) = (u & 3, u >> 2))
+    const uint32_t j = t >> 4, u = t & 15u, ry = u & 3u, rz = u >> 2;
+    uint32_t pv = 0, pb = 0;
+
+    for (int pass = 0; pass < 2; ++pass) {
+        if (pass == 1) {
+            __syncthreads();
+            if (t < 64) {  // warp 0: vertex offset, warp 1: offset among blocks with vertices
+                if (t < 32) {
+                    const uint32_t p = warp_lookback(a.status_v, blockIdx.x, s_cta_v, epoch, &q->error, 40u);
+                    if (t == 0) {
+                        s_pv = p;
+                        if (blockIdx.x == G - 1) q->num_verts = p + s_cta_v;
+                    }
+                } else {
+                    const uint32_t p = warp_lookback(a.status_b, blockIdx.x, s_cta_b, epoch, &q->error, 41u);
+                    if (t == 32) {
+                        s_pb = p;
+                        if (blockIdx.x == G - 1) q->num_with_verts = p + s_cta_b;
+                    }
                 }
             }
-        }
-        __syncthreads();
-        // per-cell case and vertex count
-        float val[8];
-        uint32_t cs = 0, nv = 0;
-        if (valid && cx + 1 < dx && cy + 1 < dy && cz + 1 < dz) {
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const uint32_t o = c_corner[i];
-                val[i] = s_vol[j][(cx + (o & 1u)) + 5u * ((cy + ((o >> 1) & 1u)) + 5u * (cz + (o >> 2)))];
-                cs |= (val[i] <= iso ? 1u : 0u) << i;
+            __syncthreads();
+            pv = s_pv;
+            pb = s_pb;
+            if ((uint64_t)pv + s_cta_v > cap) {  // host grows the vertex buffer and re-runs
+                if (t == 0) atomicOr(&q->vert_overflow, 1u);
+                break;
             }
-            const int8_t* row = s_tri[cs];
-            while (nv < 16 && row[nv] != -1) ++nv;
         }
-        // block-local exclusive scan (two warps per block)
-        const uint32_t inc = warp_inclusive_scan(nv);
-        if (lane == 31) s_wsum[warp] = inc;
-        __syncthreads();
-        const uint32_t local = inc - nv + ((warp & 1) ? s_wsum[warp - 1] : 0u);
-        uint32_t btot[kMcBlocks], boff[kMcBlocks], bwv_rank[kMcBlocks];
-        uint32_t tile_v = 0, tile_b = 0;
+        for (uint32_t base = start; base < end; base += kMcBlocks) {
+            __syncthreads();
+            if (t == 0) s_any = 0;
+            __syncthreads();
+            if (t < kMcBlocks) {
+                const uint32_t idx = base + t;
+                uint32_t id = 0xffffffffu;
+                if (idx < end && (pass == 0 || a.block_counts[idx] != 0u)) id = __ldg(a.active_ids + idx);
+                s_id[t] = id;
+                if (id != 0xffffffffu) s_any = 1;
+            }
+            __syncthreads();
+            if (!s_any) continue;  // emit pass: no block of this tile has vertices
+            // neighbour flags and slots: thread (block t >> 3, entry t & 7)
+            if (t < kMcBlocks * 8) {
+                const uint32_t jb = t >> 3, k = t & 7u, id = s_id[jb];
+                uint32_t slot = 0xffffffffu, act = 0;
+                if (id != 0xffffffffu) {
+                    const uint32_t bx = id % nb.x, by = (id / nb.x) % nb.y, bz = id / (nb.x * nb.y);
+                    if (k == kNbSelf) {
+                        slot = (uint32_t)__ldg(a.item_slots + id);
+                    } else {
+                        const uint32_t o = c_nb_off[k], ox = o & 1u, oy = (o >> 1) & 1u, oz = o >> 2;
+                        if (bx + ox < nb.x && by + oy < nb.y && bz + oz < nb.z) {
+                            const uint32_t nid = id + ox + nb.x * (oy + nb.y * oz);
+                            act = __ldg(a.active + nid) != 0u ? 1u : 0u;
+                            slot = (uint32_t)__ldg(a.item_slots + nid);
+                        }
+                    }
+                }
+                s_slot[jb][k] = slot;
+                const uint32_t bits = __ballot_sync(0xffffffffu, act != 0u);  // 4 blocks per warp
+                if ((t & 7u) == 0) s_act[jb] = (bits >> (t & 24u)) & 0x7fu;
+            }
+            __syncthreads();
+            // grid of each block (+ ghost layer) in shared memory
+            const uint32_t id = s_id[j];
+            const bool valid = id != 0xffffffffu;
+            uint32_t dims = 0;
+            if (valid) {
+                const uint32_t bx = id % nb.x, by = (id / nb.x) % nb.y, bz = id / (nb.x * nb.y);
+                dims = block_dims_with_ghost(s_act[j], bx + 1 < nb.x, by + 1 < nb.y, bz + 1 < nb.z);
+                const uint32_t slot = s_slot[j][kNbSelf];
+                if (slot < slots) {
+                    const float4 v4 = __ldg(reinterpret_cast<const float4*>(a.cache + (uint64_t)slot * 64u) + u);
+                    float* row = &s_vol[j][5u * (ry + 5u * rz)];
+                    row[0] = v4.x;
+                    row[1] = v4.y;
+                    row[2] = v4.z;
+                    row[3] = v4.w;
+                } else {
+                    atomicCAS(&q->error, 0u, 51u);
+                }
+                const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
 #pragma unroll
-        for (int k = 0; k < kMcBlocks; ++k) {
-            btot[k] = s_wsum[2 * k] + s_wsum[2 * k + 1];
-            boff[k] = tile_v;
-            bwv_rank[k] = tile_b;
-            tile_v += btot[k];
-            tile_b += btot[k] > 0 ? 1u : 0u;
-        }
-        if (threadIdx.x == 0) s_pv = lookback_exclusive(a.status_v, tile, tile_v, epoch, &q->error, 40u);
-        if (threadIdx.x == 32) s_pb = lookback_exclusive(a.status_b, tile, tile_b, epoch, &q->error, 41u);
-        __syncthreads();
-        const uint32_t pv = s_pv, pb = s_pb;
-        if (tile == ntiles - 1 && threadIdx.x == 0) {
-            q->num_verts = pv + tile_v;
-            q->num_with_verts = pb + tile_b;
-        }
-        if (c == 0 && valid && btot[j] > 0 && pb + bwv_rank[j] < A) {
-            a.with_verts[pb + bwv_rank[j]] = idx;
-            a.vert_offsets[pb + bwv_rank[j]] = pv + boff[j];
-        }
-        if ((uint64_t)pv + tile_v > cap) {
-            if (threadIdx.x == 0) atomicOr(&q->vert_overflow, 1u);
-        } else if (nv) {
-            uint2* out = a.verts + pv + boff[j] + local;
-            const int8_t* row = s_tri[cs];
-            const float fx = (float)cx, fy = (float)cy, fz = (float)cz;
-            for (uint32_t t = 0; t < nv; ++t) {
-                const uint32_t e = (uint32_t)row[t];
-                const uint32_t v0 = c_edge[e][0], v1 = c_edge[e][1];
-                const float fa = val[v0], fb = val[v1];
+                for (uint32_t gi = u; gi < 61; gi += 16) {
+                    const uint32_t g = c_ghost[gi];
+                    const uint32_t gx = g & 15u, gy = (g >> 4) & 15u, gz = (g >> 8) & 15u;
+                    if (gx < dx && gy < dy && gz < dz) {
+                        const uint32_t nslot = s_slot[j][g >> 12];
+                        if (nslot < slots)
+                            s_vol[j][gx + 5u * (gy + 5u * gz)] = __ldg(
+                                a.cache + (uint64_t)nslot * 64u + (gx & 3u) + 4u * ((gy & 3u) + 4u * (gz & 3u)));
+                        else
+                            atomicCAS(&q->error, 0u, 52u);
+                    }
+                }
+            }
+            __syncthreads();
+            // cases and counts of cells 4t..4t+3 (compute_block_has_vertices.comp:28-51)
+            uint32_t nv[4], cs4 = 0, mysum = 0;
+            {
+                const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
+                const bool row_ok = valid && ry + 1 < dy && rz + 1 < dz;
+#pragma unroll
+                for (uint32_t x = 0; x < 4; ++x) {
+                    uint32_t cs = 0;
+                    nv[x] = 0;
+                    if (row_ok && x + 1 < dx) {
+                        const float* v = &s_vol[j][x + 5u * (ry + 5u * rz)];
+                        cs = (v[0] <= iso ? 1u : 0u) | (v[1] <= iso ? 2u : 0u) | (v[6] <= iso ? 4u : 0u) |
+                             (v[5] <= iso ? 8u : 0u) | (v[25] <= iso ? 16u : 0u) | (v[26] <= iso ? 32u : 0u) |
+                             (v[31] <= iso ? 64u : 0u) | (v[30] <= iso ? 128u : 0u);
+                        nv[x] = s_cnt[cs];
+                    }
+                    cs4 |= cs << (8u * x);
+                    mysum += nv[x];
+                }
+            }
+            uint32_t tile_v;
+            uint32_t run = cta_exclusive_scan<kMcThreads>(mysum, s_warp, &tile_v);
+            if (pass == 0) {
+                // block total = sum over its 16 threads (a half warp)
+                uint32_t bsum = mysum;
+#pragma unroll
+                for (int o = 8; o; o >>= 1) bsum += __shfl_xor_sync(0xffffffffu, bsum, o);
+                if (u == 0 && valid) {
+                    a.block_counts[base + j] = bsum;
+                    if (bsum) atomicAdd(&s_cta_b, 1u);
+                }
+                if (t == 0) s_cta_v += tile_v;
+                continue;
+            }
+            *reinterpret_cast<uint32_t*>(&s_case[4u * t]) = cs4;
+#pragma unroll
+            for (uint32_t x = 0; x < 4; ++x) {
+                s_off[4u * t + x] = run;
+                run += nv[x];
+            }
+            if (t == 0) s_off[kMcCells] = tile_v;
+            __syncthreads();
+            if (t < kMcBlocks && s_off[64 * (t + 1)] > s_off[64 * t]) {
+                uint32_t rank = 0;
+                for (uint32_t k = 0; k < t; ++k) rank += s_off[64 * (k + 1)] > s_off[64 * k] ? 1u : 0u;
+                a.with_verts[pb + rank] = base + t;
+                a.vert_offsets[pb + rank] = pv + s_off[64 * t];
+            }
+            uint2* out = a.verts + pv;
+            for (uint32_t k = t; k < tile_v; k += kMcThreads) {
+                uint32_t cell = 0;
+#pragma unroll
+                for (uint32_t step = kMcCells / 2; step; step >>= 1)
+                    if (s_off[cell + step] <= k) cell += step;
+                const uint32_t tt_idx = k - s_off[cell];
+                const uint32_t ed = s_edge[(uint32_t)s_tri[s_case[cell]][tt_idx]];
+                const uint32_t jb = cell >> 6, cc = cell & 63u;
+                const uint32_t x = cc & 3u, y = (cc >> 2) & 3u, z = cc >> 4;
+                const uint32_t o0 = ed & 7u, o1 = ed >> 3;
+                const uint32_t ax = o0 & 1u, ay = (o0 >> 1) & 1u, az = o0 >> 2;
+                const uint32_t bx = o1 & 1u, by = (o1 >> 1) & 1u, bz = o1 >> 2;
+                const float fa = s_vol[jb][(x + ax) + 5u * ((y + ay) + 5u * (z + az))];
+                const float fb = s_vol[jb][(x + bx) + 5u * ((y + by) + 5u * (z + bz))];
+                // lerp_verts (compute_block_vertices.comp:62-74)
                 float tt = 0.0f;
                 if (!(fabsf(__fsub_rn(fa, fb)) < 0.001f)) tt = __fdiv_rn(__fsub_rn(iso, fa), __fsub_rn(fb, fa));
-                const uint32_t o0 = c_corner[v0], o1 = c_corner[v1];
-                const int ax = (int)(o0 & 1u), ay = (int)((o0 >> 1) & 1u), az = (int)(o0 >> 2);
-                const int bx = (int)(o1 & 1u), by = (int)((o1 >> 1) & 1u), bz = (int)(o1 >> 2);
-                const float px = __fadd_rn(__fadd_rn(__fadd_rn((float)ax, __fmul_rn(tt, (float)(bx - ax))), fx), 0.5f);
-                const float py = __fadd_rn(__fadd_rn(__fadd_rn((float)ay, __fmul_rn(tt, (float)(by - ay))), fy), 0.5f);
-                const float pz = __fadd_rn(__fadd_rn(__fadd_rn((float)az, __fmul_rn(tt, (float)(bz - az))), fz), 0.5f);
-                out[t] = make_uint2((quantize(px) << 20) | (quantize(py) << 10) | quantize(pz), id);
+                const float px = __fadd_rn(__fadd_rn(__fadd_rn((float)ax, __fmul_rn(tt, (float)((int)bx - (int)ax))), (float)x), 0.5f);
+                const float py = __fadd_rn(__fadd_rn(__fadd_rn((float)ay, __fmul_rn(tt, (float)((int)by - (int)ay))), (float)y), 0.5f);
+                const float pz = __fadd_rn(__fadd_rn(__fadd_rn((float)az, __fmul_rn(tt, (float)((int)bz - (int)az))), (float)z), 0.5f);
+                out[k] = make_uint2((quantize(px) << 20) | (quantize(py) << 10) | quantize(pz), s_id[jb]);
             }
+            uint32_t tile_b = 0;
+#pragma unroll
+            for (int k = 0; k < kMcBlocks; ++k) tile_b += s_off[64 * (k + 1)] > s_off[64 * k] ? 1u : 0u;
+            pv += tile_v;
+            pb += tile_b;
         }
-        __syncthreads();
     }
 }
 
@@ -474,7 +602,7 @@ void query_begin_launch(QueryState* q, float iso, int mc_only, uint32_t capacity
 
 void active_launch(bcmc_ctx* ctx, QueryState* q, const ActiveArgs& a, cudaStream_t s)
 {
-    k_active<<<pgrid(ctx, div_up(a.total, kActTile), 4), kActThreads, 0, s>>>(q, a);
+    k_active<<<pgrid(ctx, div_up(a.total, kActiveTile), 8), kActThreads, 0, s>>>(q, a);
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
 }
@@ -495,12 +623,18 @@ void assign_launch(bcmc_ctx* ctx, QueryState* q, const AssignArgs& a, uint32_t m
 
 void mc_launch(bcmc_ctx* ctx, QueryState* q, const McArgs& a, uint32_t max_active, cudaStream_t s)
 {
-    k_mc<<<pgrid(ctx, div_up(max_active, kMcBlocks), 8), kMcThreads, 0, s>>>(q, a);
+    k_mc<<<mc_grid(ctx, max_active), kMcThreads, 0, s>>>(q, a);
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
 }
 
-uint32_t active_tiles(uint32_t total) { return div_up(total, kActTile); }
-uint32_t mc_tiles(uint32_t total) { return div_up(total, kMcBlocks); }
+uint32_t active_tiles(uint32_t total) { return div_up(total, kActiveTile); }
+uint32_t slot_tiles(uint32_t slots) { return div_up(slots, kActTile); }
+// one CTA per range of active blocks: 5 resident CTAs per SM at most
+uint32_t mc_grid(bcmc_ctx* ctx, uint32_t max_active)
+{
+    const uint32_t r = (uint32_t)ctx->num_sms * 5u, tiles = div_up(max_active ? max_active : 1, kMcBlocks);
+    return tiles < r ? tiles : r;
+}
 
 }  // namespace bcmc

@@ -82,9 +82,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(QueryState* q, const uint
         if (tile >= ntiles) break;
         uint32_t vals[kScanItems], excl, total;
         tile_scan(in, n, tile, s_buf, s_warp, [](uint32_t v) { return v; }, vals, &excl, &total);
-        if (threadIdx.x == 0) {
-            s_prefix = lookback_exclusive(status, tile, total, epoch, &q->error, 1u);
-            if (tile == ntiles - 1 && d_total) *d_total = s_prefix + total;
+        if (threadIdx.x < 32) {
+            const uint32_t p = warp_lookback(status, tile, total, epoch, &q->error, 1u);
+            if (threadIdx.x == 0) {
+                s_prefix = p;
+                if (tile == ntiles - 1 && d_total) *d_total = p + total;
+            }
         }
         __syncthreads();
         uint32_t run = s_prefix + excl;
@@ -122,9 +125,12 @@ __global__ void __launch_bounds__(kScanThreads) k_select(QueryState* q, const ui
         uint32_t vals[kScanItems], excl, total;
         tile_scan(flags, n, tile, s_buf, s_warp, [](uint32_t v) { return v != 0u ? 1u : 0u; }, vals, &excl,
                   &total);
-        if (threadIdx.x == 0) {
-            s_prefix = lookback_exclusive(status, tile, total, epoch, &q->error, 2u);
-            if (tile == ntiles - 1 && d_count) *d_count = s_prefix + total;
+        if (threadIdx.x < 32) {
+            const uint32_t p = warp_lookback(status, tile, total, epoch, &q->error, 2u);
+            if (threadIdx.x == 0) {
+                s_prefix = p;
+                if (tile == ntiles - 1 && d_count) *d_count = p + total;
+            }
         }
         __syncthreads();
         uint32_t pos = s_prefix + excl;

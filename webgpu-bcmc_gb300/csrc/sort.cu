@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(QueryState* q, const
         uint32_t tile_total;
         const uint32_t start = cta_exclusive_scan<kSortThreads>(run, s_warp_sums, &tile_total);
         s_start[t] = start;
-        const uint32_t excl = lookback_exclusive(b.status + t, tile, run, epoch, &q->error, 20u + pass, 256u);
+        const uint32_t excl = lookback_exclusive_w8(b.status + t, tile, run, epoch, &q->error, 20u + pass, 256u);
         s_gbase[t] = bucket[t] + excl - start;
         __syncthreads();
 #pragma unroll
