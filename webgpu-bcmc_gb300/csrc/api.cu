@@ -233,14 +233,19 @@ static void lru_grow_capacity(bcmc_lru* c, uint32_t needed)
     lru_free_slots(&tmp);
 }
 
-static void lru_begin(bcmc_lru* c, cudaStream_t s, float iso, int mc_only, uint32_t vert_capacity)
+// Epoch rewind well before the 2^28 limit of the sort's status tags.
+static void lru_epoch_tick(bcmc_lru* c, cudaStream_t s)
 {
-    // epoch rewind well before the 2^28 limit of the sort's status tags
     if (++c->epoch_calls >= (1ull << 26)) {
         BCMC_CUDA(cudaMemsetAsync(c->status, 0, c->status_words * 8, s));
         BCMC_CUDA(cudaMemsetAsync(&c->q->epoch, 0, 4, s));
         c->epoch_calls = 1;
     }
+}
+
+static void lru_begin(bcmc_lru* c, cudaStream_t s, float iso, int mc_only, uint32_t vert_capacity)
+{
+    lru_epoch_tick(c, s);
     query_begin_launch(c->q, iso, mc_only, c->capacity, vert_capacity, s);
 }
 
@@ -364,6 +369,12 @@ struct bcmc_vol {
     bcmc_lru* lru = nullptr;
     bcmc_stats stats{};
     cudaEvent_t ev[5]{};
+    // the query as one CUDA graph: inputs copied from pinned memory, state
+    // copied back to pinned memory; re-captured when a buffer is regrown
+    QueryInputs* h_in = nullptr;  // pinned
+    cudaGraphExec_t graph = nullptr;
+    uint64_t graph_key[4]{};
+    uint64_t graph_kernels = 0;
 };
 
 static void vol_free(bcmc_vol* v)
@@ -382,6 +393,8 @@ static void vol_free(bcmc_vol* v)
     lru_delete(v->lru);
     for (auto& e : v->ev)
         if (e) cudaEventDestroy(e);
+    if (v->graph) cudaGraphExecDestroy(v->graph);
+    if (v->h_in) cudaFreeHost(v->h_in);
     delete v;
     ctx_child_removed(ctx);
 }
@@ -449,6 +462,7 @@ static bcmc_status vol_create_common(bcmc_ctx* ctx, const void* src, bool src_de
             v->vert_capacity = init_verts;
             v->verts_storage = 0;
             for (auto& e : v->ev) BCMC_CUDA(cudaEventCreate(&e));
+            BCMC_CUDA(cudaMallocHost(&v->h_in, sizeof(QueryInputs)));
             zfp_ranges_launch(ctx, v->words, v->dims, max_bits, v->ranges, s);
             BCMC_CUDA(cudaStreamSynchronize(s));
             v->stats.totalBlocks = v->total;
@@ -547,6 +561,67 @@ bcmc_status bcmc_volume_create_device(bcmc_ctx* ctx, const void* d_zfp, size_t l
 
 void bcmc_volume_destroy(bcmc_vol* v) { vol_free(v); }
 
+// The kernels of one query, in order, on stream s (captured into the graph).
+static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_state)
+{
+    bcmc_ctx* ctx = v->ctx;
+    bcmc_lru* c = v->lru;
+    const uint3 nb = make_uint3(v->nb[0], v->nb[1], v->nb[2]);
+    const BlockGrid grid = make_block_grid(nb);
+    ActiveArgs aa{reinterpret_cast<const float2*>(v->ranges), nb, grid, nullptr, v->active, c->item_slots,
+                  v->total, v->active_ids, c->new_ids, c->st_active_a, c->st_active_n};
+    McArgs ma{v->active, v->active_ids, c->item_slots, reinterpret_cast<const float*>(c->cache), nb, grid,
+              v->with_verts, v->vert_offsets, v->block_counts, v->verts, c->st_mc_v, c->st_mc_b};
+    SlotArgs sa{v->active, c->slot_age, c->slot_avail, c->slot_item, c->avail_ids, c->avail_keys, c->st_slots, 1u};
+    AssignArgs as{c->new_ids, c->sort_bv, c->sort_cv, c->slot_age, c->slot_avail, c->slot_item,
+                  c->item_slots, v->words, v->max_bits, reinterpret_cast<float*>(c->cache)};
+    BCMC_CUDA(cudaEventRecordWithFlags(v->ev[0], s, cudaEventRecordExternal));
+    query_begin_launch(c->q, iso, 0, c->capacity, v->vert_capacity, s, from_state);
+    active_launch(ctx, c->q, aa, s);
+    BCMC_CUDA(cudaEventRecordWithFlags(v->ev[1], s, cudaEventRecordExternal));
+    slots_launch(ctx, c->q, sa, c->capacity, s);
+    sort_launch(ctx, c->q, &c->q->num_avail, c->capacity, lru_sort_buffers(c), 1, s);
+    BCMC_CUDA(cudaEventRecordWithFlags(v->ev[2], s, cudaEventRecordExternal));
+    assign_launch(ctx, c->q, as, v->total, s);
+    BCMC_CUDA(cudaEventRecordWithFlags(v->ev[3], s, cudaEventRecordExternal));
+    mc_launch(ctx, c->q, ma, v->total, s);
+    BCMC_CUDA(cudaEventRecordWithFlags(v->ev[4], s, cudaEventRecordExternal));
+    BCMC_CUDA(cudaMemcpyAsync(c->h_q, c->q, sizeof(QueryState), cudaMemcpyDeviceToHost, s));
+}
+
+// Captures the query into a CUDA graph if the buffers it refers to changed.
+static void vol_ensure_graph(bcmc_vol* v)
+{
+    bcmc_lru* c = v->lru;
+    const uint64_t key[4] = {c->capacity, v->vert_capacity, (uint64_t)(uintptr_t)v->verts,
+                             (uint64_t)(uintptr_t)c->cache};
+    if (v->graph && std::memcmp(key, v->graph_key, sizeof(key)) == 0) return;
+    if (v->graph) {
+        cudaGraphExecDestroy(v->graph);
+        v->graph = nullptr;
+    }
+    cudaStream_t s = v->ctx->stream;
+    const uint64_t before = g_kernel_launches.load();
+    BCMC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaGraph_t g = nullptr;
+    try {
+        BCMC_CUDA(cudaMemcpyAsync(&c->q->in, v->h_in, sizeof(QueryInputs), cudaMemcpyHostToDevice, s));
+        vol_enqueue_query(v, s, 0.0f, 1);
+    } catch (...) {
+        cudaStreamEndCapture(s, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    BCMC_CUDA(cudaStreamEndCapture(s, &g));
+    const cudaError_t e = cudaGraphInstantiate(&v->graph, g, 0);
+    cudaGraphDestroy(g);
+    BCMC_CUDA(e);
+    // captured launches did not run: count them per replay instead
+    v->graph_kernels = g_kernel_launches.load() - before;
+    g_kernel_launches.fetch_sub(v->graph_kernels);
+    std::memcpy(v->graph_key, key, sizeof(key));
+}
+
 bcmc_status bcmc_compute_surface(bcmc_vol* v, float iso, bcmc_perf* perf, uint32_t* num_vertices)
 {
     if (!v) return BCMC_E_ARG;
@@ -554,29 +629,13 @@ bcmc_status bcmc_compute_surface(bcmc_vol* v, float iso, bcmc_perf* perf, uint32
     return guarded(ctx, [&]() -> bcmc_status {
         bcmc_lru* c = v->lru;
         cudaStream_t s = ctx->stream;
-        const uint3 nb = make_uint3(v->nb[0], v->nb[1], v->nb[2]);
-        ActiveArgs aa{reinterpret_cast<const float2*>(v->ranges), nb, nullptr, v->active, c->item_slots, v->total,
-                      v->active_ids, c->new_ids, c->st_active_a, c->st_active_n};
-        McArgs ma{v->active, v->active_ids, c->item_slots, reinterpret_cast<const float*>(c->cache), nb,
-                  v->with_verts, v->vert_offsets, v->block_counts, v->verts, c->st_mc_v, c->st_mc_b};
         for (int attempt = 0;; ++attempt) {
-            if (perf) BCMC_CUDA(cudaEventRecord(v->ev[0], s));
-            lru_begin(c, s, iso, 0, v->vert_capacity);
-            active_launch(ctx, c->q, aa, s);
-            if (perf) BCMC_CUDA(cudaEventRecord(v->ev[1], s));
-            SlotArgs sa{v->active, c->slot_age, c->slot_avail, c->slot_item, c->avail_ids, c->avail_keys, c->st_slots, 1u};
-            slots_launch(ctx, c->q, sa, c->capacity, s);
-            sort_launch(ctx, c->q, &c->q->num_avail, c->capacity, lru_sort_buffers(c), 1, s);
-            if (perf) BCMC_CUDA(cudaEventRecord(v->ev[2], s));
-            AssignArgs as{c->new_ids, c->sort_bv, c->sort_cv, c->slot_age, c->slot_avail, c->slot_item,
-                          c->item_slots, v->words, v->max_bits, reinterpret_cast<float*>(c->cache)};
-            assign_launch(ctx, c->q, as, v->total, s);
-            if (perf) BCMC_CUDA(cudaEventRecord(v->ev[3], s));
-            ma.cache = reinterpret_cast<const float*>(c->cache);
-            ma.verts = v->verts;
-            mc_launch(ctx, c->q, ma, v->total, s);
-            if (perf) BCMC_CUDA(cudaEventRecord(v->ev[4], s));
-            lru_read_state(c, s);
+            vol_ensure_graph(v);
+            lru_epoch_tick(c, s);
+            *v->h_in = QueryInputs{iso, c->capacity, v->vert_capacity, 0u};
+            BCMC_CUDA(cudaGraphLaunch(v->graph, s));
+            count_launches(v->graph_kernels);
+            BCMC_CUDA(cudaStreamSynchronize(s));
             if (c->h_q->error) return fail(ctx, BCMC_E_TIMEOUT, "device wait timed out (site " + std::to_string(c->h_q->error) + ")");
             if (c->h_q->grow_needed) {
                 if (attempt > 2) return fail(ctx, BCMC_E_STATE, "cache growth did not converge");
@@ -585,6 +644,10 @@ bcmc_status bcmc_compute_surface(bcmc_vol* v, float iso, bcmc_perf* perf, uint32
             }
             break;
         }
+        const uint3 nb = make_uint3(v->nb[0], v->nb[1], v->nb[2]);
+        McArgs ma{v->active, v->active_ids, c->item_slots, reinterpret_cast<const float*>(c->cache), nb,
+                  make_block_grid(nb), v->with_verts, v->vert_offsets, v->block_counts, v->verts, c->st_mc_v,
+                  c->st_mc_b};
         QueryState& h = *c->h_q;
         if (h.num_active > 0 && h.num_verts > 0 && h.vert_overflow) {
             vol_grow_verts(v, h.num_verts);
@@ -743,8 +806,8 @@ bcmc_status bcmc_lru_update(bcmc_lru* c, const uint32_t* d_item_needed, uint32_t
         cudaStream_t s = ctx->stream;
         for (int attempt = 0;; ++attempt) {
             lru_begin(c, s, 0.0f, 0, 0);
-            ActiveArgs aa{nullptr, make_uint3(0, 0, 0), d_item_needed, nullptr, c->item_slots, c->total, nullptr,
-                          c->new_ids, c->st_active_a, c->st_active_n};
+            ActiveArgs aa{nullptr, make_uint3(0, 0, 0), make_block_grid(make_uint3(1, 1, 1)), d_item_needed, nullptr,
+                          c->item_slots, c->total, nullptr, c->new_ids, c->st_active_a, c->st_active_n};
             active_launch(ctx, c->q, aa, s);
             lru_enqueue_update(c, s, d_item_needed, nullptr, 0);
             lru_read_state(c, s);
@@ -957,8 +1020,8 @@ bcmc_status bcmc_block_active(bcmc_ctx* ctx, const float* d_ranges, const uint32
         const uint64_t total = (uint64_t)nb.x * nb.y * nb.z;
         ensure_status(ctx, 2 * (active_tiles((uint32_t)total) + 1));
         query_begin_launch(ctx->d_prim, iso, 0, 0, 0, s);
-        ActiveArgs aa{reinterpret_cast<const float2*>(d_ranges), nb, nullptr, d_active, nullptr, (uint32_t)total,
-                      nullptr, nullptr, ctx->d_status, ctx->d_status + active_tiles((uint32_t)total) + 1};
+        ActiveArgs aa{reinterpret_cast<const float2*>(d_ranges), nb, make_block_grid(nb), nullptr, d_active, nullptr,
+                      (uint32_t)total, nullptr, nullptr, ctx->d_status, ctx->d_status + active_tiles((uint32_t)total) + 1};
         active_launch(ctx, ctx->d_prim, aa, s);
         return BCMC_OK;
     });

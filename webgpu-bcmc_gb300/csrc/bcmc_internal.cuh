@@ -18,7 +18,17 @@ constexpr uint32_t kSpinLimit = 1u << 22;  // bounded device-side waits
 // query is a fixed sequence of launches with no host round trip in between;
 // the host reads this struct once at the end of the query.
 // ---------------------------------------------------------------------------
+// Inputs of one query as the host writes them (pinned memory, copied in by the
+// first node of a query's CUDA graph).
+struct QueryInputs {
+    float isovalue;
+    uint32_t capacity;
+    uint32_t vert_capacity;
+    uint32_t mc_only;
+};
+
 struct QueryState {
+    QueryInputs in;  // copy of the host inputs (graph launches)
     // inputs written by the host (or the query-init kernel)
     float isovalue;
     uint32_t epoch;          // tags the decoupled-lookback status words
@@ -278,6 +288,53 @@ __device__ __forceinline__ uint32_t cta_exclusive_scan(uint32_t v, uint32_t* war
     *total = warp_sums[kWarps];
     __syncthreads();
     return r;
+}
+
+// Division by a run-time invariant divisor as a multiply-high and shifts
+// (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994): exact for every 32-bit dividend.
+struct FastDiv {
+    uint32_t d, m, s;
+};
+
+__host__ __device__ inline FastDiv make_fastdiv(uint32_t d)
+{
+    FastDiv f{d, 0u, 0u};
+    if (d > 1) {
+        uint32_t l = 0;
+        while ((1ull << l) < d) ++l;  // l = ceil(log2 d)
+        f.m = (uint32_t)((((1ull << l) - d) << 32) / d + 1ull);
+        f.s = l;
+    }
+    return f;
+}
+
+__host__ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f)
+{
+#ifdef __CUDA_ARCH__
+    if (f.d == 1) return n;
+    const uint32_t t = __umulhi(n, f.m);
+#else
+    if (f.d == 1) return n;
+    const uint32_t t = (uint32_t)(((uint64_t)n * f.m) >> 32);
+#endif
+    return (t + ((n - t) >> 1)) >> (f.s - 1);
+}
+
+// block id -> (x, y, z) for a grid of nb.x * nb.y * nb.z blocks
+struct BlockGrid {
+    uint3 nb;
+    FastDiv dx, dxy;
+};
+
+inline BlockGrid make_block_grid(uint3 nb) { return BlockGrid{nb, make_fastdiv(nb.x), make_fastdiv(nb.x * nb.y)}; }
+
+__device__ __forceinline__ uint3 block_coords(uint32_t id, const BlockGrid& g)
+{
+    const uint32_t z = fdiv(id, g.dxy);
+    const uint32_t r = id - z * g.nb.x * g.nb.y;
+    const uint32_t y = fdiv(r, g.dx);
+    return make_uint3(r - y * g.nb.x, y, z);
 }
 
 __host__ __device__ __forceinline__ uint32_t align_up(uint32_t v, uint32_t a)

@@ -9,6 +9,7 @@ namespace bcmc {
 struct ActiveArgs {
     const float2* ranges;     // set: test ranges against the isovalue (MC path)
     uint3 nb;                 // blocks per axis
+    BlockGrid grid;           // id -> (x, y, z) without integer division
     const uint32_t* item_needed;  // set instead of ranges: standalone LRU update
     uint32_t* active_out;     // per-block active flags (MC path)
     const int32_t* item_slots;  // cachedItemSlots
@@ -51,6 +52,7 @@ struct McArgs {
     const int32_t* item_slots;
     const float* cache;
     uint3 nb;
+    BlockGrid grid;
     uint32_t* with_verts;
     uint32_t* vert_offsets;
     uint32_t* block_counts;  // vertices of each active block (count pass -> emit pass)
@@ -60,7 +62,7 @@ struct McArgs {
 };
 
 void query_begin_launch(QueryState* q, float iso, int mc_only, uint32_t capacity, uint32_t vert_capacity,
-                        cudaStream_t s);
+                        cudaStream_t s, int from_state = 0);
 void active_launch(bcmc_ctx* ctx, QueryState* q, const ActiveArgs& a, cudaStream_t s);
 void slots_launch(bcmc_ctx* ctx, QueryState* q, const SlotArgs& a, uint32_t max_slots, cudaStream_t s);
 void assign_launch(bcmc_ctx* ctx, QueryState* q, const AssignArgs& a, uint32_t max_new, cudaStream_t s);

@@ -36,9 +36,18 @@ __constant__ uint8_t c_corner[8] = {0, 1, 3, 2, 4, 5, 7, 6};
 __constant__ uint8_t c_edge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {6, 5},
                                       {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
 
-__global__ void k_query_begin(QueryState* q, float iso, int mc_only, uint32_t capacity, uint32_t vert_capacity)
+// Starts a query: inputs come from the arguments, or, when `from_state` is
+// set, from q->in (written by the graph's host-to-device copy).
+__global__ void k_query_begin(QueryState* q, float iso, int mc_only, uint32_t capacity, uint32_t vert_capacity,
+                              int from_state)
 {
     const int t = threadIdx.x;
+    if (from_state) {
+        iso = q->in.isovalue;
+        mc_only = (int)q->in.mc_only;
+        capacity = q->in.capacity;
+        vert_capacity = q->in.vert_capacity;
+    }
     if (t == 0) {
         q->epoch += 1;
         q->capacity = capacity;
@@ -64,10 +73,10 @@ __global__ void k_query_begin(QueryState* q, float iso, int mc_only, uint32_t ca
 // k_active
 // ---------------------------------------------------------------------------
 constexpr int kActThreads = 256;
-constexpr int kActItems = 8;
-constexpr int kActTile = kActThreads * kActItems;  // slots per k_slots tile
-constexpr int kActiveItems = 2;
+constexpr int kActiveItems = 4;
 constexpr int kActiveTile = kActThreads * kActiveItems;  // blocks per k_active tile
+constexpr int kSlotItems = 2;
+constexpr int kSlotTile = kActThreads * kSlotItems;  // slots per k_slots tile
 
 __device__ __forceinline__ uint32_t spad8(uint32_t i) { return i + (i >> 5); }
 
@@ -77,12 +86,14 @@ __device__ __forceinline__ uint32_t spad8(uint32_t i) { return i + (i >> 5); }
 // neighbours (and b itself, which adds nothing new):
 //   active = (A_b && anyB) || (B_b && anyA) || any(A_n && B_n)
 // -- the same booleans, evaluated without branches or early exits.
-__device__ __forceinline__ uint32_t block_is_active(const float2* __restrict__ ranges, uint3 nb, uint32_t b,
-                                                    float iso)
+__device__ __forceinline__ uint32_t block_is_active(const float2* __restrict__ ranges, const BlockGrid& g,
+                                                    uint32_t b, float iso)
 {
+    const uint3 nb = g.nb;
     const float2 r = __ldg(ranges + b);
     const bool A = iso >= r.x, B = iso <= r.y;
-    const int bx = (int)(b % nb.x), by = (int)((b / nb.x) % nb.y), bz = (int)(b / (nb.x * nb.y));
+    const uint3 c = block_coords(b, g);
+    const int bx = (int)c.x, by = (int)c.y, bz = (int)c.z;
     bool anyA = false, anyB = false, anyC = false;
 #pragma unroll
     for (int k = -1; k < 2; ++k)
@@ -101,9 +112,53 @@ __device__ __forceinline__ uint32_t block_is_active(const float2* __restrict__ r
     return ((A && anyB) || (B && anyA) || anyC) ? 1u : 0u;
 }
 
+__device__ __forceinline__ void range_bits(const float2 r, float iso, uint32_t& a, uint32_t& b)
+{
+    a = iso >= r.x ? 1u : 0u;
+    b = iso <= r.y ? 1u : 0u;
+}
+
+// Active flags of the 4 consecutive blocks b0..b0+3 of one x-row: the 9
+// neighbour rows (y-1..y+1, z-1..z+1) are read once for the 4 blocks (6 ranges
+// per row), 13.5 loads per block instead of 27.
+__device__ __forceinline__ uint32_t row4_active(const float2* __restrict__ ranges, const BlockGrid& g, uint3 c,
+                                                uint32_t b0, float iso)
+{
+    const uint3 nb = g.nb;
+    uint32_t anyA = 0, anyB = 0, anyC = 0, selfA = 0, selfB = 0;  // bit i = block b0+i
+#pragma unroll
+    for (int dz = -1; dz < 2; ++dz)
+#pragma unroll
+        for (int dy = -1; dy < 2; ++dy) {
+            const int yy = (int)c.y + dy, zz = (int)c.z + dz;
+            if (yy < 0 || zz < 0 || yy >= (int)nb.y || zz >= (int)nb.z) continue;
+            const int64_t shift = (int64_t)dy * nb.x + (int64_t)dz * nb.x * nb.y;
+            const float2* row = ranges + (int64_t)b0 + shift;  // position x0 of the neighbour row
+            uint32_t A = 0, B = 0;  // bit p = position x0 - 1 + p, p = 0..5
+#pragma unroll
+            for (int p = 0; p < 6; ++p) {
+                const int xx = (int)c.x - 1 + p;
+                if (xx < 0 || xx >= (int)nb.x) continue;
+                uint32_t a, b;
+                range_bits(__ldg(row + (p - 1)), iso, a, b);
+                A |= a << p;
+                B |= b << p;
+            }
+            const uint32_t C = A & B;
+            // window of block i covers positions i..i+2
+            anyA |= (A | (A >> 1) | (A >> 2)) & 15u;
+            anyB |= (B | (B >> 1) | (B >> 2)) & 15u;
+            anyC |= (C | (C >> 1) | (C >> 2)) & 15u;
+            if (dy == 0 && dz == 0) {
+                selfA = (A >> 1) & 15u;
+                selfB = (B >> 1) & 15u;
+            }
+        }
+    return ((selfA & anyB) | (selfB & anyA) | anyC) & 15u;
+}
+
 __global__ void __launch_bounds__(kActThreads) k_active(QueryState* q, ActiveArgs a)
 {
-    __shared__ uint8_t s_flags[kActiveTile + kActiveTile / 32];
     __shared__ uint32_t s_warp[kActThreads / 32 + 1];
     __shared__ uint32_t s_tile, s_pa, s_pn;
     const uint32_t total = a.total;
@@ -115,33 +170,37 @@ __global__ void __launch_bounds__(kActThreads) k_active(QueryState* q, ActiveArg
         __syncthreads();
         const uint32_t tile = s_tile;
         if (tile >= ntiles) break;
-        const uint32_t base = tile * kActiveTile;
-#pragma unroll
-        for (int j = 0; j < kActiveItems; ++j) {
-            const uint32_t local = j * kActThreads + threadIdx.x;
-            const uint32_t b = base + local;
-            uint32_t f = 0;
-            if (b < total) {
-                uint32_t act;
-                if (a.ranges) {
-                    act = block_is_active(a.ranges, a.nb, b, iso);
-                    a.active_out[b] = act;
+        // thread -> 4 consecutive blocks (thread-blocked order = block order)
+        const uint32_t b0 = tile * kActiveTile + kActiveItems * threadIdx.x;
+        uint32_t act = 0, need = 0;  // bit i = block b0 + i
+        if (b0 < total) {
+            const uint32_t n = min(4u, total - b0);
+            if (a.ranges) {
+                const uint3 c = block_coords(b0, a.grid);
+                if (n == 4 && c.x + 3 < a.grid.nb.x) {
+                    act = row4_active(a.ranges, a.grid, c, b0, iso);
                 } else {
-                    act = a.item_needed[b] != 0u ? 1u : 0u;
+                    for (uint32_t i = 0; i < n; ++i) act |= block_is_active(a.ranges, a.grid, b0 + i, iso) << i;
                 }
-                const uint32_t need = (act && a.item_slots && a.item_slots[b] < 0) ? 1u : 0u;
-                f = act | (need << 1);
+                if (n == 4)
+                    *reinterpret_cast<uint4*>(a.active_out + b0) =
+                        make_uint4(act & 1u, (act >> 1) & 1u, (act >> 2) & 1u, (act >> 3) & 1u);
+                else
+                    for (uint32_t i = 0; i < n; ++i) a.active_out[b0 + i] = (act >> i) & 1u;
+            } else {
+                for (uint32_t i = 0; i < n; ++i) act |= (a.item_needed[b0 + i] != 0u ? 1u : 0u) << i;
             }
-            s_flags[spad8(local)] = (uint8_t)f;
+            if (a.item_slots && act) {
+                if (n == 4) {
+                    const int4 s4 = __ldg(reinterpret_cast<const int4*>(a.item_slots + b0));
+                    need = (s4.x < 0 ? 1u : 0u) | (s4.y < 0 ? 2u : 0u) | (s4.z < 0 ? 4u : 0u) | (s4.w < 0 ? 8u : 0u);
+                } else {
+                    for (uint32_t i = 0; i < n; ++i) need |= (a.item_slots[b0 + i] < 0 ? 1u : 0u) << i;
+                }
+                need &= act;
+            }
         }
-        __syncthreads();
-        uint32_t cnt = 0;
-        uint8_t fl[kActiveItems];
-#pragma unroll
-        for (int j = 0; j < kActiveItems; ++j) {
-            fl[j] = s_flags[spad8(threadIdx.x * kActiveItems + j)];
-            cnt += (fl[j] & 1u) | ((uint32_t)(fl[j] >> 1) << 16);
-        }
+        const uint32_t cnt = (uint32_t)__popc(act) | ((uint32_t)__popc(need) << 16);
         uint32_t tot;
         const uint32_t excl = cta_exclusive_scan<kActThreads>(cnt, s_warp, &tot);
         if (threadIdx.x < 32) {
@@ -153,15 +212,14 @@ __global__ void __launch_bounds__(kActThreads) k_active(QueryState* q, ActiveArg
         }
         __syncthreads();
         uint32_t pa = s_pa + (excl & 0xffffu), pn = s_pn + (excl >> 16);
-        const uint32_t first = base + threadIdx.x * kActiveItems;
 #pragma unroll
-        for (int j = 0; j < kActiveItems; ++j) {
-            if (fl[j] & 1u) {
-                if (a.active_ids) a.active_ids[pa] = first + j;
+        for (uint32_t i = 0; i < 4; ++i) {
+            if (act >> i & 1u) {
+                if (a.active_ids) a.active_ids[pa] = b0 + i;
                 ++pa;
             }
-            if (fl[j] & 2u) {
-                if (a.new_ids) a.new_ids[pn] = first + j;
+            if (need >> i & 1u) {
+                if (a.new_ids) a.new_ids[pn] = b0 + i;
                 ++pn;
             }
         }
@@ -201,22 +259,22 @@ __global__ void __launch_bounds__(kActThreads) k_active(QueryState* q, ActiveArg
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a)
 {
-    __shared__ uint8_t s_flags[kActTile + kActTile / 32];
+    __shared__ uint8_t s_flags[kSlotTile + kSlotTile / 32];
     __shared__ uint32_t s_warp[kActThreads / 32 + 1];
     __shared__ uint32_t s_tile, s_prefix;
     if ((a.skip_when_inactive && q->num_active == 0) || q->grow_needed) return;
     const uint32_t old = q->old_cache_size, nsz = q->new_cache_size;
     const bool compact = q->num_new > 0;
-    const uint32_t ntiles = div_up(nsz, kActTile);
+    const uint32_t ntiles = div_up(nsz, kSlotTile);
     const uint32_t epoch = q->epoch;
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(&q->tiles_slots, 1u);
         __syncthreads();
         const uint32_t tile = s_tile;
         if (tile >= ntiles) break;
-        const uint32_t base = tile * kActTile;
+        const uint32_t base = tile * kSlotTile;
 #pragma unroll
-        for (int j = 0; j < kActItems; ++j) {
+        for (int j = 0; j < kSlotItems; ++j) {
             const uint32_t local = j * kActThreads + threadIdx.x;
             const uint32_t s = base + local;
             uint32_t av = 0;
@@ -238,10 +296,10 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
         if (compact) {
             __syncthreads();
             uint32_t cnt = 0;
-            uint8_t fl[kActItems];
+            uint8_t fl[kSlotItems];
 #pragma unroll
-            for (int j = 0; j < kActItems; ++j) {
-                fl[j] = s_flags[spad8(threadIdx.x * kActItems + j)];
+            for (int j = 0; j < kSlotItems; ++j) {
+                fl[j] = s_flags[spad8(threadIdx.x * kSlotItems + j)];
                 cnt += fl[j];
             }
             uint32_t tot;
@@ -252,9 +310,9 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
             }
             __syncthreads();
             uint32_t p = s_prefix + excl;
-            const uint32_t first = base + threadIdx.x * kActItems;
+            const uint32_t first = base + threadIdx.x * kSlotItems;
 #pragma unroll
-            for (int j = 0; j < kActItems; ++j)
+            for (int j = 0; j < kSlotItems; ++j)
                 if (fl[j]) {
                     const uint32_t s = first + j;
                     a.avail_ids[p] = s;
@@ -291,7 +349,7 @@ __global__ void __launch_bounds__(128) k_assign(QueryState* q, AssignArgs a)
         a.item_slots[item] = (int32_t)slot;
         if (a.words) {
             float v[64];
-            zfp_decode_block(a.words, (uint64_t)item * a.max_bits, a.max_bits, v);
+            zfp_decode_block<true>(a.words, (uint64_t)item * a.max_bits, a.max_bits, v);
             float4* d4 = reinterpret_cast<float4*>(a.cache + (uint64_t)slot * 64u);
 #pragma unroll
             for (int k = 0; k < 16; ++k) d4[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
@@ -380,6 +438,8 @@ __global__ void __launch_bounds__(kMcThreads) k_mc(QueryState* q, McArgs a)
     __shared__ uint32_t s_act[kMcBlocks];
     __shared__ uint32_t s_warp[kMcThreads / 32 + 1];
     __shared__ uint32_t s_any, s_pv, s_pb, s_cta_v, s_cta_b;
+    __shared__ uint16_t s_ghost[64];  // per-lane table reads: shared, not __constant__ memory
+    __shared__ uint8_t s_nb_off[8];
 
     const uint32_t A = q->num_active;
     if (A == 0 || q->grow_needed) return;
@@ -403,6 +463,8 @@ __global__ void __launch_bounds__(kMcThreads) k_mc(QueryState* q, McArgs a)
         }
         if (t < 12) s_edge[t] = (uint8_t)(c_corner[c_edge[t][0]] | (c_corner[c_edge[t][1]] << 3));
         if (t == 0) s_cta_v = s_cta_b = 0;
+        if (t < 61) s_ghost[t] = c_ghost[t];
+        if (t < 7) s_nb_off[t] = c_nb_off[t];
     }
     // thread -> (block j, cells 4u..4u+3 = the x-row (y, z) = (u & 3, u >> 2))
     const uint32_t j = t >> 4, u = t & 15u, ry = u & 3u, rz = u >> 2;
@@ -452,11 +514,15 @@ __global__ void __launch_bounds__(kMcThreads) k_mc(QueryState* q, McArgs a)
                 const uint32_t jb = t >> 3, k = t & 7u, id = s_id[jb];
                 uint32_t slot = 0xffffffffu, act = 0;
                 if (id != 0xffffffffu) {
-                    const uint32_t bx = id % nb.x, by = (id / nb.x) % nb.y, bz = id / (nb.x * nb.y);
+                    const uint3 bc = block_coords(id, a.grid);
+                    const uint32_t bx = bc.x, by = bc.y, bz = bc.z;
                     if (k == kNbSelf) {
                         slot = (uint32_t)__ldg(a.item_slots + id);
+                        // which +x/+y/+z neighbours exist (bits 8-10 of s_act)
+                        act = (bx + 1 < nb.x ? 0x100u : 0u) | (by + 1 < nb.y ? 0x200u : 0u) |
+                              (bz + 1 < nb.z ? 0x400u : 0u);
                     } else {
-                        const uint32_t o = c_nb_off[k], ox = o & 1u, oy = (o >> 1) & 1u, oz = o >> 2;
+                        const uint32_t o = s_nb_off[k], ox = o & 1u, oy = (o >> 1) & 1u, oz = o >> 2;
                         if (bx + ox < nb.x && by + oy < nb.y && bz + oz < nb.z) {
                             const uint32_t nid = id + ox + nb.x * (oy + nb.y * oz);
                             act = __ldg(a.active + nid) != 0u ? 1u : 0u;
@@ -465,8 +531,8 @@ __global__ void __launch_bounds__(kMcThreads) k_mc(QueryState* q, McArgs a)
                     }
                 }
                 s_slot[jb][k] = slot;
-                const uint32_t bits = __ballot_sync(0xffffffffu, act != 0u);  // 4 blocks per warp
-                if ((t & 7u) == 0) s_act[jb] = (bits >> (t & 24u)) & 0x7fu;
+                const uint32_t bits = __ballot_sync(0xffffffffu, (act & 1u) != 0u);  // 4 blocks per warp
+                if (k == kNbSelf) s_act[jb] = ((bits >> (t & 24u)) & 0x7fu) | act;
             }
             __syncthreads();
             // grid of each block (+ ghost layer) in shared memory
@@ -474,8 +540,8 @@ __global__ void __launch_bounds__(kMcThreads) k_mc(QueryState* q, McArgs a)
             const bool valid = id != 0xffffffffu;
             uint32_t dims = 0;
             if (valid) {
-                const uint32_t bx = id % nb.x, by = (id / nb.x) % nb.y, bz = id / (nb.x * nb.y);
-                dims = block_dims_with_ghost(s_act[j], bx + 1 < nb.x, by + 1 < nb.y, bz + 1 < nb.z);
+                const uint32_t act = s_act[j];
+                dims = block_dims_with_ghost(act, (act & 0x100u) != 0u, (act & 0x200u) != 0u, (act & 0x400u) != 0u);
                 const uint32_t slot = s_slot[j][kNbSelf];
                 if (slot < slots) {
                     const float4 v4 = __ldg(reinterpret_cast<const float4*>(a.cache + (uint64_t)slot * 64u) + u);
@@ -490,7 +556,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc(QueryState* q, McArgs a)
                 const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
 #pragma unroll
                 for (uint32_t gi = u; gi < 61; gi += 16) {
-                    const uint32_t g = c_ghost[gi];
+                    const uint32_t g = s_ghost[gi];
                     const uint32_t gx = g & 15u, gy = (g >> 4) & 15u, gz = (g >> 8) & 15u;
                     if (gx < dx && gy < dy && gz < dz) {
                         const uint32_t nslot = s_slot[j][g >> 12];
@@ -593,9 +659,9 @@ static int pgrid(bcmc_ctx* ctx, uint32_t tiles, uint32_t per_sm)
 }
 
 void query_begin_launch(QueryState* q, float iso, int mc_only, uint32_t capacity, uint32_t vert_capacity,
-                        cudaStream_t s)
+                        cudaStream_t s, int from_state)
 {
-    k_query_begin<<<1, 256, 0, s>>>(q, iso, mc_only, capacity, vert_capacity);
+    k_query_begin<<<1, 256, 0, s>>>(q, iso, mc_only, capacity, vert_capacity, from_state);
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
 }
@@ -609,7 +675,7 @@ void active_launch(bcmc_ctx* ctx, QueryState* q, const ActiveArgs& a, cudaStream
 
 void slots_launch(bcmc_ctx* ctx, QueryState* q, const SlotArgs& a, uint32_t max_slots, cudaStream_t s)
 {
-    k_slots<<<pgrid(ctx, div_up(max_slots, kActTile), 4), kActThreads, 0, s>>>(q, a);
+    k_slots<<<pgrid(ctx, div_up(max_slots, kSlotTile), 8), kActThreads, 0, s>>>(q, a);
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
 }
@@ -629,7 +695,7 @@ void mc_launch(bcmc_ctx* ctx, QueryState* q, const McArgs& a, uint32_t max_activ
 }
 
 uint32_t active_tiles(uint32_t total) { return div_up(total, kActiveTile); }
-uint32_t slot_tiles(uint32_t slots) { return div_up(slots, kActTile); }
+uint32_t slot_tiles(uint32_t slots) { return div_up(slots, kSlotTile); }
 // one CTA per range of active blocks: 5 resident CTAs per SM at most
 uint32_t mc_grid(bcmc_ctx* ctx, uint32_t max_active)
 {

@@ -131,6 +131,42 @@ __device__ __forceinline__ void zfp_decode_ints(BitReader& rd, uint32_t budget, 
     }
 }
 
+// Same decode with the coefficients in registers: each plane is shifted into
+// all 64 accumulators (acc = acc*2 + bit), so the critical path is short --
+// used where a launch decodes few blocks and latency, not throughput, counts.
+__device__ __forceinline__ void zfp_decode_ints_regs(BitReader& rd, uint32_t budget, uint32_t* u)
+{
+#pragma unroll
+    for (int i = 0; i < 64; ++i) u[i] = 0;
+    uint32_t bits = budget, n = 0;
+    int k = 31;
+    for (; k >= 0 && bits != 0; --k) {
+        const uint32_t m = n < bits ? n : bits;
+        bits -= m;
+        uint64_t x = rd.bits(m);
+        while (n < 64u && bits != 0) {
+            --bits;
+            if (!rd.bit()) break;
+            const uint32_t room = 63u - (n < 63u ? n : 63u);
+            bool hit;
+            const uint32_t z = rd.skip_zeros(room < bits ? room : bits, &hit);
+            bits -= z + (hit ? 1u : 0u);
+            n += z;
+            x |= 1ull << n;
+            ++n;
+        }
+        const uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) u[i] = (u[i] << 1) | ((lo >> i) & 1u);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) u[32 + i] = (u[32 + i] << 1) | ((hi >> i) & 1u);
+    }
+    // planes k..0 were not reached: they are zero
+    const uint32_t rest = (uint32_t)(k + 1);
+#pragma unroll
+    for (int i = 0; i < 64; ++i) u[i] = rest >= 32u ? 0u : u[i] << rest;
+}
+
 __device__ __forceinline__ int32_t zfp_uint2int(uint32_t x)
 {
     return (int32_t)((x ^ 0xaaaaaaaau) - 0xaaaaaaaau);
@@ -179,6 +215,8 @@ __device__ __forceinline__ float zfp_inv_weight(int32_t emax)
 }
 
 // Decode one block starting at `bit_offset` into out[64] (natural order).
+// kLatency selects the register-resident bit-plane deposit.
+template <bool kLatency = false>
 __device__ __forceinline__ void zfp_decode_block(const uint64_t* __restrict__ words,
                                                  uint64_t bit_offset, uint32_t max_bits,
                                                  float* out)
@@ -192,7 +230,8 @@ __device__ __forceinline__ void zfp_decode_block(const uint64_t* __restrict__ wo
     }
     const int32_t emax = (int32_t)((uint32_t)rd.bits(8) - 127u);
     uint32_t u[64];
-    zfp_decode_ints(rd, max_bits - 9u, u);
+    if (kLatency) zfp_decode_ints_regs(rd, max_bits - 9u, u);
+    else zfp_decode_ints(rd, max_bits - 9u, u);
     int32_t v[64];
     uint32_t un[64];
     BCMC_ZFP_GATHER(un, u)
