@@ -6,7 +6,7 @@
 
 #include <string>
 
-#include "../../include/bcmc.h"
+#include "bcmc.h"  // include/ (on the include path)
 
 namespace bcmc {
 

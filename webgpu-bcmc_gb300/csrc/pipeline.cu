@@ -425,7 +425,7 @@ __device__ __forceinline__ uint32_t quantize(float p)
 // A CTA walks back once per launch, not once per tile, so the look-back never
 // waits on a wave of unfinished tiles.  Output order = the reference's:
 // active-block order, cell order, table order.
-__global__ void __launch_bounds__(kMcThreads) k_mc(QueryState* q, McArgs a)
+__global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
 {
     __shared__ float s_vol[kMcBlocks][128];
     __shared__ int8_t s_tri[256][16];
@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc(QueryState* q, McArgs a)
     __shared__ uint32_t s_slot[kMcBlocks][8];
     __shared__ uint32_t s_act[kMcBlocks];
     __shared__ uint32_t s_warp[kMcThreads / 32 + 1];
-    __shared__ uint32_t s_any, s_pv, s_pb, s_cta_v, s_cta_b;
+    __shared__ uint32_t s_any, s_pv, s_pb, s_cta_v, s_cta_b, s_rank;
     __shared__ uint16_t s_ghost[64];  // per-lane table reads: shared, not __constant__ memory
     __shared__ uint8_t s_nb_off[8];
 
@@ -450,8 +450,13 @@ __global__ void __launch_bounds__(kMcThreads) k_mc(QueryState* q, McArgs a)
     const uint3 nb = a.nb;
     const uint32_t t = threadIdx.x;
     const uint32_t G = gridDim.x;
+    // the CTA's place in the look-back order comes from a counter, not from
+    // blockIdx: a CTA then only waits on ranges claimed by CTAs already running
+    if (t == 0) s_rank = atomicAdd(&q->tiles_mc, 1u);
+    __syncthreads();
+    const uint32_t rank = s_rank;
     const uint32_t range = div_up(div_up(A, G), kMcBlocks) * kMcBlocks;
-    const uint32_t start = min(A, blockIdx.x * range), end = min(A, start + range);
+    const uint32_t start = min(A, rank * range), end = min(A, start + range);
     {
         const uint4* src = reinterpret_cast<const uint4*>(&kTriEdges[0][0]);
         uint4* dst = reinterpret_cast<uint4*>(&s_tri[0][0]);
@@ -475,16 +480,16 @@ __global__ void __launch_bounds__(kMcThreads) k_mc(QueryState* q, McArgs a)
             __syncthreads();
             if (t < 64) {  // warp 0: vertex offset, warp 1: offset among blocks with vertices
                 if (t < 32) {
-                    const uint32_t p = warp_lookback(a.status_v, blockIdx.x, s_cta_v, epoch, &q->error, 40u);
+                    const uint32_t p = warp_lookback(a.status_v, rank, s_cta_v, epoch, &q->error, 40u);
                     if (t == 0) {
                         s_pv = p;
-                        if (blockIdx.x == G - 1) q->num_verts = p + s_cta_v;
+                        if (rank == G - 1) q->num_verts = p + s_cta_v;
                     }
                 } else {
-                    const uint32_t p = warp_lookback(a.status_b, blockIdx.x, s_cta_b, epoch, &q->error, 41u);
+                    const uint32_t p = warp_lookback(a.status_b, rank, s_cta_b, epoch, &q->error, 41u);
                     if (t == 32) {
                         s_pb = p;
-                        if (blockIdx.x == G - 1) q->num_with_verts = p + s_cta_b;
+                        if (rank == G - 1) q->num_with_verts = p + s_cta_b;
                     }
                 }
             }
@@ -543,30 +548,39 @@ __global__ void __launch_bounds__(kMcThreads) k_mc(QueryState* q, McArgs a)
                 const uint32_t act = s_act[j];
                 dims = block_dims_with_ghost(act, (act & 0x100u) != 0u, (act & 0x200u) != 0u, (act & 0x400u) != 0u);
                 const uint32_t slot = s_slot[j][kNbSelf];
-                if (slot < slots) {
-                    const float4 v4 = __ldg(reinterpret_cast<const float4*>(a.cache + (uint64_t)slot * 64u) + u);
-                    float* row = &s_vol[j][5u * (ry + 5u * rz)];
-                    row[0] = v4.x;
-                    row[1] = v4.y;
-                    row[2] = v4.z;
-                    row[3] = v4.w;
-                } else {
-                    atomicCAS(&q->error, 0u, 51u);
-                }
+                float4 v4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (slot < slots) v4 = __ldg(reinterpret_cast<const float4*>(a.cache + (uint64_t)slot * 64u) + u);
+                else atomicCAS(&q->error, 0u, 51u);
                 const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
+                float gv[4];
+                uint32_t gaddr[4];
 #pragma unroll
-                for (uint32_t gi = u; gi < 61; gi += 16) {
-                    const uint32_t g = s_ghost[gi];
-                    const uint32_t gx = g & 15u, gy = (g >> 4) & 15u, gz = (g >> 8) & 15u;
-                    if (gx < dx && gy < dy && gz < dz) {
-                        const uint32_t nslot = s_slot[j][g >> 12];
-                        if (nslot < slots)
-                            s_vol[j][gx + 5u * (gy + 5u * gz)] = __ldg(
-                                a.cache + (uint64_t)nslot * 64u + (gx & 3u) + 4u * ((gy & 3u) + 4u * (gz & 3u)));
-                        else
-                            atomicCAS(&q->error, 0u, 52u);
+                for (uint32_t r = 0; r < 4; ++r) {
+                    const uint32_t gi = u + 16u * r;
+                    gv[r] = 0.0f;
+                    gaddr[r] = 0xffffffffu;
+                    if (gi < 61) {
+                        const uint32_t g = s_ghost[gi];
+                        const uint32_t gx = g & 15u, gy = (g >> 4) & 15u, gz = (g >> 8) & 15u;
+                        if (gx < dx && gy < dy && gz < dz) {
+                            const uint32_t nslot = s_slot[j][g >> 12];
+                            if (nslot < slots) {
+                                gv[r] = __ldg(a.cache + (uint64_t)nslot * 64u + (gx & 3u) + 4u * ((gy & 3u) + 4u * (gz & 3u)));
+                                gaddr[r] = gx + 5u * (gy + 5u * gz);
+                            } else {
+                                atomicCAS(&q->error, 0u, 52u);
+                            }
+                        }
                     }
                 }
+                float* row = &s_vol[j][5u * (ry + 5u * rz)];
+                row[0] = v4.x;
+                row[1] = v4.y;
+                row[2] = v4.z;
+                row[3] = v4.w;
+#pragma unroll
+                for (uint32_t r = 0; r < 4; ++r)
+                    if (gaddr[r] != 0xffffffffu) s_vol[j][gaddr[r]] = gv[r];
             }
             __syncthreads();
             // cases and counts of cells 4t..4t+3 (compute_block_has_vertices.comp:28-51)
@@ -635,10 +649,25 @@ __global__ void __launch_bounds__(kMcThreads) k_mc(QueryState* q, McArgs a)
                 // lerp_verts (compute_block_vertices.comp:62-74)
                 float tt = 0.0f;
                 if (!(fabsf(__fsub_rn(fa, fb)) < 0.001f)) tt = __fdiv_rn(__fsub_rn(iso, fa), __fsub_rn(fb, fa));
-                const float px = __fadd_rn(__fadd_rn(__fadd_rn((float)ax, __fmul_rn(tt, (float)((int)bx - (int)ax))), (float)x), 0.5f);
-                const float py = __fadd_rn(__fadd_rn(__fadd_rn((float)ay, __fmul_rn(tt, (float)((int)by - (int)ay))), (float)y), 0.5f);
-                const float pz = __fadd_rn(__fadd_rn(__fadd_rn((float)az, __fmul_rn(tt, (float)((int)bz - (int)az))), (float)z), 0.5f);
-                out[k] = make_uint2((quantize(px) << 20) | (quantize(py) << 10) | quantize(pz), s_id[jb]);
+                uint32_t qx, qy, qz;
+                if (isfinite(tt)) {
+                    // edges are axis aligned: along the two fixed axes
+                    // a + tt*0 + v + 0.5 is exactly a + v + 0.5, which
+                    // quantizes to floor((a + v) * 255.75); only the edge's
+                    // own axis needs the f32 arithmetic
+                    const uint32_t d = (o0 ^ o1) >> 1;  // 0, 1, 2 = x, y, z
+                    const uint32_t ad = (o0 >> d) & 1u, vd = d == 0 ? x : (d == 1 ? y : z);
+                    const float pd = __fadd_rn(__fadd_rn(ad ? __fsub_rn(1.0f, tt) : tt, (float)vd), 0.5f);
+                    const uint32_t q = quantize(pd);
+                    qx = d == 0 ? q : (((ax + x) * 1023u) >> 2);
+                    qy = d == 1 ? q : (((ay + y) * 1023u) >> 2);
+                    qz = d == 2 ? q : (((az + z) * 1023u) >> 2);
+                } else {
+                    qx = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)ax, __fmul_rn(tt, (float)((int)bx - (int)ax))), (float)x), 0.5f));
+                    qy = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)ay, __fmul_rn(tt, (float)((int)by - (int)ay))), (float)y), 0.5f));
+                    qz = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)az, __fmul_rn(tt, (float)((int)bz - (int)az))), (float)z), 0.5f));
+                }
+                out[k] = make_uint2((qx << 20) | (qy << 10) | qz, s_id[jb]);
             }
             uint32_t tile_b = 0;
 #pragma unroll
@@ -699,7 +728,7 @@ uint32_t slot_tiles(uint32_t slots) { return div_up(slots, kSlotTile); }
 // one CTA per range of active blocks: 5 resident CTAs per SM at most
 uint32_t mc_grid(bcmc_ctx* ctx, uint32_t max_active)
 {
-    const uint32_t r = (uint32_t)ctx->num_sms * 5u, tiles = div_up(max_active ? max_active : 1, kMcBlocks);
+    const uint32_t r = (uint32_t)ctx->num_sms * 6u, tiles = div_up(max_active ? max_active : 1, kMcBlocks);
     return tiles < r ? tiles : r;
 }
 
