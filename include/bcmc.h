@@ -35,7 +35,8 @@ typedef enum {
     BCMC_E_CUDA = 3,      /* a CUDA call failed; see bcmc_last_error()          */
     BCMC_E_TIMEOUT = 4,   /* a device-side wait hit its iteration limit         */
     BCMC_E_ADMISSION = 5, /* a request does not fit the configured memory       */
-    BCMC_E_STATE = 6      /* call order violated (e.g. no surface computed yet) */
+    BCMC_E_STATE = 6,     /* call order violated (e.g. no surface computed yet) */
+    BCMC_E_LIMIT = 7      /* size above a fixed compile-time limit of the call  */
 } bcmc_status;
 
 typedef struct bcmc_ctx bcmc_ctx;
@@ -179,6 +180,23 @@ bcmc_status bcmc_scan_exclusive_u32(bcmc_ctx* ctx, uint32_t* d_data, uint32_t n,
 /* Asynchronous form: d_out may equal d_in; the total lands in *d_total. */
 bcmc_status bcmc_scan_exclusive_u32_async(bcmc_ctx* ctx, const uint32_t* d_in, uint32_t* d_out,
                                           uint32_t n, uint32_t* d_total, void* stream);
+/* No counterpart in the reference.  The asynchronous scan above without a
+ * context and without any device allocation, for callers that may not
+ * allocate on the call (a runtime that owns all device memory through its own
+ * pool, or one that cannot take an allocation's implicit synchronisation) or
+ * hold no context.  Scratch is a fixed ~132 KB static array per device, so
+ * n > BCMC_SCAN_NOALLOC_MAX_N returns BCMC_E_LIMIT with nothing launched.
+ * Runs on the calling thread's current device; `stream` NULL is the legacy
+ * default stream (there is no context stream).  The first call on a device
+ * does its one-time set-up (looks up the scratch array's device address and
+ * the SM count), so make it before any stream capture on that device.  Calls
+ * on one device share the scratch: calls that may run concurrently (other
+ * streams or threads without ordering) race, and their results are undefined.
+ * Failures: BCMC_E_ARG (null pointers with n > 0), BCMC_E_CUDA (set-up or
+ * launch). */
+#define BCMC_SCAN_NOALLOC_MAX_N (1u << 26)
+bcmc_status bcmc_scan_exclusive_u32_noalloc(const uint32_t* d_in, uint32_t* d_out, uint32_t n,
+                                            uint32_t* d_total, void* stream);
 
 /* ---- StreamCompact (js/stream_compact.js) ------------------------------- */
 /* compactActiveIDs(numElements, isActive, offsets, output)

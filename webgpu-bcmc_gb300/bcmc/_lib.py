@@ -15,7 +15,8 @@ HEADER = os.path.join(os.path.dirname(PKG_ROOT), "include", "bcmc.h")
 
 BCMC_OK = 0
 STATUS_NAMES = {0: "BCMC_OK", 1: "BCMC_E_ARG", 2: "BCMC_E_OOM", 3: "BCMC_E_CUDA", 4: "BCMC_E_TIMEOUT",
-                5: "BCMC_E_ADMISSION", 6: "BCMC_E_STATE"}
+                5: "BCMC_E_ADMISSION", 6: "BCMC_E_STATE",
+                7: "BCMC_E_LIMIT"}
 
 
 class bcmc_opts(C.Structure):
@@ -85,6 +86,7 @@ SIGNATURES = {
     "bcmc_scan_aligned_size": (U32, [U32]),
     "bcmc_scan_exclusive_u32": (C.c_int, [P, P, U32, U32, U32P]),
     "bcmc_scan_exclusive_u32_async": (C.c_int, [P, P, P, U32, P, P]),
+    "bcmc_scan_exclusive_u32_noalloc": (C.c_int, [P, P, U32, P, P]),
     "bcmc_compact_ids": (C.c_int, [P, U32, P, P, P, P]),
     "bcmc_select_ids": (C.c_int, [P, U32, P, P, P, P]),
     "bcmc_sort_aligned_size": (U32, [U32]),

@@ -75,6 +75,10 @@ constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
 void scan_launch(bcmc_ctx* ctx, QueryState* q, const uint32_t* in, uint32_t* out, uint32_t n,
                  uint32_t* d_total, uint64_t* status, cudaStream_t s);
+// Same kernel as scan_launch, sized from an SM count instead of a context;
+// reports a launch error by return value (throws nothing).
+cudaError_t scan_launch_sms(int num_sms, QueryState* q, const uint32_t* in, uint32_t* out, uint32_t n,
+                            uint32_t* d_total, uint64_t* status, cudaStream_t s);
 void select_launch(bcmc_ctx* ctx, QueryState* q, const uint32_t* flags, uint32_t* out, uint32_t n,
                    uint32_t* d_count, uint64_t* status, cudaStream_t s);
 void compact_launch(bcmc_ctx* ctx, uint32_t n, const uint32_t* flags, const uint32_t* offsets,

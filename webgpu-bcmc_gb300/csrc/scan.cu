@@ -166,6 +166,16 @@ void scan_launch(bcmc_ctx* ctx, QueryState* q, const uint32_t* in, uint32_t* out
     BCMC_CUDA(cudaGetLastError());
 }
 
+cudaError_t scan_launch_sms(int num_sms, QueryState* q, const uint32_t* in, uint32_t* out, uint32_t n,
+                            uint32_t* d_total, uint64_t* status, cudaStream_t s)
+{
+    const uint32_t tiles = div_up(n, kScanTile), r = (uint32_t)num_sms * 4u;
+    const int grid = (int)(tiles < r ? (tiles ? tiles : 1) : r);
+    k_scan<<<grid, kScanThreads, 0, s>>>(q, in, out, n, d_total, status);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
 void select_launch(bcmc_ctx* ctx, QueryState* q, const uint32_t* flags, uint32_t* out, uint32_t n,
                    uint32_t* d_count, uint64_t* status, cudaStream_t s)
 {
