@@ -155,6 +155,54 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+DECODE = dict(workload="turb512: 512^3 k^-5/3 spectral field, ZFP rate 2, full-volume decode "
+                       "(2,097,152 blocks -> 512 MiB float32)", dims=(512, 512, 512), rate=2, seed=3)
+
+
+def decode_bench(ctx, flush, reps: int = 10) -> dict:
+    """Full-volume ZFP decode throughput: blocks * (8*rate + 256) B / event time."""
+    import torch
+
+    import bcmc
+    from bcmc import datasets as D
+
+    dims, rate = DECODE["dims"], DECODE["rate"]
+    f = torch.from_numpy(D.turbulence(dims, DECODE["seed"])).cuda()
+    words = bcmc.zfp_encode(ctx, f, rate)
+    del f
+    nb = int(np.prod([(d + 3) // 4 for d in dims]))
+    out = torch.empty(nb * 64, dtype=torch.float32, device="cuda")
+    L = bcmc._lib.load()
+    torch.cuda.synchronize()
+    s = torch.cuda.ExternalStream(ctx.stream)  # the library's stream: the kernel and the events share it
+
+    def run():
+        st = L.bcmc_zfp_decode_volume(ctx.handle, words.data_ptr(), nb, rate, out.data_ptr(), ctx.stream)
+        if st != 0:
+            raise RuntimeError(f"bcmc_zfp_decode_volume failed: {st}")
+
+    for _ in range(3):
+        run()
+    times = []
+    for _ in range(reps):
+        flush.fill_(2)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        run()
+        e1.record(s)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = float(np.median(times))
+    algo = nb * (8 * rate + 256)
+    peak, peak_kind = _peaks()
+    gbs = algo / (ms / 1000.0) / 1e9
+    del out, words
+    return {"workload": DECODE["workload"], "unit": "GB/s", "value": gbs, "ms": ms, "peak": peak,
+            "peak_kind": peak_kind, "frac": gbs / peak, "algorithmic_bytes": algo,
+            "kernel": "k_decode_volume", "l2": "flushed (512 MB write) before each rep"}
+
+
 def algorithmic_bytes(stage: str, st: dict, rate: int, total_blocks: int) -> float:
     """Algorithmic DRAM bytes per launch of each stage's kernel."""
     if stage == "computeVertices":  # k_mc: block data + ids/slots + vertices
@@ -193,11 +241,14 @@ def run_gb300(args):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
     L = bcmc._lib.load()
 
-    def step(perf=None, copy_out=None):
+    def step(perf=None, copy_out=None, lat=None):
         mc.lruCache.reset()
         n_tot = 0
         for iso in isos:
+            t_q = time.perf_counter()
             n = mc.computeSurface(float(iso), perf)
+            if lat is not None:
+                lat.append(1000.0 * (time.perf_counter() - t_q))
             if copy_out is not None:
                 mc.copyVertices(copy_out)
             n_tot += n
@@ -214,12 +265,13 @@ def run_gb300(args):
     times = []
     launches0 = L.bcmc_kernel_launches()
     perf = {}
+    lat = []
     for _ in range(args.steps):
         flush.fill_(1)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        step(perf)
+        step(perf, None, lat)
         e1.record(stream)
         e1.synchronize()
         times.append(e0.elapsed_time(e1))
@@ -267,6 +319,8 @@ def run_gb300(args):
     kernel_of = {"computeVertices": "k_mc", "decompression": "k_assign (LRU assign + ZFP decode)",
                  "computeActiveBlocks": "k_active", "cacheUpdate": "k_slots + radix sort"}
 
+    decode = decode_bench(ctx, flush) if not args.no_decode else None
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         qps, threads, _ = cpu_oracle_time(field, isos, steps=1)
@@ -286,6 +340,10 @@ def run_gb300(args):
                              "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                              "traffic": None, "avg_launch_ms": avg_ms, "algorithmic_bytes": bytes_per_launch},
                 "stage_ms_per_query": {s: tot[s] / nq for s in stages},
+                "latency_ms": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
+                               "p99": float(np.percentile(lat, 99)), "queries": len(lat),
+                               "what": "host wall time of each computeSurface call (returns the vertex count)"},
+                "decode": decode,
                 "gpu_launches": int(launches),
                 "clocks": clk,
                 "volume_load_s": load_s,
@@ -302,6 +360,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-decode", action="store_true", help="skip the full-volume decode leg")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

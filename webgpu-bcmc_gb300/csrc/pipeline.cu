@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(128) k_assign(QueryState* q, AssignArgs a)
         a.item_slots[item] = (int32_t)slot;
         if (a.words) {
             float v[64];
-            zfp_decode_block<true>(a.words, (uint64_t)item * a.max_bits, a.max_bits, v);
+            zfp_decode_block<1>(a.words, (uint64_t)item * a.max_bits, a.max_bits, v);
             float4* d4 = reinterpret_cast<float4*>(a.cache + (uint64_t)slot * 64u);
 #pragma unroll
             for (int k = 0; k < 16; ++k) d4[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
