@@ -48,10 +48,19 @@ typedef struct bcmc_lru bcmc_lru;
 typedef struct {
     int device;                    /* CUDA device ordinal                          */
     double initial_cache_fraction; /* LRU initial size as a fraction of blocks     */
-    uint32_t flags;                /* reserved, 0                                  */
+    uint32_t flags;                /* BCMC_FLAG_* bits, 0 = the reference's behaviour */
 } bcmc_opts;
 
 void bcmc_opts_default(bcmc_opts* opts);
+
+/* bcmc_opts.flags bits.
+ * BCMC_FLAG_FULL_RANGES: compute the value range of every block.  By default
+ * block ranges follow the reference exactly: zfp_compute_block_range.comp:22
+ * counts the blocks as (padded x * padded y) / 64 * padded z in 32-bit integers,
+ * which truncates when (x/4)*(y/4) is not a multiple of 4, and the ranges of the
+ * blocks past that count stay at the zero of the freshly created buffer
+ * (compressed_marching_cubes.js:526-529). */
+#define BCMC_FLAG_FULL_RANGES 1u
 
 /* ---- context ------------------------------------------------------------ */
 /* Replaces the WebGPU device handed to `new CompressedMarchingCubes(device)`

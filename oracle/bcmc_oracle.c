@@ -525,9 +525,19 @@ void bcmc_oracle_block_ranges(const uint64_t* words, const uint32_t dims[3], uin
     const uint32_t nbx = align_to(dims[0], 4) / 4, nby = align_to(dims[1], 4) / 4,
                    nbz = align_to(dims[2], 4) / 4;
     const uint64_t nblocks = (uint64_t)nbx * nby * nbz;
+    /* total_blocks = (padded_dims.x * padded_dims.y) / 64 * padded_dims.z in
+     * u32 (zfp_compute_block_range.comp:22): the division truncates when
+     * nbx*nby is not a multiple of 4, and blocks from there on keep the zero
+     * the freshly created range buffer holds (compressed_marching_cubes.js:526-529). */
+    const uint32_t ranged = (align_to(dims[0], 4) * align_to(dims[1], 4)) / 64u * align_to(dims[2], 4);
 #pragma omp parallel for schedule(static)
     for (int64_t bi = 0; bi < (int64_t)nblocks; ++bi) {
         const uint64_t b = (uint64_t)bi;
+        if (b >= ranged) {
+            ranges[2 * b] = 0.0f;
+            ranges[2 * b + 1] = 0.0f;
+            continue;
+        }
         float blk[64];
         bcmc_oracle_decode_block(words, b, max_bits, 0, blk);
         const uint32_t x0 = (uint32_t)(b % nbx) * 4, y0 = (uint32_t)((b / nbx) % nby) * 4,

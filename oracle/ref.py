@@ -1,0 +1,137 @@
+"""ctypes front end of oracle/_ref/libbcmc_ref.so: the reference's own compute
+shaders compiled as host C++ by oracle/ref_build.py (TEST INFRASTRUCTURE ONLY).
+
+`available()` is False when the reference checkout is absent (for example on a
+machine that only has this repository); callers then fall back to the golden
+fixtures under tests/golden/, which were generated from this module.
+
+`surface(words, rate, dims, iso)` composes the shader programs the way
+js/compressed_marching_cubes.js does for one query with every active block
+cached (computeBlockRanges :522-578, computeActiveBlocks :811-829, stream
+compaction, decompressBlocks :831-913, computeBlockHasVertices :915-991,
+computeBlockVertexCounts :993-1042, computeVertices :1044-1122).  The host
+steps between dispatches (compaction to ascending ids, exclusive scan of the
+per-block counts) are restated in numpy.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+P = C.c_void_p
+U32 = C.c_uint32
+F32 = C.c_float
+_SIGS = {
+    "ref_zfp_decompress_blocks": [P, U32, P, U32, P, P],
+    "ref_zfp_block_ranges": [P, P, U32, P],
+    "ref_block_active": [P, P, F32, P],
+    "ref_block_has_vertices": [P, F32, P, P, P, P, U32, P],
+    "ref_block_num_verts": [P, F32, P, P, P, P, P, U32, P],
+    "ref_block_vertices": [P, F32, P, P, P, P, P, U32, P],
+}
+
+
+def build(reference: str | None = None):
+    import ref_build
+
+    return ref_build.build(reference)
+
+
+def available() -> bool:
+    try:
+        return load() is not None
+    except OSError:
+        return False
+
+
+def load():
+    global _LIB
+    if _LIB is None:
+        path = build()
+        if path is None:
+            return None
+        lib = C.CDLL(path)
+        for name, args in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = None
+        _LIB = lib
+    return _LIB
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _dims(dims):
+    return np.ascontiguousarray(np.asarray(dims, dtype=np.uint32))
+
+
+def _words(words: np.ndarray) -> np.ndarray:
+    w = np.ascontiguousarray(words).view(np.uint64)
+    return np.concatenate([w, np.zeros(2, np.uint64)])  # the reader may fetch one word past the end
+
+
+def block_ranges(words, rate: int, dims) -> np.ndarray:
+    d = _dims(dims)
+    nb = int(np.prod([(int(x) + 3) // 4 for x in dims]))
+    out = np.zeros((nb, 2), np.float32)
+    w = _words(words)
+    load().ref_zfp_block_ranges(_p(w), _p(d), 64 * rate, _p(out))
+    return out
+
+
+def decode_blocks(words, rate: int, ids: np.ndarray, slots: np.ndarray, cache_slots: int) -> np.ndarray:
+    ids = np.ascontiguousarray(ids, dtype=np.uint32)
+    slots = np.ascontiguousarray(slots).astype(np.int32).view(np.uint32)
+    cache = np.zeros((cache_slots, 64), np.float32)
+    w = _words(words)
+    load().ref_zfp_decompress_blocks(_p(w), 64 * rate, _p(ids), len(ids), _p(slots), _p(cache))
+    return cache
+
+
+def block_active(ranges: np.ndarray, dims, iso: float) -> np.ndarray:
+    d = _dims(dims)
+    r = np.ascontiguousarray(ranges, dtype=np.float32)
+    out = np.zeros(len(r), np.uint32)
+    load().ref_block_active(_p(r), _p(d), F32(iso), _p(out))
+    return out
+
+
+def surface(words, rate: int, dims, iso: float) -> dict:
+    """One query with every active block cached (slot = rank among active blocks)."""
+    L = load()
+    d = _dims(dims)
+    ranges = block_ranges(words, rate, dims)
+    active = block_active(ranges, dims, iso)
+    ids = np.nonzero(active)[0].astype(np.uint32)
+    n = len(ids)
+    total = len(active)
+    slots = np.full(total, -1, np.int32)
+    slots[ids] = np.arange(n, dtype=np.int32)
+    cache = decode_blocks(words, rate, ids, slots, max(n, 1))
+    uslots = slots.view(np.uint32)
+    has = np.zeros(max(n, 1), np.uint32)
+    if n:
+        L.ref_block_has_vertices(_p(d), F32(iso), _p(cache), _p(active), _p(uslots), _p(ids), n, _p(has))
+    with_verts = np.nonzero(has[:n])[0].astype(np.uint32)
+    m = len(with_verts)
+    counts = np.zeros(max(m, 1), np.uint32)
+    if m:
+        L.ref_block_num_verts(_p(d), F32(iso), _p(cache), _p(active), _p(uslots), _p(ids), _p(with_verts), m,
+                              _p(counts))
+    counts = counts[:m]
+    offsets = (np.cumsum(counts.astype(np.uint64)) - counts).astype(np.uint32)
+    nverts = int(counts.astype(np.uint64).sum())
+    verts = np.zeros((max(nverts, 1), 2), np.uint32)
+    if m:
+        info = np.ascontiguousarray(np.stack([with_verts, offsets], axis=1).astype(np.uint32))
+        L.ref_block_vertices(_p(d), F32(iso), _p(cache), _p(active), _p(uslots), _p(ids), _p(info), m, _p(verts))
+    return {"ranges": ranges, "active": active, "active_ids": ids, "with_verts": with_verts,
+            "block_counts": counts, "vert_offsets": offsets, "num_vertices": nverts, "vertices": verts[:nverts],
+            "decoded": cache[:n]}

@@ -1,0 +1,286 @@
+// ref_shim.h -- TEST INFRASTRUCTURE ONLY.
+//
+// Just enough of GLSL 4.50 compute semantics, in C++20, to compile the
+// reference's own compute shaders (Twinklebear/webgpu-bcmc shaders/*.comp,
+// after the mechanical rewrites in ref_build.py) as host code, so that the
+// CPU oracle can be checked against the reference's shader source itself.
+//
+// Semantics chosen to match how the reference runs (GLSL -> SPIR-V -> WGSL
+// under Dawn): uint/int are 32-bit and wrap (built with -fwrapv), f32
+// arithmetic is not contracted (-ffp-contract=off), float -> uint/int
+// conversion saturates as WGSL's u32()/i32() do, min/max follow the GLSL
+// definitions, and barrier() is a workgroup barrier implemented with fibers
+// by ref_runtime.cpp.
+#pragma once
+
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <limits>
+#include <type_traits>
+
+typedef uint32_t uint;
+
+namespace glsl {
+
+template <class To, class From>
+inline To cvt(From f)
+{
+    if constexpr (std::is_floating_point_v<From> && std::is_integral_v<To> && !std::is_same_v<To, bool>) {
+        // WGSL u32()/i32(): saturating, NaN -> 0
+        if (f != f) return To(0);
+        const double lo = (double)std::numeric_limits<To>::min(), hi = (double)std::numeric_limits<To>::max();
+        const double d = (double)f;
+        if (d <= lo) return std::numeric_limits<To>::min();
+        if (d >= hi) return std::numeric_limits<To>::max();
+        return (To)d;
+    } else {
+        return static_cast<To>(f);
+    }
+}
+
+template <class T, int N>
+struct VS;
+template <class T>
+struct VS<T, 2> {
+    T x, y;
+};
+template <class T>
+struct VS<T, 3> {
+    T x, y, z;
+};
+template <class T>
+struct VS<T, 4> {
+    T x, y, z, w;
+};
+
+template <class T, int N>
+struct V : VS<T, N> {
+    V() : VS<T, N>{} {}
+    template <class S, class = std::enable_if_t<std::is_arithmetic_v<S>>>
+    explicit V(S s)
+    {
+        for (int i = 0; i < N; ++i) (*this)[i] = cvt<T>(s);
+    }
+    template <class A, class B>
+    V(A a, B b)
+        requires(N == 2)
+    {
+        this->x = cvt<T>(a);
+        this->y = cvt<T>(b);
+    }
+    template <class A, class B, class C>
+    V(A a, B b, C c)
+        requires(N == 3)
+    {
+        this->x = cvt<T>(a);
+        this->y = cvt<T>(b);
+        (*this)[2] = cvt<T>(c);
+    }
+    template <class A, class B, class C, class D>
+    V(A a, B b, C c, D d)
+        requires(N == 4)
+    {
+        this->x = cvt<T>(a);
+        this->y = cvt<T>(b);
+        (*this)[2] = cvt<T>(c);
+        (*this)[3] = cvt<T>(d);
+    }
+    // GLSL's implicit int -> uint -> float conversions between vector types
+    template <class U, class = std::enable_if_t<!std::is_same_v<U, T>>>
+    V(const V<U, N>& o)
+    {
+        for (int i = 0; i < N; ++i) (*this)[i] = cvt<T>(o[i]);
+    }
+    T& operator[](int i) { return (&this->x)[i]; }
+    const T& operator[](int i) const { return (&this->x)[i]; }
+    T& operator[](uint i) { return (&this->x)[i]; }
+    const T& operator[](uint i) const { return (&this->x)[i]; }
+};
+
+template <class A, class B>
+using common_t = std::common_type_t<A, B>;
+
+#define GLSL_VEC_BINOP(OP)                                                                         \
+    template <class A, class B, int N>                                                             \
+    inline V<common_t<A, B>, N> operator OP(const V<A, N>& a, const V<B, N>& b)                    \
+    {                                                                                              \
+        V<common_t<A, B>, N> r;                                                                    \
+        for (int i = 0; i < N; ++i) r[i] = (common_t<A, B>)a[i] OP(common_t<A, B>) b[i];           \
+        return r;                                                                                  \
+    }                                                                                              \
+    template <class A, class S, int N, class = std::enable_if_t<std::is_arithmetic_v<S>>>          \
+    inline V<common_t<A, S>, N> operator OP(const V<A, N>& a, S s)                                 \
+    {                                                                                              \
+        V<common_t<A, S>, N> r;                                                                    \
+        for (int i = 0; i < N; ++i) r[i] = (common_t<A, S>)a[i] OP(common_t<A, S>) s;              \
+        return r;                                                                                  \
+    }                                                                                              \
+    template <class A, class S, int N, class = std::enable_if_t<std::is_arithmetic_v<S>>>          \
+    inline V<common_t<A, S>, N> operator OP(S s, const V<A, N>& a)                                 \
+    {                                                                                              \
+        V<common_t<A, S>, N> r;                                                                    \
+        for (int i = 0; i < N; ++i) r[i] = (common_t<A, S>)s OP(common_t<A, S>) a[i];              \
+        return r;                                                                                  \
+    }
+GLSL_VEC_BINOP(+)
+GLSL_VEC_BINOP(-)
+GLSL_VEC_BINOP(*)
+GLSL_VEC_BINOP(/)
+GLSL_VEC_BINOP(%)
+#undef GLSL_VEC_BINOP
+
+template <class A, class B, int N>
+inline V<A, N>& operator+=(V<A, N>& a, const B& b)
+{
+    a = V<A, N>(a + b);
+    return a;
+}
+template <class A, class B, int N>
+inline V<A, N>& operator-=(V<A, N>& a, const B& b)
+{
+    a = V<A, N>(a - b);
+    return a;
+}
+
+// GLSL == / != on vectors compare all components and return bool
+template <class A, class B, int N>
+inline bool operator==(const V<A, N>& a, const V<B, N>& b)
+{
+    for (int i = 0; i < N; ++i)
+        if ((common_t<A, B>)a[i] != (common_t<A, B>)b[i]) return false;
+    return true;
+}
+template <class A, class B, int N>
+inline bool operator!=(const V<A, N>& a, const V<B, N>& b)
+{
+    return !(a == b);
+}
+
+#define GLSL_VEC_CMP(NAME, OP)                                                                     \
+    template <class A, class B, int N>                                                             \
+    inline V<bool, N> NAME(const V<A, N>& a, const V<B, N>& b)                                     \
+    {                                                                                              \
+        V<bool, N> r;                                                                              \
+        for (int i = 0; i < N; ++i) r[i] = (common_t<A, B>)a[i] OP(common_t<A, B>) b[i];           \
+        return r;                                                                                  \
+    }
+GLSL_VEC_CMP(lessThan, <)
+GLSL_VEC_CMP(lessThanEqual, <=)
+GLSL_VEC_CMP(greaterThan, >)
+GLSL_VEC_CMP(greaterThanEqual, >=)
+#undef GLSL_VEC_CMP
+
+template <int N>
+inline bool any(const V<bool, N>& b)
+{
+    for (int i = 0; i < N; ++i)
+        if (b[i]) return true;
+    return false;
+}
+template <int N>
+inline bool all(const V<bool, N>& b)
+{
+    for (int i = 0; i < N; ++i)
+        if (!b[i]) return false;
+    return true;
+}
+
+// Swizzles used by the shaders: .xyz reads, .xy/.xz/.yz read, compare and assign.
+template <class Vec>
+inline auto swz_xyz(const Vec& v)
+{
+    return V<std::remove_cv_t<std::remove_reference_t<decltype(v[0])>>, 3>(v[0], v[1], v[2]);
+}
+template <class Vec, int I, int J>
+struct Swz2 {
+    Vec& v;
+    using T = std::remove_cv_t<std::remove_reference_t<decltype(v[0])>>;
+    operator V<T, 2>() const { return V<T, 2>(v[I], v[J]); }
+    template <class U>
+    Swz2& operator=(const V<U, 2>& o)
+    {
+        v[I] = cvt<T>(o[0]);
+        v[J] = cvt<T>(o[1]);
+        return *this;
+    }
+    template <class U>
+    bool operator==(const V<U, 2>& o) const
+    {
+        return V<T, 2>(v[I], v[J]) == o;
+    }
+};
+template <class Vec>
+inline Swz2<Vec, 0, 1> swz_xy(Vec& v)
+{
+    return {v};
+}
+template <class Vec>
+inline Swz2<Vec, 0, 2> swz_xz(Vec& v)
+{
+    return {v};
+}
+template <class Vec>
+inline Swz2<Vec, 1, 2> swz_yz(Vec& v)
+{
+    return {v};
+}
+
+// GLSL min/max definitions: min(x, y) = y < x ? y : x, max(x, y) = x < y ? y : x
+template <class T>
+inline T min(T x, T y)
+{
+    return y < x ? y : x;
+}
+template <class T>
+inline T max(T x, T y)
+{
+    return x < y ? y : x;
+}
+
+}  // namespace glsl
+
+// min/max/abs/ldexp calls in the shader text are renamed to these (ref_build.py)
+// so that they cannot collide with the C library's overloads.
+template <class T>
+inline T glsl_min(T x, T y)
+{
+    return glsl::min(x, y);
+}
+template <class T>
+inline T glsl_max(T x, T y)
+{
+    return glsl::max(x, y);
+}
+inline float glsl_abs(float x) { return std::fabs(x); }
+inline int glsl_abs(int x) { return x < 0 ? -x : x; }
+inline float glsl_ldexp(float x, int e) { return std::ldexp(x, e); }
+
+using glsl::all;
+using glsl::any;
+using glsl::greaterThan;
+using glsl::greaterThanEqual;
+using glsl::lessThan;
+using glsl::lessThanEqual;
+
+typedef glsl::V<float, 2> vec2;
+typedef glsl::V<float, 3> vec3;
+typedef glsl::V<float, 4> vec4;
+typedef glsl::V<int, 2> ivec2;
+typedef glsl::V<int, 3> ivec3;
+typedef glsl::V<int, 4> ivec4;
+typedef glsl::V<uint, 2> uvec2;
+typedef glsl::V<uint, 3> uvec3;
+typedef glsl::V<uint, 4> uvec4;
+typedef glsl::V<bool, 3> bvec3;
+
+// Invocation ids of the running invocation (set by the runtime before it
+// resumes each invocation) and the workgroup barrier.
+extern uvec3 gl_GlobalInvocationID;
+extern uvec3 gl_LocalInvocationID;
+extern uvec3 gl_WorkGroupID;
+void ref_barrier();
+
+// Runs `invocations` invocations of `main_fn` per workgroup over `groups`
+// workgroups (x-major ids), as fibers that switch at barrier().
+void ref_dispatch(void (*main_fn)(), uvec3 groups, uint invocations);

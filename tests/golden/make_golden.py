@@ -1,0 +1,86 @@
+"""Generates the golden fixtures in this folder from the reference's own compute
+shaders, compiled as host C++ (oracle/_ref, built by oracle/ref_build.py from
+a checkout of Twinklebear/webgpu-bcmc).
+
+Inputs are seeded synthetic fields (bcmc.datasets) encoded with the oracle's
+fixed-rate ZFP encoder (the reference has no encoder: its streams come from
+zfp), plus random bit streams for the decoder.  Outputs are what the
+reference's shaders produce for them:
+
+  mc_<case>.npz      words, rate, dims, isos; block ranges; per iso: active
+                     flags, active ids, blocks with vertices, vertex offsets,
+                     the packed vertex buffer
+  decode_rate<r>.npz random words and the reference decoder's output, bits
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path[:0] = [os.path.join(ROOT, "oracle"), os.path.join(ROOT, "webgpu-bcmc_gb300")]
+
+import oracle as O  # noqa: E402
+import ref as R  # noqa: E402
+from bcmc import datasets as D  # noqa: E402
+
+MC_CASES = {
+    # name: (field kind, dims (x, y, z), seed, rate, isovalues)
+    "blobs32_r8": ("blobs", (32, 32, 32), 1, 8, [0.5, 0.3]),
+    "blobs_partial_r4": ("blobs", (30, 21, 17), 4, 4, [0.6, 1.5]),
+    "ct44_r4": ("ct_like", (44, 40, 36), 2, 4, [60.0, 150.0]),
+    "turb24_r2": ("turbulence", (24, 24, 24), 3, 2, [0.0, 0.3]),
+    "ct16bit_r4": ("ct_uint16", (36, 32, 28), 5, 4, [800.0, 2500.0]),
+}
+DECODE_RATES = (1, 2, 3, 8, 16, 32)
+DECODE_BLOCKS = 96
+
+
+def make_mc(name, kind, dims, seed, rate, isos):
+    f = D.make_field(kind, dims, seed)
+    words = O.zfp_encode(f, rate)
+    ranges = R.block_ranges(words, rate, dims)
+    out = {"words": words, "rate": np.int32(rate), "dims": np.asarray(dims, np.uint32),
+           "isos": np.asarray(isos, np.float32), "ranges": ranges}
+    for i, iso in enumerate(isos):
+        s = R.surface(words, rate, dims, float(iso))
+        assert np.array_equal(s["ranges"].view(np.uint32), ranges.view(np.uint32))
+        out[f"active_{i}"] = s["active"]
+        out[f"active_ids_{i}"] = s["active_ids"]
+        out[f"with_verts_{i}"] = s["with_verts"]
+        out[f"vert_offsets_{i}"] = s["vert_offsets"]
+        out[f"vertices_{i}"] = s["vertices"]
+        print(f"{name} iso {iso}: {len(s['active_ids'])} active, {len(s['with_verts'])} with vertices, "
+              f"{s['num_vertices']} vertices")
+    np.savez_compressed(os.path.join(HERE, f"mc_{name}.npz"), **out)
+
+
+def make_decode(rate):
+    rng = np.random.default_rng(1000 + rate)
+    nwords = DECODE_BLOCKS * rate + 2
+    words = rng.integers(0, 1 << 63, size=nwords, dtype=np.int64).view(np.uint64)
+    words[0] |= np.uint64(1)  # first block nonzero
+    words[-2:] = 0
+    ids = np.arange(DECODE_BLOCKS, dtype=np.uint32)
+    dec = R.decode_blocks(words, rate, ids, ids.astype(np.int32), DECODE_BLOCKS)
+    np.savez_compressed(os.path.join(HERE, f"decode_rate{rate}.npz"), words=words, rate=np.int32(rate),
+                        decoded_bits=dec.view(np.uint32))
+
+
+def main():
+    O.build()
+    if not R.available():
+        sys.exit("oracle/_ref is not built (no reference checkout): cannot generate fixtures")
+    for name, spec in MC_CASES.items():
+        make_mc(name, *spec)
+    for rate in DECODE_RATES:
+        make_decode(rate)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,94 @@
+"""The CPU oracle against the reference's own shaders.
+
+* Golden fixtures (tests/golden/*.npz, generated by tests/golden/make_golden.py
+  from the reference's compute shaders compiled as host C++): decode of random
+  bit streams at six rates, and full queries (ranges, active flags, active ids,
+  blocks with vertices, vertex offsets, packed vertices) on five volumes.
+* When the reference checkout is present, the same comparison live on further
+  seeded cases (oracle/_ref built by oracle/ref_build.py).
+
+Everything is integer/bit data: compared exactly.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+MC_FILES = sorted(glob.glob(os.path.join(GOLDEN, "mc_*.npz")))
+DECODE_FILES = sorted(glob.glob(os.path.join(GOLDEN, "decode_rate*.npz")))
+
+
+def test_fixtures_present():
+    assert len(MC_FILES) >= 5 and len(DECODE_FILES) >= 6
+
+
+@pytest.mark.parametrize("path", DECODE_FILES, ids=os.path.basename)
+def test_oracle_decoder_matches_reference_shader(oracle, path):
+    g = np.load(path)
+    rate, words = int(g["rate"]), g["words"]
+    want = g["decoded_bits"]
+    for b in range(want.shape[0]):
+        got = oracle.decode_block(words, b, 64 * rate)
+        assert np.array_equal(np.asarray(got, np.float32).view(np.uint32), want[b]), b
+        emu = oracle.decode_block(words, b, 64 * rate, native=True)
+        assert np.array_equal(np.asarray(emu, np.float32).view(np.uint32), want[b]), b
+
+
+def check_mc_against_golden(m, g, i, n):
+    """m: an object with the oracle's CompressedMarchingCubes accessors."""
+    s = m.stats()
+    assert np.array_equal(m.active(), g[f"active_{i}"])
+    assert np.array_equal(m.active_ids(s["numActiveBlocks"]), g[f"active_ids_{i}"])
+    assert np.array_equal(m.with_verts(s["numBlocksWithVertices"]), g[f"with_verts_{i}"])
+    assert np.array_equal(m.vert_offsets(s["numBlocksWithVertices"]), g[f"vert_offsets_{i}"])
+    assert n == len(g[f"vertices_{i}"])
+    assert np.array_equal(m.vertices(n), g[f"vertices_{i}"])
+
+
+@pytest.mark.parametrize("path", MC_FILES, ids=os.path.basename)
+@pytest.mark.parametrize("cache_fraction", [1.0, 0.05])
+def test_oracle_pipeline_matches_reference_shaders(oracle, path, cache_fraction):
+    g = np.load(path)
+    rate, dims = int(g["rate"]), tuple(int(d) for d in g["dims"])
+    m = oracle.CompressedMarchingCubes(g["words"], rate, dims, initial_cache_fraction=cache_fraction)
+    assert np.array_equal(m.ranges().view(np.uint32), g["ranges"].reshape(-1).view(np.uint32))
+    for i, iso in enumerate(g["isos"]):
+        n = m.compute_surface(float(iso))
+        check_mc_against_golden(m, g, i, n)
+
+
+def _ref():
+    import ref
+
+    if not ref.available():
+        pytest.skip("reference checkout not present: live shader comparison skipped")
+    return ref
+
+
+@pytest.mark.parametrize("kind,dims,seed,rate,isos", [
+    ("blobs", (20, 28, 24), 11, 8, [0.4, 0.9]),
+    ("ct_like", (33, 29, 27), 12, 3, [45.0, 200.0]),
+    ("turbulence", (20, 20, 20), 13, 1, [-0.2, 0.1]),
+    ("ct_uint16", (25, 22, 19), 14, 6, [300.0]),
+])
+def test_oracle_matches_reference_shaders_live(oracle, kind, dims, seed, rate, isos):
+    R = _ref()
+    from bcmc import datasets as D
+
+    f = D.make_field(kind, dims, seed)
+    words = oracle.zfp_encode(f, rate)
+    nb = int(np.prod([(d + 3) // 4 for d in dims]))
+    ids = np.arange(nb, dtype=np.uint32)
+    dec_ref = R.decode_blocks(words, rate, ids, ids.astype(np.int32), nb)
+    dec = oracle.decode_volume(words, nb, 64 * rate).reshape(nb, 64)
+    assert np.array_equal(dec.view(np.uint32), dec_ref.view(np.uint32))
+    m = oracle.CompressedMarchingCubes(words, rate, dims, initial_cache_fraction=0.3)
+    for iso in isos:
+        s = R.surface(words, rate, dims, float(iso))
+        n = m.compute_surface(float(iso))
+        assert np.array_equal(m.ranges().view(np.uint32), s["ranges"].reshape(-1).view(np.uint32))
+        g = {"active_0": s["active"], "active_ids_0": s["active_ids"], "with_verts_0": s["with_verts"],
+             "vert_offsets_0": s["vert_offsets"], "vertices_0": s["vertices"]}
+        check_mc_against_golden(m, g, 0, n)

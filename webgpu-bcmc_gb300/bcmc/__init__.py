@@ -80,9 +80,16 @@ def _ptr(buf) -> int:
     raise BcmcError(1, f"not a device buffer: {type(buf)!r}")
 
 
+_CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy: the legacy default stream, named explicitly
+
+
 def _torch_stream() -> int:
+    """torch's current stream as a cudaStream_t value.  torch reports its
+    default stream as 0, which the C ABI reads as "the context's own stream",
+    so it is passed as cudaStreamLegacy to keep the call ordered with torch."""
     t = _torch()
-    return int(t.cuda.current_stream().cuda_stream)
+    s = int(t.cuda.current_stream().cuda_stream)
+    return s if s != 0 else _CUDA_STREAM_LEGACY
 
 
 def _sync_torch():
@@ -94,12 +101,15 @@ def _sync_torch():
 class Context:
     """The CUDA device a pipeline runs on (the reference's WebGPU device)."""
 
-    def __init__(self, device: int = 0, initial_cache_fraction: float = 0.05):
+    FULL_RANGES = 1  # BCMC_FLAG_FULL_RANGES
+
+    def __init__(self, device: int = 0, initial_cache_fraction: float = 0.05, flags: int = 0):
         L = _lib.load()
         opts = _lib.bcmc_opts()
         L.bcmc_opts_default(C.byref(opts))
         opts.device = int(device)
         opts.initial_cache_fraction = float(initial_cache_fraction)
+        opts.flags = int(flags)
         h = C.c_void_p()
         rc = L.bcmc_ctx_create(C.byref(opts), C.byref(h))
         if rc != 0:

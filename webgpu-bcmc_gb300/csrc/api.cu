@@ -499,7 +499,8 @@ bcmc_status bcmc_ctx_create(const bcmc_opts* opts, bcmc_ctx** out)
     if (!ctx) return BCMC_E_OOM;
     if (opts) ctx->opts = *opts;
     else bcmc_opts_default(&ctx->opts);
-    if (!(ctx->opts.initial_cache_fraction > 0.0) || ctx->opts.initial_cache_fraction > 1.0) {
+    if (!(ctx->opts.initial_cache_fraction > 0.0) || ctx->opts.initial_cache_fraction > 1.0 ||
+        (ctx->opts.flags & ~BCMC_FLAG_FULL_RANGES) != 0) {
         delete ctx;
         return BCMC_E_ARG;
     }

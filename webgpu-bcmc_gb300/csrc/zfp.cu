@@ -8,17 +8,22 @@ namespace bcmc {
 // zfp_compute_block_range.comp:19-61: min/max over the voxels of each block
 // that lie inside the volume (partial blocks at the +x/+y/+z faces are
 // clipped), starting from (1e20, -1e20).  One thread per block.
-// Bit-plane deposit of the bulk decoders: plane rows + bit transpose (measured
-// fastest for full decodes of many blocks, 256-thread CTAs, one block per thread).
-constexpr int kBulkDeposit = 2;
-constexpr int kBulkThreads = 256;
+// Bulk decoders: register bit-plane deposit, one block per thread, 128-thread
+// CTAs (measured fastest of the deposit variants on full-volume decodes).
+constexpr int kBulkDeposit = 1;
+constexpr int kBulkThreads = 128;
 
 __global__ void __launch_bounds__(kBulkThreads) k_block_ranges(const uint64_t* __restrict__ words, uint3 dims, uint3 nb,
-                                                      uint32_t max_bits, float2* __restrict__ ranges)
+                                                      uint32_t max_bits, uint64_t ranged,
+                                                      float2* __restrict__ ranges)
 {
     const uint64_t nblocks = (uint64_t)nb.x * nb.y * nb.z;
     for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nblocks;
          b += (uint64_t)gridDim.x * blockDim.x) {
+        if (b >= ranged) {  // beyond the reference's block count: the buffer's zero
+            ranges[b] = make_float2(0.0f, 0.0f);
+            continue;
+        }
         float v[64];
         zfp_decode_block<kBulkDeposit>(words, b * max_bits, max_bits, v);
         const uint32_t bx = (uint32_t)(b % nb.x), by = (uint32_t)((b / nb.x) % nb.y),
@@ -136,7 +141,14 @@ void zfp_ranges_launch(bcmc_ctx* ctx, const uint64_t* words, const uint32_t dims
     const uint3 d = make_uint3(dims[0], dims[1], dims[2]);
     const uint3 nb = make_uint3(div_up(dims[0], 4), div_up(dims[1], 4), div_up(dims[2], 4));
     const uint64_t n = (uint64_t)nb.x * nb.y * nb.z;
-    k_block_ranges<<<grid_all(n, kBulkThreads), kBulkThreads, 0, s>>>(words, d, nb, max_bits, reinterpret_cast<float2*>(ranges));
+    // zfp_compute_block_range.comp:22 counts (padded x * padded y) / 64 * padded z
+    // blocks in u32, which truncates when nb.x * nb.y is not a multiple of 4;
+    // the blocks past that count keep the zero of the new range buffer
+    // (compressed_marching_cubes.js:526-529).  BCMC_FLAG_FULL_RANGES ranges all.
+    const uint32_t ref_count = (4u * nb.x * 4u * nb.y) / 64u * (4u * nb.z);
+    const uint64_t ranged = (ctx->opts.flags & BCMC_FLAG_FULL_RANGES) ? n : (ref_count < n ? ref_count : n);
+    k_block_ranges<<<grid_all(n, kBulkThreads), kBulkThreads, 0, s>>>(words, d, nb, max_bits, ranged,
+                                                                      reinterpret_cast<float2*>(ranges));
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
 }

@@ -167,98 +167,37 @@ __device__ __forceinline__ void zfp_decode_ints_regs(BitReader& rd, uint32_t bud
     for (int i = 0; i < 64; ++i) u[i] = rest >= 32u ? 0u : u[i] << rest;
 }
 
-// One stage of a 32x32 bit-matrix transpose over a[32] (row r = word r, column
-// c = bit c): swaps the J-bit off-diagonal blocks of rows k and k + J.
-template <int J, uint32_t M>
-__device__ __forceinline__ void bit_transpose_stage(uint32_t* a)
-{
-#pragma unroll
-    for (int k = 0; k < 32; ++k) {
-        if (k & J) continue;
-        if (J == 16) {  // 16-bit halves: two byte permutes
-            const uint32_t x = a[k], y = a[k + 16];
-            a[k] = __byte_perm(x, y, 0x5410);
-            a[k + 16] = __byte_perm(x, y, 0x7632);
-        } else if (J == 8) {  // bytes: two byte permutes
-            const uint32_t x = a[k], y = a[k + 8];
-            a[k] = __byte_perm(x, y, 0x6240);
-            a[k + 8] = __byte_perm(x, y, 0x7351);
-        } else {
-            const uint32_t t = ((a[k] >> J) ^ a[k + J]) & M;
-            a[k] ^= t << J;
-            a[k + J] ^= t;
-        }
-    }
-}
-
-// a[c] bit r <- a[r] bit c
-__device__ __forceinline__ void bit_transpose32(uint32_t* a)
-{
-    bit_transpose_stage<16, 0x0000ffffu>(a);
-    bit_transpose_stage<8, 0x00ff00ffu>(a);
-    bit_transpose_stage<4, 0x0f0f0f0fu>(a);
-    bit_transpose_stage<2, 0x33333333u>(a);
-    bit_transpose_stage<1, 0x55555555u>(a);
-}
-
-// Same decode, keeping each bit plane as a 64-bit row (planes k = 31..0 fully
-// unrolled so every row has a fixed register); the coefficients are then the
-// columns, recovered with two 32x32 bit transposes -- a fixed ~600 operations
-// instead of 64 shift-ins per decoded plane.  Used for throughput (full
-// decodes of many blocks).
-__device__ __forceinline__ void zfp_decode_ints_planes(BitReader& rd, uint32_t budget, uint32_t* u)
-{
-    uint32_t* lo = u;       // rows 0..31: plane k's coefficients 0..31
-    uint32_t* hi = u + 32;  // rows 0..31: plane k's coefficients 32..63
-#pragma unroll
-    for (int i = 0; i < 32; ++i) lo[i] = hi[i] = 0;
-    uint32_t bits = budget, n = 0;
-#pragma unroll
-    for (int k = 31; k >= 0; --k) {
-        if (bits == 0) break;
-        const uint32_t m = n < bits ? n : bits;
-        bits -= m;
-        uint64_t x = rd.bits(m);
-        while (n < 64u && bits != 0) {
-            --bits;
-            if (!rd.bit()) break;
-            const uint32_t room = 63u - (n < 63u ? n : 63u);
-            bool hit;
-            const uint32_t z = rd.skip_zeros(room < bits ? room : bits, &hit);
-            bits -= z + (hit ? 1u : 0u);
-            n += z;
-            x |= 1ull << n;
-            ++n;
-        }
-        lo[k] = (uint32_t)x;
-        hi[k] = (uint32_t)(x >> 32);
-    }
-    bit_transpose32(lo);
-    bit_transpose32(hi);
-}
-
 __device__ __forceinline__ int32_t zfp_uint2int(uint32_t x)
 {
     return (int32_t)((x ^ 0xaaaaaaaau) - 0xaaaaaaaau);
 }
 
-// inverse_lift (zfp_decompress.comp:296-332), wrapping int32 arithmetic
+// inverse_lift (zfp_decompress.comp:296-332).  WGSL integer arithmetic wraps,
+// and streams that are not encoder output (or corrupt ones) do overflow here,
+// so adds, subtracts and left shifts run in uint32 (C++ signed overflow would
+// be undefined and the compiler may assume it away); only >> is on int32
+// (arithmetic shift, as on the reference's int).
 __device__ __forceinline__ void zfp_inv_lift(int32_t& x, int32_t& y, int32_t& z, int32_t& w)
 {
-    y += w >> 1;
-    w -= y >> 1;
-    y += w;
-    w = (int32_t)((uint32_t)w << 1);
-    w -= y;
-    z += x;
-    x = (int32_t)((uint32_t)x << 1);
-    x -= z;
-    y += z;
-    z = (int32_t)((uint32_t)z << 1);
-    z -= y;
-    w += x;
-    x = (int32_t)((uint32_t)x << 1);
-    x -= w;
+    uint32_t ux = (uint32_t)x, uy = (uint32_t)y, uz = (uint32_t)z, uw = (uint32_t)w;
+    uy += (uint32_t)((int32_t)uw >> 1);
+    uw -= (uint32_t)((int32_t)uy >> 1);
+    uy += uw;
+    uw <<= 1;
+    uw -= uy;
+    uz += ux;
+    ux <<= 1;
+    ux -= uz;
+    uy += uz;
+    uz <<= 1;
+    uz -= uy;
+    uw += ux;
+    ux <<= 1;
+    ux -= uw;
+    x = (int32_t)ux;
+    y = (int32_t)uy;
+    z = (int32_t)uz;
+    w = (int32_t)uw;
 }
 
 __device__ __forceinline__ void zfp_inverse_transform(int32_t* v)
@@ -286,7 +225,7 @@ __device__ __forceinline__ float zfp_inv_weight(int32_t emax)
 
 // Decode one block starting at `bit_offset` into out[64] (natural order).
 // kDeposit: 0 = per-set-bit deposit into a local array, 1 = register
-// shift-in per plane, 2 = plane rows + bit transpose.
+// shift-in per plane (faster on GB300 for both bulk and latency-bound decodes).
 template <int kDeposit = 0>
 __device__ __forceinline__ void zfp_decode_block(const uint64_t* __restrict__ words,
                                                  uint64_t bit_offset, uint32_t max_bits,
@@ -301,8 +240,7 @@ __device__ __forceinline__ void zfp_decode_block(const uint64_t* __restrict__ wo
     }
     const int32_t emax = (int32_t)((uint32_t)rd.bits(8) - 127u);
     uint32_t u[64];
-    if (kDeposit == 2) zfp_decode_ints_planes(rd, max_bits - 9u, u);
-    else if (kDeposit == 1) zfp_decode_ints_regs(rd, max_bits - 9u, u);
+    if (kDeposit == 1) zfp_decode_ints_regs(rd, max_bits - 9u, u);
     else zfp_decode_ints(rd, max_bits - 9u, u);
     int32_t v[64];
     uint32_t un[64];
