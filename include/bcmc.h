@@ -253,6 +253,57 @@ bcmc_status bcmc_zfp_encode(bcmc_ctx* ctx, const float* d_field, const uint32_t 
 bcmc_status bcmc_block_active(bcmc_ctx* ctx, const float* d_ranges, const uint32_t dims[3],
                               float isovalue, uint32_t* d_active, void* stream);
 
+/* ---- Batched engine ------------------------------------------------------ */
+/* No counterpart in the reference, which runs one computeSurface at a time per
+ * volume.  An engine holds several compressed volumes resident on one device
+ * and one pool of decoded-block slots shared by all of them, and answers a
+ * batch of (volume, isovalue) queries with a fixed, device-driven launch
+ * sequence: every query's active test and compaction in one persistent launch,
+ * the decode of every block some query needs and no slot holds, every query's
+ * marching cubes in one persistent launch.  Each query's vertices are the
+ * vertices the plain path (bcmc_compute_surface on that volume) returns for it,
+ * bit for bit and in the same order: the mesh depends only on the decoded
+ * values of the active blocks, not on which slots hold them.  Slots are reused
+ * across batches and evicted least-recently-used when the pool is full. */
+typedef struct bcmc_engine bcmc_engine;
+typedef struct {
+    uint64_t pool_slots;       /* decoded-block slots (256 B each); 0 = every block of every volume */
+    uint64_t vertex_capacity;  /* initial vertices per batch (grows on demand); 0 = 1<<24 */
+    uint32_t max_batch;        /* queries per launch sequence; 0 = 1024 (larger batches are split) */
+    uint32_t flags;            /* reserved, 0 */
+} bcmc_engine_opts;
+typedef struct {
+    uint32_t volume;  /* id from bcmc_engine_add_volume */
+    float isovalue;
+} bcmc_query;
+typedef struct {
+    uint64_t vertex_offset;     /* first vertex of this query in the batch vertex buffer */
+    uint32_t num_vertices;
+    uint32_t num_active_blocks;
+} bcmc_query_result;
+typedef struct {
+    uint64_t batches, launch_sequences, queries, decoded_blocks, evicted_blocks;
+    uint64_t pool_slots, pool_used, vertex_capacity, device_bytes;
+    double last_batch_ms;       /* device time of the last batch (CUDA events) */
+} bcmc_engine_stats;
+
+bcmc_status bcmc_engine_create(bcmc_ctx* ctx, const bcmc_engine_opts* opts, bcmc_engine** out);
+void bcmc_engine_destroy(bcmc_engine* eng);
+/* Uploads a fixed-rate ZFP stream (host bytes, as bcmc_volume_create) and
+ * computes its block ranges; *volume receives its id. */
+bcmc_status bcmc_engine_add_volume(bcmc_engine* eng, const uint8_t* zfp, size_t len, uint32_t rate,
+                                   const uint32_t dims[3], uint32_t* volume);
+/* Runs n queries (split into launch sequences of at most max_batch) and blocks
+ * until their vertex counts are known.  results[i] locates query i's vertices
+ * in the batch vertex buffer (valid until the next run on this engine). */
+bcmc_status bcmc_engine_run(bcmc_engine* eng, const bcmc_query* queries, uint32_t n,
+                            bcmc_query_result* results);
+/* The batch vertex buffer of the last run: 8 bytes per vertex, laid out as the
+ * plain path's (packed 10:10:10 position, block id). */
+bcmc_status bcmc_engine_vertices(bcmc_engine* eng, const void** d_vertices, uint64_t* count);
+bcmc_status bcmc_engine_copy_vertices(bcmc_engine* eng, uint64_t first, uint64_t count, void* host);
+bcmc_status bcmc_engine_stats_get(bcmc_engine* eng, bcmc_engine_stats* out);
+
 #ifdef __cplusplus
 }
 #endif

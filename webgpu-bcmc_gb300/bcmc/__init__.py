@@ -8,6 +8,8 @@ over the CUDA library libbcmc_gb300.so (C ABI: include/bcmc.h):
 * ``ExclusiveScanPipeline`` / ``ExclusiveScanner``  js/exclusive_scan.js
 * ``StreamCompact``            js/stream_compact.js
 * ``RadixSorter``              js/radix_sort_by_key.js
+* ``Engine``                   (no reference counterpart) batched queries over
+                               several resident volumes, shared slot pool
 
 Method names, argument meaning and return values follow the reference.  The
 WebGPU ``device`` argument becomes a CUDA device ordinal or a ``Context``;
@@ -28,7 +30,7 @@ from ._lib import BcmcError, check, dims3, scale3
 
 __all__ = ["Context", "CompressedMarchingCubes", "LRUCache", "ExclusiveScanPipeline", "ExclusiveScanner",
            "StreamCompact", "RadixSorter", "DeviceArray", "BcmcError", "zfp_encode", "zfp_decode_volume",
-           "zfp_block_ranges", "block_active", "stream_words"]
+           "zfp_block_ranges", "block_active", "stream_words", "Engine"]
 
 
 def _torch():
@@ -515,3 +517,73 @@ def block_active(ctx: Context, ranges, dims, isovalue: float):
                                         C.c_void_p(out.data_ptr()), None), ctx.handle)
     ctx.synchronize()
     return out
+
+
+class Engine:
+    """Batched isosurface queries over several resident compressed volumes
+    with one shared pool of decoded-block slots (bcmc_engine_*).  Every query's
+    vertices equal what CompressedMarchingCubes.computeSurface returns for it
+    on its volume, bit for bit."""
+
+    def __init__(self, device=0, pool_slots: int = 0, vertex_capacity: int = 0, max_batch: int = 0):
+        self.ctx = _ctx(device)
+        o = _lib.bcmc_engine_opts(int(pool_slots), int(vertex_capacity), int(max_batch), 0)
+        h = C.c_void_p()
+        check(_lib.load().bcmc_engine_create(self.ctx.handle, C.byref(o), C.byref(h)), self.ctx.handle)
+        self._h = h
+        self.volumes = []
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _lib.load().bcmc_engine_destroy(self._h)
+            self._h = None
+
+    def addVolume(self, volume, compressionRate: int, volumeDims) -> int:
+        ptr, nbytes, keep, on_dev = _host_bytes(volume)
+        if on_dev:
+            raise ValueError("Engine.addVolume takes the compressed stream in host memory")
+        vid = C.c_uint32()
+        check(_lib.load().bcmc_engine_add_volume(self._h, ptr, nbytes, int(compressionRate), dims3(volumeDims),
+                                                 C.byref(vid)), self.ctx.handle)
+        del keep
+        self.volumes.append((tuple(int(d) for d in volumeDims), int(compressionRate)))
+        return int(vid.value)
+
+    def run(self, queries) -> np.ndarray:
+        """queries: sequence of (volume id, isovalue).  Returns a structured
+        array (vertex_offset, num_vertices, num_active_blocks) per query."""
+        n = len(queries)
+        qs = (_lib.bcmc_query * max(n, 1))()
+        for i, (v, iso) in enumerate(queries):
+            qs[i].volume = int(v)
+            qs[i].isovalue = float(iso)
+        res = (_lib.bcmc_query_result * max(n, 1))()
+        check(_lib.load().bcmc_engine_run(self._h, qs, n, res), self.ctx.handle)
+        out = np.zeros(n, dtype=[("vertex_offset", "<u8"), ("num_vertices", "<u4"), ("num_active_blocks", "<u4")])
+        for i in range(n):
+            out[i] = (res[i].vertex_offset, res[i].num_vertices, res[i].num_active_blocks)
+        return out
+
+    @property
+    def vertexBuffer(self) -> DeviceArray:
+        p = C.c_void_p()
+        cnt = C.c_uint64()
+        check(_lib.load().bcmc_engine_vertices(self._h, C.byref(p), C.byref(cnt)), self.ctx.handle)
+        return DeviceArray(p.value, (int(cnt.value), 2), "<u4", self)
+
+    def copyVertices(self, first: int = 0, count: int | None = None, out: np.ndarray | None = None) -> np.ndarray:
+        if count is None:
+            p = C.c_void_p()
+            cnt = C.c_uint64()
+            check(_lib.load().bcmc_engine_vertices(self._h, C.byref(p), C.byref(cnt)), self.ctx.handle)
+            count = int(cnt.value) - int(first)
+        if out is None:
+            out = np.empty((count, 2), dtype=np.uint32)
+        check(_lib.load().bcmc_engine_copy_vertices(self._h, int(first), int(count), out.ctypes.data_as(C.c_void_p)),
+              self.ctx.handle)
+        return out[:count]
+
+    def stats(self) -> dict:
+        st = _lib.bcmc_engine_stats()
+        check(_lib.load().bcmc_engine_stats_get(self._h, C.byref(st)), self.ctx.handle)
+        return {k: getattr(st, k) for k, _ in _lib.bcmc_engine_stats._fields_}

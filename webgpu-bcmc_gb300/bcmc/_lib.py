@@ -54,6 +54,25 @@ class bcmc_lru_view(C.Structure):
                 ("lastNumSlotsAvailable", C.c_uint32)]
 
 
+class bcmc_engine_opts(C.Structure):
+    _fields_ = [("pool_slots", C.c_uint64), ("vertex_capacity", C.c_uint64), ("max_batch", C.c_uint32),
+                ("flags", C.c_uint32)]
+
+
+class bcmc_query(C.Structure):
+    _fields_ = [("volume", C.c_uint32), ("isovalue", C.c_float)]
+
+
+class bcmc_query_result(C.Structure):
+    _fields_ = [("vertex_offset", C.c_uint64), ("num_vertices", C.c_uint32), ("num_active_blocks", C.c_uint32)]
+
+
+class bcmc_engine_stats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("batches", "launch_sequences", "queries", "decoded_blocks",
+                                           "evicted_blocks", "pool_slots", "pool_used", "vertex_capacity",
+                                           "device_bytes")] + [("last_batch_ms", C.c_double)]
+
+
 P = C.c_void_p
 U32 = C.c_uint32
 U64 = C.c_uint64
@@ -87,6 +106,13 @@ SIGNATURES = {
     "bcmc_scan_exclusive_u32": (C.c_int, [P, P, U32, U32, U32P]),
     "bcmc_scan_exclusive_u32_async": (C.c_int, [P, P, P, U32, P, P]),
     "bcmc_scan_exclusive_u32_noalloc": (C.c_int, [P, P, U32, P, P]),
+    "bcmc_engine_create": (C.c_int, [P, C.POINTER(bcmc_engine_opts), C.POINTER(P)]),
+    "bcmc_engine_destroy": (None, [P]),
+    "bcmc_engine_add_volume": (C.c_int, [P, P, C.c_size_t, U32, U32P, U32P]),
+    "bcmc_engine_run": (C.c_int, [P, C.POINTER(bcmc_query), U32, C.POINTER(bcmc_query_result)]),
+    "bcmc_engine_vertices": (C.c_int, [P, C.POINTER(P), C.POINTER(U64)]),
+    "bcmc_engine_copy_vertices": (C.c_int, [P, U64, U64, P]),
+    "bcmc_engine_stats_get": (C.c_int, [P, C.POINTER(bcmc_engine_stats)]),
     "bcmc_compact_ids": (C.c_int, [P, U32, P, P, P, P]),
     "bcmc_select_ids": (C.c_int, [P, U32, P, P, P, P]),
     "bcmc_sort_aligned_size": (U32, [U32]),

@@ -107,8 +107,8 @@ static void ctx_release(bcmc_ctx* ctx)
 
 // A context outlives the volumes and caches made from it, whatever order the
 // caller destroys them in (garbage collectors finalize in arbitrary order).
-static void ctx_child_added(bcmc_ctx* ctx) { ++ctx->children; }
-static void ctx_child_removed(bcmc_ctx* ctx)
+void bcmc::ctx_child_added(bcmc_ctx* ctx) { ++ctx->children; }
+void bcmc::ctx_child_removed(bcmc_ctx* ctx)
 {
     if (--ctx->children == 0 && ctx->destroy_pending) ctx_release(ctx);
 }

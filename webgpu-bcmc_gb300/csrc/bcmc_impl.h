@@ -37,6 +37,10 @@ namespace bcmc {
 extern std::atomic<uint64_t> g_kernel_launches;
 inline void count_launches(uint64_t n) { g_kernel_launches.fetch_add(n, std::memory_order_relaxed); }
 
+// Objects made from a context (volumes, caches, engines) keep it alive:
+// bcmc_ctx_destroy defers the release until the last of them is gone.
+void ctx_child_added(bcmc_ctx* ctx);
+void ctx_child_removed(bcmc_ctx* ctx);
 // Growable device allocation helpers (cudaMalloc; throw CudaError).
 void* dev_alloc(bcmc_ctx* ctx, size_t bytes);
 void dev_free(bcmc_ctx* ctx, void* p, size_t bytes);

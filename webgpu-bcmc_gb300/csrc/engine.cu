@@ -1,0 +1,1204 @@
+// engine.cu -- batched isosurface queries over several resident volumes with
+// one shared pool of decoded-block slots (bcmc_engine_* in include/bcmc.h).
+//
+// A launch sequence answers up to max_batch (volume, isovalue) queries:
+//   k_bbegin   new look-back epoch, counters cleared
+//   k_bactive  every query's active test over its volume's blocks, as one
+//              stream of 1024-block tiles (query-major).  A tile whose
+//              extended value range (its blocks and their 26 neighbours, from
+//              volume load) excludes the isovalue is skipped whole.  Active
+//              flags go to a per-query bitmap; active (query, block) entries
+//              are compacted in query-major, block-ascending order by one
+//              decoupled look-back over all tiles; blocks no slot holds are
+//              claimed (one claim per block across the batch) and given a
+//              slot from the pool's free list
+//   k_bdecode  ZFP decode of every claimed block into its slot
+//   k_bmc      marching cubes over all entries: the per-query kernel's
+//              range-per-CTA count pass, one look-back per CTA, emit pass;
+//              per-block isovalue, volume and neighbour flags come from the
+//              entry's query; every query's vertices come out contiguous and
+//              in the plain path's order
+//   k_bfinish  per-query vertex offsets and counts
+// replayed as one CUDA graph per batch-size bucket.  The host reads the batch
+// state once at the end and re-runs only when a capacity was exceeded (entry
+// list, slot pool -> eviction of slots the batch does not use, vertex buffer).
+#include <algorithm>
+#include <map>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "active_test.cuh"
+#include "bcmc_impl.h"
+#include "mc_common.cuh"
+#include "zfp_device.cuh"
+
+namespace bcmc {
+namespace {
+
+constexpr int kEngThreads = 256;
+constexpr uint32_t kEngTile = 1024;  // blocks per active tile (4 per thread)
+constexpr int kBmcBlocks = 16;
+constexpr int kBmcThreads = 256;
+constexpr int kBmcCells = 64 * kBmcBlocks;
+constexpr int kBmcPerSm = 6;
+constexpr uint32_t kMaxVolumes = 4096;
+
+struct EngVolDev {
+    const uint64_t* words;
+    const float2* ranges;
+    const float2* tile_ext;  // extended range of each 1024-block tile
+    int32_t* item_slots;     // slot of each block, -1 none, -2 claimed by this batch
+    BlockGrid grid;
+    uint32_t total;
+    uint32_t max_bits;
+};
+
+struct EngQuery {
+    uint32_t vol;
+    float iso;
+    uint32_t tile0;  // first tile of this query in the batch's tile stream
+    uint32_t bit0;   // first word of its active bitmap
+};
+
+struct EngResult {
+    unsigned long long vstart;
+    uint32_t nverts;
+    uint32_t nactive;
+};
+
+// Batch state: written by the host before a sequence (inputs) and by the
+// kernels (counters, outputs), read back once at the end.
+struct EngState {
+    // inputs
+    uint32_t nq, ntiles, entry_capacity, use_epoch;
+    unsigned long long vert_capacity, vert_base;
+    // device-side
+    uint32_t epoch, tiles_active, tiles_mc, num_entries;
+    uint32_t num_decode, pool_exhausted, entry_overflow, vert_overflow;
+    uint32_t error, pad0;
+    unsigned long long num_verts;  // this sequence's vertices (64-bit, from the per-query totals)
+};
+
+// Free list of pool slots: slots free_list[head % cap .. tail % cap) are free.
+struct EngPool {
+    uint32_t capacity;
+    uint32_t head;  // advanced by allocations (may overshoot tail; the host clamps)
+    uint32_t tail;  // advanced by evictions
+    uint32_t pad;
+};
+
+struct BatchArgs {
+    const EngVolDev* vols;
+    const EngQuery* queries;
+    EngResult* results;
+    EngState* st;
+    EngPool* pool;
+    uint32_t* free_list;
+    uint32_t* last_use;
+    uint32_t* owner_vol;
+    uint32_t* owner_block;
+    float* cache;
+    uint32_t* bitmap;
+    uint32_t* ent_id;
+    uint32_t* ent_q;
+    uint32_t* block_counts;
+    uint32_t* q_nactive;
+    uint32_t* q_nverts;
+    uint32_t* dec_vol;
+    uint32_t* dec_block;
+    uint32_t* dec_slot;
+    uint2* verts;
+    uint64_t* status_a;  // look-back over active tiles
+    uint64_t* status_v;  // look-back over MC CTAs (vertices)
+};
+
+// ---------------------------------------------------------------------------
+// volume set-up: extended range of every 1024-block tile
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kEngThreads) k_tile_ext(const float2* __restrict__ ranges, BlockGrid g,
+                                                         uint32_t total, float2* __restrict__ ext)
+{
+    __shared__ float s_lo[kEngThreads / 32], s_hi[kEngThreads / 32];
+    const uint32_t tile = blockIdx.x;
+    float lo = INFINITY, hi = -INFINITY;
+    for (uint32_t i = threadIdx.x; i < kEngTile; i += kEngThreads) {
+        const uint32_t b = tile * kEngTile + i;
+        if (b >= total) break;
+        const uint3 c = block_coords(b, g);
+        for (int dz = -1; dz < 2; ++dz)
+            for (int dy = -1; dy < 2; ++dy)
+                for (int dx = -1; dx < 2; ++dx) {
+                    const int x = (int)c.x + dx, y = (int)c.y + dy, z = (int)c.z + dz;
+                    if (x < 0 || y < 0 || z < 0 || x >= (int)g.nb.x || y >= (int)g.nb.y || z >= (int)g.nb.z)
+                        continue;
+                    const float2 r = __ldg(ranges + ((uint32_t)x + g.nb.x * ((uint32_t)y + g.nb.y * (uint32_t)z)));
+                    lo = fminf(lo, r.x);  // NaN ranges never make a block active: ignored
+                    hi = fmaxf(hi, r.y);
+                }
+    }
+    for (int o = 16; o; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31u) == 0) {
+        s_lo[threadIdx.x >> 5] = lo;
+        s_hi[threadIdx.x >> 5] = hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < kEngThreads / 32; ++w) {
+            lo = fminf(lo, s_lo[w]);
+            hi = fmaxf(hi, s_hi[w]);
+        }
+        ext[tile] = make_float2(lo, hi);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_bbegin
+// ---------------------------------------------------------------------------
+__global__ void k_bbegin(EngState* st, uint32_t* q_nverts, uint32_t* q_nactive, uint32_t nq)
+{
+    if (threadIdx.x == 0) {
+        st->epoch += 1;
+        st->tiles_active = st->tiles_mc = 0;
+        st->num_entries = st->num_decode = 0;
+        st->pool_exhausted = st->entry_overflow = st->vert_overflow = 0;
+        st->error = 0;
+        st->num_verts = 0;
+    }
+    for (uint32_t i = threadIdx.x; i < nq; i += blockDim.x) q_nverts[i] = q_nactive[i] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// k_bactive
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t find_query(const EngQuery* __restrict__ qs, uint32_t nq, uint32_t tile)
+{
+    uint32_t lo = 0, hi = nq;  // last q with tile0 <= tile
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&qs[mid].tile0) <= tile) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Claims block b of volume v for this batch and gives it a slot from the free
+// list; when the pool has no free slot the claim is released and the batch
+// flagged (the host evicts and re-runs).
+__device__ __forceinline__ void claim_block(const BatchArgs& a, uint32_t v, int32_t* item_slots, uint32_t b,
+                                            uint32_t use_epoch)
+{
+    if (atomicCAS(item_slots + b, -1, -2) != -1) return;  // cached meanwhile, or claimed by another query
+    EngPool* pool = a.pool;
+    const uint32_t idx = atomicAdd(&pool->head, 1u);
+    const uint32_t tail = *(volatile uint32_t*)&pool->tail;
+    if ((int32_t)(idx - tail) >= 0) {  // no free slot: release the claim
+        atomicExch(item_slots + b, -1);
+        atomicOr(&a.st->pool_exhausted, 1u);
+        return;
+    }
+    const uint32_t slot = a.free_list[idx % pool->capacity];
+    a.last_use[slot] = use_epoch;
+    const uint32_t d = atomicAdd(&a.st->num_decode, 1u);
+    a.dec_vol[d] = v;
+    a.dec_block[d] = b;
+    a.dec_slot[d] = slot;
+}
+
+__global__ void __launch_bounds__(kEngThreads) k_bactive(BatchArgs a)
+{
+    __shared__ uint32_t s_warp[kEngThreads / 32 + 1];
+    __shared__ uint32_t s_tile, s_q, s_p;
+    EngState* st = a.st;
+    const uint32_t ntiles = st->ntiles, nq = st->nq, epoch = st->epoch, cap = st->entry_capacity;
+    const uint32_t use_epoch = st->use_epoch;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const uint32_t tile = atomicAdd(&st->tiles_active, 1u);
+            s_tile = tile;
+            s_q = tile < ntiles ? find_query(a.queries, nq, tile) : 0u;
+        }
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        if (tile >= ntiles) break;
+        const uint32_t qi = s_q;
+        const EngQuery Q = a.queries[qi];
+        const EngVolDev& V = a.vols[Q.vol];
+        const uint32_t lt = tile - Q.tile0;
+        const uint32_t total = V.total;
+        const float iso = Q.iso;
+        const uint32_t b0 = lt * kEngTile + 4u * threadIdx.x;
+        uint32_t act = 0;
+        const float2 ext = __ldg(V.tile_ext + lt);
+        if (iso >= ext.x && iso <= ext.y && b0 < total) {
+            const uint32_t n = min(4u, total - b0);
+            const uint3 c = block_coords(b0, V.grid);
+            if (n == 4 && c.x + 3 < V.grid.nb.x) {
+                act = row4_active(V.ranges, V.grid, c, b0, iso);
+            } else {
+                for (uint32_t i = 0; i < n; ++i) act |= block_is_active(V.ranges, V.grid, b0 + i, iso) << i;
+            }
+            // cache lookup: mark use, claim what no slot holds
+            for (uint32_t i = 0; i < 4; ++i) {
+                if (!(act >> i & 1u)) continue;
+                const int32_t s = *(volatile int32_t*)(V.item_slots + b0 + i);
+                if (s >= 0) a.last_use[s] = use_epoch;
+                else if (s == -1) claim_block(a, Q.vol, V.item_slots, b0 + i, use_epoch);
+            }
+        }
+        // active bitmap: 8 threads (32 blocks) per word
+        uint32_t word = act << (4u * (threadIdx.x & 7u));
+        word |= __shfl_xor_sync(0xffffffffu, word, 1);
+        word |= __shfl_xor_sync(0xffffffffu, word, 2);
+        word |= __shfl_xor_sync(0xffffffffu, word, 4);
+        if ((threadIdx.x & 7u) == 0) a.bitmap[Q.bit0 + lt * (kEngTile / 32) + (threadIdx.x >> 3)] = word;
+        // compaction of (block, query) entries over the whole tile stream
+        uint32_t tot;
+        const uint32_t excl = cta_exclusive_scan<kEngThreads>((uint32_t)__popc(act), s_warp, &tot);
+        if (threadIdx.x < 32) {
+            const uint32_t p = warp_lookback(a.status_a, tile, tot, epoch, &st->error, 60u);
+            if (threadIdx.x == 0) {
+                s_p = p;
+                if (tot) atomicAdd(a.q_nactive + qi, tot);
+                if (tile == ntiles - 1) {
+                    st->num_entries = p + tot;
+                    if (p + tot > cap) st->entry_overflow = 1;
+                }
+            }
+        }
+        __syncthreads();
+        uint32_t pos = s_p + excl;
+#pragma unroll
+        for (uint32_t i = 0; i < 4; ++i) {
+            if (act >> i & 1u) {
+                if (pos < cap) {
+                    a.ent_id[pos] = b0 + i;
+                    a.ent_q[pos] = qi;
+                }
+                ++pos;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_bdecode: claimed blocks into their slots, then publish the slot
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_bdecode(BatchArgs a)
+{
+    const uint32_t n = a.st->num_decode;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t v = a.dec_vol[i], b = a.dec_block[i], slot = a.dec_slot[i];
+        const EngVolDev& V = a.vols[v];
+        float out[64];
+        zfp_decode_block<1>(V.words, (uint64_t)b * V.max_bits, V.max_bits, out);
+        float4* d4 = reinterpret_cast<float4*>(a.cache + (uint64_t)slot * 64u);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) d4[k] = make_float4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
+        a.owner_vol[slot] = v;
+        a.owner_block[slot] = b;
+        V.item_slots[b] = (int32_t)slot;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_bmc: the per-query MC kernel (pipeline.cu, k_mc) over a batch's entries
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBmcThreads, kBmcPerSm) k_bmc(BatchArgs a)
+{
+    __shared__ float s_vol[kBmcBlocks][128];
+    __shared__ int8_t s_tri[256][16];
+    __shared__ uint8_t s_cnt[256];
+    __shared__ uint8_t s_edge[12];
+    __shared__ __align__(16) uint8_t s_case[kBmcCells];
+    __shared__ uint32_t s_off[kBmcCells + 1];
+    __shared__ uint32_t s_id[kBmcBlocks];
+    __shared__ uint32_t s_qi[kBmcBlocks];
+    __shared__ float s_iso[kBmcBlocks];
+    __shared__ uint32_t s_slot[kBmcBlocks][8];
+    __shared__ uint32_t s_act[kBmcBlocks];
+    __shared__ uint32_t s_warp[kBmcThreads / 32 + 1];
+    __shared__ uint32_t s_any, s_pv, s_cta_v, s_rank;
+    __shared__ uint16_t s_ghost[64];
+    __shared__ uint8_t s_nb_off[8];
+
+    EngState* st = a.st;
+    const uint32_t A = min(st->num_entries, st->entry_capacity);
+    if (A == 0 || st->entry_overflow || st->pool_exhausted) return;
+    const uint32_t epoch = st->epoch;
+    const uint64_t cap = st->vert_capacity, vbase = st->vert_base;
+    const uint32_t t = threadIdx.x;
+    const uint32_t G = gridDim.x;
+    if (t == 0) s_rank = atomicAdd(&st->tiles_mc, 1u);
+    __syncthreads();
+    const uint32_t rank = s_rank;
+    const uint32_t range = div_up(div_up(A, G), kBmcBlocks) * kBmcBlocks;
+    const uint32_t start = min(A, rank * range), end = min(A, start + range);
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(&kTriEdges[0][0]);
+        uint4* dst = reinterpret_cast<uint4*>(&s_tri[0][0]);
+        for (uint32_t i = t; i < 256; i += kBmcThreads) dst[i] = src[i];
+        for (uint32_t i = t; i < 256; i += kBmcThreads) {
+            uint32_t n = 0;
+            while (n < 16 && kTriEdges[i][n] != -1) ++n;
+            s_cnt[i] = (uint8_t)n;
+        }
+        if (t < 12) s_edge[t] = (uint8_t)(c_corner[c_edge[t][0]] | (c_corner[c_edge[t][1]] << 3));
+        if (t == 0) s_cta_v = 0;
+        if (t < 61) s_ghost[t] = c_ghost[t];
+        if (t < 7) s_nb_off[t] = c_nb_off[t];
+    }
+    const uint32_t j = t >> 4, u = t & 15u, ry = u & 3u, rz = u >> 2;
+    uint64_t pv = 0;
+
+    for (int pass = 0; pass < 2; ++pass) {
+        if (pass == 1) {
+            __syncthreads();
+            if (t < 32) {
+                const uint32_t p = warp_lookback(a.status_v, rank, s_cta_v, epoch, &st->error, 61u);
+                if (t == 0) s_pv = p;
+            }
+            __syncthreads();
+            // 32-bit prefix: a batch over 2^32 vertices wraps here; k_bfinish
+            // detects it from the 64-bit per-query totals and the host splits
+            pv = vbase + s_pv;
+            if (pv + s_cta_v > cap) {
+                if (t == 0) atomicOr(&st->vert_overflow, 1u);
+                break;
+            }
+        }
+        for (uint32_t base = start; base < end; base += kBmcBlocks) {
+            __syncthreads();
+            if (t == 0) s_any = 0;
+            __syncthreads();
+            if (t < kBmcBlocks) {
+                const uint32_t idx = base + t;
+                uint32_t id = 0xffffffffu, qi = 0;
+                if (idx < end && (pass == 0 || a.block_counts[idx] != 0u)) {
+                    id = __ldg(a.ent_id + idx);
+                    qi = __ldg(a.ent_q + idx);
+                }
+                s_id[t] = id;
+                s_qi[t] = qi;
+                s_iso[t] = __ldg(&a.queries[qi].iso);
+                if (id != 0xffffffffu) s_any = 1;
+            }
+            __syncthreads();
+            if (!s_any) continue;
+            if (t < kBmcBlocks * 8) {
+                const uint32_t jb = t >> 3, k = t & 7u, id = s_id[jb];
+                uint32_t slot = 0xffffffffu, act = 0;
+                if (id != 0xffffffffu) {
+                    const EngQuery* Q = a.queries + s_qi[jb];
+                    const EngVolDev& V = a.vols[__ldg(&Q->vol)];
+                    const uint3 nb = V.grid.nb;
+                    const uint3 bc = block_coords(id, V.grid);
+                    if (k == kNbSelf) {
+                        slot = (uint32_t)__ldg(V.item_slots + id);
+                        act = (bc.x + 1 < nb.x ? 0x100u : 0u) | (bc.y + 1 < nb.y ? 0x200u : 0u) |
+                              (bc.z + 1 < nb.z ? 0x400u : 0u);
+                    } else {
+                        const uint32_t o = s_nb_off[k], ox = o & 1u, oy = (o >> 1) & 1u, oz = o >> 2;
+                        if (bc.x + ox < nb.x && bc.y + oy < nb.y && bc.z + oz < nb.z) {
+                            const uint32_t nid = id + ox + nb.x * (oy + nb.y * oz);
+                            const uint32_t w = __ldg(a.bitmap + __ldg(&Q->bit0) + (nid >> 5));
+                            act = (w >> (nid & 31u)) & 1u;
+                            slot = (uint32_t)__ldg(V.item_slots + nid);
+                        }
+                    }
+                }
+                s_slot[jb][k] = slot;
+                const uint32_t bits = __ballot_sync(0xffffffffu, (act & 1u) != 0u);
+                if (k == kNbSelf) s_act[jb] = ((bits >> (t & 24u)) & 0x7fu) | act;
+            }
+            __syncthreads();
+            const uint32_t id = s_id[j];
+            const bool valid = id != 0xffffffffu;
+            const float iso = s_iso[j];
+            uint32_t dims = 0;
+            if (valid) {
+                const uint32_t act = s_act[j];
+                dims = block_dims_with_ghost(act, (act & 0x100u) != 0u, (act & 0x200u) != 0u, (act & 0x400u) != 0u);
+                const uint32_t slot = s_slot[j][kNbSelf];
+                const uint32_t slots = a.pool->capacity;
+                float4 v4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (slot < slots) v4 = __ldg(reinterpret_cast<const float4*>(a.cache + (uint64_t)slot * 64u) + u);
+                else atomicCAS(&st->error, 0u, 62u);
+                const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
+                float gv[4];
+                uint32_t gaddr[4];
+#pragma unroll
+                for (uint32_t r = 0; r < 4; ++r) {
+                    const uint32_t gi = u + 16u * r;
+                    gv[r] = 0.0f;
+                    gaddr[r] = 0xffffffffu;
+                    if (gi < 61) {
+                        const uint32_t g = s_ghost[gi];
+                        const uint32_t gx = g & 15u, gy = (g >> 4) & 15u, gz = (g >> 8) & 15u;
+                        if (gx < dx && gy < dy && gz < dz) {
+                            const uint32_t nslot = s_slot[j][g >> 12];
+                            if (nslot < slots) {
+                                gv[r] = __ldg(a.cache + (uint64_t)nslot * 64u + (gx & 3u) + 4u * ((gy & 3u) + 4u * (gz & 3u)));
+                                gaddr[r] = gx + 5u * (gy + 5u * gz);
+                            } else {
+                                atomicCAS(&st->error, 0u, 63u);
+                            }
+                        }
+                    }
+                }
+                float* row = &s_vol[j][5u * (ry + 5u * rz)];
+                row[0] = v4.x;
+                row[1] = v4.y;
+                row[2] = v4.z;
+                row[3] = v4.w;
+#pragma unroll
+                for (uint32_t r = 0; r < 4; ++r)
+                    if (gaddr[r] != 0xffffffffu) s_vol[j][gaddr[r]] = gv[r];
+            }
+            __syncthreads();
+            uint32_t nv[4], cs4 = 0, mysum = 0;
+            {
+                const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
+                const bool row_ok = valid && ry + 1 < dy && rz + 1 < dz;
+#pragma unroll
+                for (uint32_t x = 0; x < 4; ++x) {
+                    uint32_t cs = 0;
+                    nv[x] = 0;
+                    if (row_ok && x + 1 < dx) {
+                        const float* v = &s_vol[j][x + 5u * (ry + 5u * rz)];
+                        cs = (v[0] <= iso ? 1u : 0u) | (v[1] <= iso ? 2u : 0u) | (v[6] <= iso ? 4u : 0u) |
+                             (v[5] <= iso ? 8u : 0u) | (v[25] <= iso ? 16u : 0u) | (v[26] <= iso ? 32u : 0u) |
+                             (v[31] <= iso ? 64u : 0u) | (v[30] <= iso ? 128u : 0u);
+                        nv[x] = s_cnt[cs];
+                    }
+                    cs4 |= cs << (8u * x);
+                    mysum += nv[x];
+                }
+            }
+            uint32_t tile_v;
+            uint32_t run = cta_exclusive_scan<kBmcThreads>(mysum, s_warp, &tile_v);
+            if (pass == 0) {
+                uint32_t bsum = mysum;
+#pragma unroll
+                for (int o = 8; o; o >>= 1) bsum += __shfl_xor_sync(0xffffffffu, bsum, o);
+                if (u == 0 && valid) {
+                    a.block_counts[base + j] = bsum;
+                    if (bsum) atomicAdd(a.q_nverts + s_qi[j], bsum);
+                }
+                if (t == 0) s_cta_v += tile_v;
+                continue;
+            }
+            *reinterpret_cast<uint32_t*>(&s_case[4u * t]) = cs4;
+#pragma unroll
+            for (uint32_t x = 0; x < 4; ++x) {
+                s_off[4u * t + x] = run;
+                run += nv[x];
+            }
+            if (t == 0) s_off[kBmcCells] = tile_v;
+            __syncthreads();
+            uint2* out = a.verts + pv;
+            for (uint32_t k = t; k < tile_v; k += kBmcThreads) {
+                uint32_t cell = 0;
+#pragma unroll
+                for (uint32_t step = kBmcCells / 2; step; step >>= 1)
+                    if (s_off[cell + step] <= k) cell += step;
+                const uint32_t tt_idx = k - s_off[cell];
+                const uint32_t ed = s_edge[(uint32_t)s_tri[s_case[cell]][tt_idx]];
+                const uint32_t jb = cell >> 6, cc = cell & 63u;
+                const float biso = s_iso[jb];
+                const uint32_t x = cc & 3u, y = (cc >> 2) & 3u, z = cc >> 4;
+                const uint32_t o0 = ed & 7u, o1 = ed >> 3;
+                const uint32_t ax = o0 & 1u, ay = (o0 >> 1) & 1u, az = o0 >> 2;
+                const uint32_t bx = o1 & 1u, by = (o1 >> 1) & 1u, bz = o1 >> 2;
+                const float fa = s_vol[jb][(x + ax) + 5u * ((y + ay) + 5u * (z + az))];
+                const float fb = s_vol[jb][(x + bx) + 5u * ((y + by) + 5u * (z + bz))];
+                float tt = 0.0f;
+                if (!(fabsf(__fsub_rn(fa, fb)) < 0.001f)) tt = __fdiv_rn(__fsub_rn(biso, fa), __fsub_rn(fb, fa));
+                uint32_t qx, qy, qz;
+                if (isfinite(tt)) {
+                    const uint32_t d = (o0 ^ o1) >> 1;
+                    const uint32_t ad = (o0 >> d) & 1u, vd = d == 0 ? x : (d == 1 ? y : z);
+                    const float pd = __fadd_rn(__fadd_rn(ad ? __fsub_rn(1.0f, tt) : tt, (float)vd), 0.5f);
+                    const uint32_t qd = quantize(pd);
+                    qx = d == 0 ? qd : (((ax + x) * 1023u) >> 2);
+                    qy = d == 1 ? qd : (((ay + y) * 1023u) >> 2);
+                    qz = d == 2 ? qd : (((az + z) * 1023u) >> 2);
+                } else {
+                    qx = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)ax, __fmul_rn(tt, (float)((int)bx - (int)ax))), (float)x), 0.5f));
+                    qy = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)ay, __fmul_rn(tt, (float)((int)by - (int)ay))), (float)y), 0.5f));
+                    qz = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)az, __fmul_rn(tt, (float)((int)bz - (int)az))), (float)z), 0.5f));
+                }
+                out[k] = make_uint2((qx << 20) | (qy << 10) | qz, s_id[jb]);
+            }
+            pv += tile_v;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_bfinish: per-query results (one CTA; queries in order)
+// ---------------------------------------------------------------------------
+constexpr int kFinThreads = 1024;
+__global__ void __launch_bounds__(kFinThreads) k_bfinish(BatchArgs a)
+{
+    __shared__ unsigned long long s_sum[kFinThreads / 32 + 1];
+    EngState* st = a.st;
+    const uint32_t nq = st->nq;
+    const uint64_t vbase = st->vert_base;
+    unsigned long long carry = 0;
+    for (uint32_t b0 = 0; b0 < nq; b0 += kFinThreads) {
+        const uint32_t i = b0 + threadIdx.x;
+        const unsigned long long v = i < nq ? a.q_nverts[i] : 0ull;
+        // inclusive scan in 64 bits: warp shuffles, then the warp totals
+        unsigned long long x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if ((threadIdx.x & 31u) >= (uint32_t)o) x += y;
+        }
+        if ((threadIdx.x & 31u) == 31u) s_sum[threadIdx.x >> 5] = x;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long r = 0;
+            for (int w = 0; w < kFinThreads / 32; ++w) {
+                const unsigned long long tw = s_sum[w];
+                s_sum[w] = r;
+                r += tw;
+            }
+            s_sum[kFinThreads / 32] = r;
+        }
+        __syncthreads();
+        const unsigned long long excl = carry + s_sum[threadIdx.x >> 5] + x - v;
+        if (i < nq) {
+            EngResult r;
+            r.vstart = vbase + excl;
+            r.nverts = (uint32_t)v;
+            r.nactive = a.q_nactive[i];
+            a.results[i] = r;
+        }
+        carry += s_sum[kFinThreads / 32];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        st->num_verts = carry;
+        if (vbase + carry > st->vert_capacity || carry >= (1ull << 32)) st->vert_overflow = 1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_bevict: free every slot the current batch does not use
+// ---------------------------------------------------------------------------
+__global__ void k_bevict(BatchArgs a, uint32_t use_epoch, uint32_t nslots, unsigned long long* evicted)
+{
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < nslots; s += gridDim.x * blockDim.x) {
+        const uint32_t v = a.owner_vol[s];
+        if (v == 0xffffffffu || a.last_use[s] == use_epoch) continue;
+        a.vols[v].item_slots[a.owner_block[s]] = -1;
+        a.owner_vol[s] = 0xffffffffu;
+        const uint32_t pos = atomicAdd(&a.pool->tail, 1u);
+        a.free_list[pos % a.pool->capacity] = s;
+        atomicAdd(evicted, 1ull);
+    }
+}
+
+__global__ void k_fill_u32(uint32_t* p, uint64_t n, uint32_t v)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+__global__ void k_iota(uint32_t* p, uint32_t n)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = i;
+}
+
+}  // namespace
+}  // namespace bcmc
+
+using namespace bcmc;
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct EngVolume {
+    uint32_t dims[3];
+    uint32_t rate;
+    uint64_t* words = nullptr;
+    size_t words_bytes = 0;
+    float2* ranges = nullptr;
+    float2* tile_ext = nullptr;
+    int32_t* item_slots = nullptr;
+    uint32_t total = 0, tiles = 0;
+    BlockGrid grid;
+};
+
+struct bcmc_engine {
+    bcmc_ctx* ctx = nullptr;
+    cudaStream_t stream = nullptr;
+    bcmc_engine_opts opts{};
+    std::vector<EngVolume> vols;
+    EngVolDev* d_vols = nullptr;
+    uint32_t d_vols_cap = 0;
+    // pool
+    uint64_t pool_slots = 0;
+    float* cache = nullptr;
+    uint32_t *free_list = nullptr, *last_use = nullptr, *owner_vol = nullptr, *owner_block = nullptr;
+    EngPool* d_pool = nullptr;
+    EngPool* h_pool = nullptr;
+    unsigned long long* d_evicted = nullptr;
+    // batch buffers
+    uint32_t max_batch = 0;
+    EngQuery* d_queries = nullptr;
+    EngQuery* h_queries = nullptr;  // pinned
+    EngResult* d_results = nullptr;
+    EngResult* h_results = nullptr;  // pinned
+    EngState* d_st = nullptr;
+    EngState* h_st = nullptr;  // pinned
+    uint32_t *q_nactive = nullptr, *q_nverts = nullptr;
+    uint32_t* bitmap = nullptr;
+    uint64_t bitmap_words = 0;
+    uint32_t *ent_id = nullptr, *ent_q = nullptr, *block_counts = nullptr;
+    uint32_t entry_cap = 0;
+    uint32_t *dec_vol = nullptr, *dec_block = nullptr, *dec_slot = nullptr;
+    uint32_t dec_cap = 0;
+    uint2* verts = nullptr;
+    uint64_t vert_cap = 0, vert_used = 0;
+    uint64_t* status = nullptr;
+    uint64_t status_words = 0;
+    uint64_t status_a_words = 0;
+    uint64_t epoch_calls = 0;
+    uint32_t use_epoch = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // one graph per batch-size bucket, rebuilt when buffers move
+    struct Graph {
+        cudaGraphExec_t exec = nullptr;
+        uint64_t generation = 0;
+    };
+    std::map<uint32_t, Graph> graphs;
+    uint64_t generation = 1;
+    bcmc_engine_stats stats{};
+};
+
+namespace {
+
+int eng_grid_mc(bcmc_engine* e) { return e->ctx->num_sms * kBmcPerSm; }
+int eng_grid_act(bcmc_engine* e) { return e->ctx->num_sms * 8; }
+int eng_grid_dec(bcmc_engine* e) { return e->ctx->num_sms * 16; }
+
+template <typename T>
+void eng_realloc(bcmc_engine* e, T*& p, uint64_t old_n, uint64_t new_n)
+{
+    dev_free(e->ctx, p, old_n * sizeof(T));
+    p = nullptr;
+    p = (T*)dev_alloc(e->ctx, new_n * sizeof(T));
+}
+
+BatchArgs eng_args(bcmc_engine* e)
+{
+    BatchArgs a;
+    a.vols = e->d_vols;
+    a.queries = e->d_queries;
+    a.results = e->d_results;
+    a.st = e->d_st;
+    a.pool = e->d_pool;
+    a.free_list = e->free_list;
+    a.last_use = e->last_use;
+    a.owner_vol = e->owner_vol;
+    a.owner_block = e->owner_block;
+    a.cache = e->cache;
+    a.bitmap = e->bitmap;
+    a.ent_id = e->ent_id;
+    a.ent_q = e->ent_q;
+    a.block_counts = e->block_counts;
+    a.q_nactive = e->q_nactive;
+    a.q_nverts = e->q_nverts;
+    a.dec_vol = e->dec_vol;
+    a.dec_block = e->dec_block;
+    a.dec_slot = e->dec_slot;
+    a.verts = e->verts;
+    a.status_a = e->status;
+    a.status_v = e->status + e->status_a_words;
+    return a;
+}
+
+void eng_ensure_status(bcmc_engine* e, uint64_t active_tiles)
+{
+    const uint64_t need_a = std::max<uint64_t>(active_tiles + 1, 1024);
+    const uint64_t need = need_a + (uint64_t)eng_grid_mc(e) + 1;
+    if (need_a <= e->status_a_words && need <= e->status_words) return;
+    BCMC_CUDA(cudaStreamSynchronize(e->stream));
+    const uint64_t words = std::max<uint64_t>(need_a * 2, 4096) + eng_grid_mc(e) + 1;
+    eng_realloc(e, e->status, e->status_words, words);
+    BCMC_CUDA(cudaMemsetAsync(e->status, 0, words * 8, e->stream));
+    e->status_words = words;
+    e->status_a_words = words - eng_grid_mc(e) - 1;
+    ++e->generation;
+}
+
+// Every 2^26 sequences the look-back epoch restarts over cleared status words.
+void eng_epoch_tick(bcmc_engine* e)
+{
+    if (++e->epoch_calls < (1ull << 26)) return;
+    BCMC_CUDA(cudaMemsetAsync(e->status, 0, e->status_words * 8, e->stream));
+    BCMC_CUDA(cudaMemsetAsync(&e->d_st->epoch, 0, 4, e->stream));
+    e->epoch_calls = 0;
+}
+
+void eng_upload_vols(bcmc_engine* e)
+{
+    const uint32_t n = (uint32_t)e->vols.size();
+    if (n > e->d_vols_cap) {
+        eng_realloc(e, e->d_vols, e->d_vols_cap, std::max<uint32_t>(n * 2, 8));
+        e->d_vols_cap = std::max<uint32_t>(n * 2, 8);
+        ++e->generation;
+    }
+    std::vector<EngVolDev> h(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        const EngVolume& v = e->vols[i];
+        h[i] = EngVolDev{v.words, v.ranges, v.tile_ext, v.item_slots, v.grid, v.total, 64u * v.rate};
+    }
+    BCMC_CUDA(cudaMemcpyAsync(e->d_vols, h.data(), n * sizeof(EngVolDev), cudaMemcpyHostToDevice, e->stream));
+    BCMC_CUDA(cudaStreamSynchronize(e->stream));
+}
+
+void eng_alloc_pool(bcmc_engine* e, uint64_t slots)
+{
+    if (slots == 0 || slots > 0xffffffffull) throw std::invalid_argument("pool_slots out of range");
+    e->pool_slots = slots;
+    e->cache = (float*)dev_alloc(e->ctx, slots * 256);
+    e->free_list = (uint32_t*)dev_alloc(e->ctx, slots * 4);
+    e->last_use = (uint32_t*)dev_alloc(e->ctx, slots * 4);
+    e->owner_vol = (uint32_t*)dev_alloc(e->ctx, slots * 4);
+    e->owner_block = (uint32_t*)dev_alloc(e->ctx, slots * 4);
+    // every successful claim of a batch takes a free slot: the decode list
+    // never needs more entries than the pool has slots
+    e->dec_vol = (uint32_t*)dev_alloc(e->ctx, slots * 4);
+    e->dec_block = (uint32_t*)dev_alloc(e->ctx, slots * 4);
+    e->dec_slot = (uint32_t*)dev_alloc(e->ctx, slots * 4);
+    e->dec_cap = (uint32_t)slots;
+    const int grid = e->ctx->num_sms * 8;
+    k_iota<<<grid, 256, 0, e->stream>>>(e->free_list, (uint32_t)slots);
+    k_fill_u32<<<grid, 256, 0, e->stream>>>(e->owner_vol, slots, 0xffffffffu);
+    k_fill_u32<<<grid, 256, 0, e->stream>>>(e->last_use, slots, 0u);
+    count_launches(3);
+    e->h_pool->capacity = (uint32_t)slots;
+    e->h_pool->head = 0;
+    e->h_pool->tail = (uint32_t)slots;
+    BCMC_CUDA(cudaMemcpyAsync(e->d_pool, e->h_pool, sizeof(EngPool), cudaMemcpyHostToDevice, e->stream));
+    BCMC_CUDA(cudaStreamSynchronize(e->stream));
+    ++e->generation;
+}
+
+void eng_ensure_batch(bcmc_engine* e, uint64_t bitmap_words, uint32_t entries)
+{
+    if (bitmap_words > e->bitmap_words) {
+        BCMC_CUDA(cudaStreamSynchronize(e->stream));
+        const uint64_t n = std::max<uint64_t>(bitmap_words + bitmap_words / 2, 1u << 16);
+        eng_realloc(e, e->bitmap, e->bitmap_words, n);
+        e->bitmap_words = n;
+        ++e->generation;
+    }
+    if (entries > e->entry_cap) {
+        BCMC_CUDA(cudaStreamSynchronize(e->stream));
+        const uint64_t n64 = std::min<uint64_t>((uint64_t)entries + entries / 2, 0xffffffffull);
+        const uint32_t n = (uint32_t)std::max<uint64_t>(n64, 1u << 16);
+        eng_realloc(e, e->ent_id, e->entry_cap, n);
+        eng_realloc(e, e->ent_q, e->entry_cap, n);
+        eng_realloc(e, e->block_counts, e->entry_cap, n);
+        e->entry_cap = n;
+        ++e->generation;
+    }
+}
+
+void eng_ensure_verts(bcmc_engine* e, uint64_t need)
+{
+    if (need <= e->vert_cap) return;
+    BCMC_CUDA(cudaStreamSynchronize(e->stream));
+    const uint64_t n = std::max<uint64_t>(need + need / 2, 1u << 20);
+    // keep the vertices already written by earlier sequences of this run
+    uint2* nv = (uint2*)dev_alloc(e->ctx, n * sizeof(uint2));
+    if (e->vert_used)
+        BCMC_CUDA(cudaMemcpyAsync(nv, e->verts, e->vert_used * sizeof(uint2), cudaMemcpyDeviceToDevice, e->stream));
+    BCMC_CUDA(cudaStreamSynchronize(e->stream));
+    dev_free(e->ctx, e->verts, e->vert_cap * sizeof(uint2));
+    e->verts = nv;
+    e->vert_cap = n;
+    ++e->generation;
+}
+
+// The launch sequence of one batch (also what a graph captures).
+void eng_enqueue(bcmc_engine* e, uint32_t bucket)
+{
+    cudaStream_t s = e->stream;
+    const BatchArgs a = eng_args(e);
+    BCMC_CUDA(cudaMemcpyAsync(e->d_queries, e->h_queries, bucket * sizeof(EngQuery), cudaMemcpyHostToDevice, s));
+    BCMC_CUDA(cudaMemcpyAsync(e->d_st, e->h_st, offsetof(EngState, epoch), cudaMemcpyHostToDevice, s));
+    BCMC_CUDA(cudaEventRecordWithFlags(e->ev0, s, cudaEventRecordExternal));
+    k_bbegin<<<1, 1024, 0, s>>>(e->d_st, e->q_nverts, e->q_nactive, bucket);
+    k_bactive<<<eng_grid_act(e), kEngThreads, 0, s>>>(a);
+    k_bdecode<<<eng_grid_dec(e), 128, 0, s>>>(a);
+    count_launches(3);
+    k_bmc<<<eng_grid_mc(e), kBmcThreads, 0, s>>>(a);
+    k_bfinish<<<1, kFinThreads, 0, s>>>(a);
+    count_launches(2);
+    BCMC_CUDA(cudaGetLastError());
+    BCMC_CUDA(cudaEventRecordWithFlags(e->ev1, s, cudaEventRecordExternal));
+    BCMC_CUDA(cudaMemcpyAsync(e->h_st, e->d_st, sizeof(EngState), cudaMemcpyDeviceToHost, s));
+    BCMC_CUDA(cudaMemcpyAsync(e->h_results, e->d_results, bucket * sizeof(EngResult), cudaMemcpyDeviceToHost, s));
+}
+
+void eng_launch(bcmc_engine* e, uint32_t bucket)
+{
+    auto& g = e->graphs[bucket];
+    if (!g.exec || g.generation != e->generation) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+        cudaGraph_t graph = nullptr;
+        const uint64_t before = g_kernel_launches.load();
+        BCMC_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+        try {
+            eng_enqueue(e, bucket);
+        } catch (...) {
+            cudaStreamEndCapture(e->stream, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            throw;
+        }
+        BCMC_CUDA(cudaStreamEndCapture(e->stream, &graph));
+        g_kernel_launches.store(before);  // captured, not launched
+        const cudaError_t err = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        BCMC_CUDA(err);
+        g.generation = e->generation;
+    }
+    BCMC_CUDA(cudaGraphLaunch(g.exec, e->stream));
+    count_launches(5);
+}
+
+uint32_t bucket_of(uint32_t n)
+{
+    uint32_t b = 1;
+    while (b < n) b <<= 1;
+    return b;
+}
+
+// Runs queries[0..n) (n <= max_batch) as one launch sequence; results go to out.
+// Throws std::length_error when the pool cannot hold the sequence's active blocks.
+void eng_run_sequence(bcmc_engine* e, const bcmc_query* queries, uint32_t n, bcmc_query_result* out)
+{
+    const uint32_t bucket = std::min(bucket_of(n), e->max_batch);
+    uint64_t tiles = 0, words = 0;
+    for (uint32_t i = 0; i < bucket; ++i) {
+        EngQuery q{};
+        if (i < n) {
+            if (queries[i].volume >= e->vols.size()) throw std::invalid_argument("unknown volume id");
+            const EngVolume& v = e->vols[queries[i].volume];
+            q.vol = queries[i].volume;
+            q.iso = queries[i].isovalue;
+            q.tile0 = (uint32_t)tiles;
+            q.bit0 = (uint32_t)words;
+            tiles += v.tiles;
+            words += (uint64_t)v.tiles * (kEngTile / 32);
+        } else {  // padding queries of the bucket: no tiles
+            q.vol = 0;
+            q.iso = 0.0f;
+            q.tile0 = (uint32_t)tiles;
+            q.bit0 = (uint32_t)words;
+        }
+        e->h_queries[i] = q;
+    }
+    if (tiles >= 0xffffffffull || words >= 0xffffffffull) throw std::invalid_argument("batch too large");
+    eng_ensure_status(e, tiles);
+    eng_ensure_batch(e, words, std::max<uint32_t>(e->entry_cap, 1u << 16));
+    ++e->use_epoch;
+    for (int attempt = 0;; ++attempt) {
+        if (attempt > 8) throw std::runtime_error("batch did not converge");
+        eng_ensure_verts(e, e->vert_used + 1);
+        EngState& st = *e->h_st;
+        st.nq = bucket;
+        st.ntiles = (uint32_t)tiles;
+        st.entry_capacity = e->entry_cap;
+        st.use_epoch = e->use_epoch;
+        st.vert_capacity = e->vert_cap;
+        st.vert_base = e->vert_used;
+        eng_epoch_tick(e);
+        eng_launch(e, bucket);
+        BCMC_CUDA(cudaStreamSynchronize(e->stream));
+        ++e->stats.launch_sequences;
+        if (st.error) throw std::runtime_error("device wait timed out in the batched engine");
+        e->stats.decoded_blocks += st.num_decode;
+        if (st.entry_overflow) {
+            eng_ensure_batch(e, words, st.num_entries);
+            continue;
+        }
+        if (st.pool_exhausted) {
+            // the pool's head overshot its tail: clamp, then free what this batch does not use
+            BCMC_CUDA(cudaMemcpyAsync(e->h_pool, e->d_pool, sizeof(EngPool), cudaMemcpyDeviceToHost, e->stream));
+            BCMC_CUDA(cudaStreamSynchronize(e->stream));
+            e->h_pool->head = e->h_pool->tail;
+            BCMC_CUDA(cudaMemcpyAsync(e->d_pool, e->h_pool, sizeof(EngPool), cudaMemcpyHostToDevice, e->stream));
+            BCMC_CUDA(cudaMemsetAsync(e->d_evicted, 0, 8, e->stream));
+            k_bevict<<<e->ctx->num_sms * 8, 256, 0, e->stream>>>(eng_args(e), e->use_epoch, (uint32_t)e->pool_slots,
+                                                                 e->d_evicted);
+            count_launches(1);
+            unsigned long long ev = 0;
+            BCMC_CUDA(cudaMemcpyAsync(&ev, e->d_evicted, 8, cudaMemcpyDeviceToHost, e->stream));
+            BCMC_CUDA(cudaStreamSynchronize(e->stream));
+            e->stats.evicted_blocks += ev;
+            if (ev == 0) throw std::length_error("the slot pool cannot hold one batch's active blocks");
+            continue;
+        }
+        if (st.vert_overflow) {
+            if (st.num_verts >= (1ull << 32)) throw std::length_error("batch above 2^32 vertices");
+            eng_ensure_verts(e, e->vert_used + st.num_verts);
+            continue;  // the re-run finds every block cached: no decode work repeats
+        }
+        break;
+    }
+    for (uint32_t i = 0; i < n; ++i) {
+        out[i].vertex_offset = e->h_results[i].vstart;
+        out[i].num_vertices = e->h_results[i].nverts;
+        out[i].num_active_blocks = e->h_results[i].nactive;
+    }
+    e->vert_used += e->h_st->num_verts;
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, e->ev0, e->ev1) == cudaSuccess) e->stats.last_batch_ms = ms;
+    e->stats.queries += n;
+}
+
+// Admission by slot memory: a batch whose active blocks do not fit the pool
+// (even after evicting every slot it does not use) runs as two halves.
+void eng_run_chunk(bcmc_engine* e, const bcmc_query* queries, uint32_t n, bcmc_query_result* out)
+{
+    try {
+        eng_run_sequence(e, queries, n, out);
+    } catch (const std::length_error&) {
+        if (n < 2) throw;
+        const uint32_t h = n / 2;
+        eng_run_chunk(e, queries, h, out);
+        eng_run_chunk(e, queries + h, n - h, out + h);
+    }
+}
+
+void eng_free(bcmc_engine* e)
+{
+    bcmc_ctx* ctx = e->ctx;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    for (auto& kv : e->graphs)
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    for (auto& v : e->vols) {
+        dev_free(ctx, v.words, v.words_bytes);
+        dev_free(ctx, v.ranges, (size_t)v.total * 8);
+        dev_free(ctx, v.tile_ext, (size_t)v.tiles * 8);
+        dev_free(ctx, v.item_slots, (size_t)v.total * 4);
+    }
+    dev_free(ctx, e->d_vols, e->d_vols_cap * sizeof(EngVolDev));
+    dev_free(ctx, e->cache, e->pool_slots * 256);
+    dev_free(ctx, e->free_list, e->pool_slots * 4);
+    dev_free(ctx, e->last_use, e->pool_slots * 4);
+    dev_free(ctx, e->owner_vol, e->pool_slots * 4);
+    dev_free(ctx, e->owner_block, e->pool_slots * 4);
+    dev_free(ctx, e->d_pool, sizeof(EngPool));
+    dev_free(ctx, e->d_evicted, 8);
+    dev_free(ctx, e->d_queries, e->max_batch * sizeof(EngQuery));
+    dev_free(ctx, e->d_results, e->max_batch * sizeof(EngResult));
+    dev_free(ctx, e->d_st, sizeof(EngState));
+    dev_free(ctx, e->q_nactive, e->max_batch * 4);
+    dev_free(ctx, e->q_nverts, e->max_batch * 4);
+    dev_free(ctx, e->bitmap, e->bitmap_words * 4);
+    dev_free(ctx, e->ent_id, (size_t)e->entry_cap * 4);
+    dev_free(ctx, e->ent_q, (size_t)e->entry_cap * 4);
+    dev_free(ctx, e->block_counts, (size_t)e->entry_cap * 4);
+    dev_free(ctx, e->dec_vol, (size_t)e->dec_cap * 4);
+    dev_free(ctx, e->dec_block, (size_t)e->dec_cap * 4);
+    dev_free(ctx, e->dec_slot, (size_t)e->dec_cap * 4);
+    dev_free(ctx, e->verts, e->vert_cap * sizeof(uint2));
+    dev_free(ctx, e->status, e->status_words * 8);
+    if (e->h_queries) cudaFreeHost(e->h_queries);
+    if (e->h_results) cudaFreeHost(e->h_results);
+    if (e->h_st) cudaFreeHost(e->h_st);
+    if (e->h_pool) cudaFreeHost(e->h_pool);
+    if (e->ev0) cudaEventDestroy(e->ev0);
+    if (e->ev1) cudaEventDestroy(e->ev1);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+    ctx_child_removed(ctx);
+}
+
+template <typename F>
+bcmc_status eng_guarded(bcmc_engine* e, F&& f)
+{
+    try {
+        return f();
+    } catch (const CudaError& x) {
+        e->ctx->last_error = std::string(x.what) + ": " + cudaGetErrorString(x.err);
+        return x.err == cudaErrorMemoryAllocation ? BCMC_E_OOM : BCMC_E_CUDA;
+    } catch (const std::invalid_argument& x) {
+        e->ctx->last_error = x.what();
+        return BCMC_E_ARG;
+    } catch (const std::length_error& x) {
+        e->ctx->last_error = x.what();
+        return BCMC_E_ADMISSION;
+    } catch (const std::bad_alloc&) {
+        e->ctx->last_error = "host allocation failed";
+        return BCMC_E_OOM;
+    } catch (const std::exception& x) {
+        e->ctx->last_error = x.what();
+        return BCMC_E_CUDA;
+    }
+}
+
+}  // namespace
+
+extern "C" bcmc_status bcmc_engine_create(bcmc_ctx* ctx, const bcmc_engine_opts* opts, bcmc_engine** out)
+{
+    if (!ctx || !out) return BCMC_E_ARG;
+    *out = nullptr;
+    bcmc_engine* e = new (std::nothrow) bcmc_engine();
+    if (!e) return BCMC_E_OOM;
+    e->ctx = ctx;
+    if (opts) e->opts = *opts;
+    if (e->opts.flags != 0) {
+        delete e;
+        return BCMC_E_ARG;
+    }
+    ctx_child_added(ctx);  // eng_free removes it, also on the error path below
+    const bcmc_status st = eng_guarded(e, [&]() -> bcmc_status {
+        BCMC_CUDA(cudaSetDevice(ctx->device));
+        BCMC_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+        BCMC_CUDA(cudaEventCreate(&e->ev0));
+        BCMC_CUDA(cudaEventCreate(&e->ev1));
+        e->max_batch = bucket_of(e->opts.max_batch ? std::min<uint32_t>(e->opts.max_batch, 1u << 16) : 1024u);
+        BCMC_CUDA(cudaMallocHost(&e->h_queries, e->max_batch * sizeof(EngQuery)));
+        BCMC_CUDA(cudaMallocHost(&e->h_results, e->max_batch * sizeof(EngResult)));
+        BCMC_CUDA(cudaMallocHost(&e->h_st, sizeof(EngState)));
+        BCMC_CUDA(cudaMallocHost(&e->h_pool, sizeof(EngPool)));
+        memset(e->h_st, 0, sizeof(EngState));
+        e->d_queries = (EngQuery*)dev_alloc(ctx, e->max_batch * sizeof(EngQuery));
+        e->d_results = (EngResult*)dev_alloc(ctx, e->max_batch * sizeof(EngResult));
+        e->d_st = (EngState*)dev_alloc(ctx, sizeof(EngState));
+        BCMC_CUDA(cudaMemsetAsync(e->d_st, 0, sizeof(EngState), e->stream));
+        e->q_nactive = (uint32_t*)dev_alloc(ctx, e->max_batch * 4);
+        e->q_nverts = (uint32_t*)dev_alloc(ctx, e->max_batch * 4);
+        e->d_pool = (EngPool*)dev_alloc(ctx, sizeof(EngPool));
+        e->d_evicted = (unsigned long long*)dev_alloc(ctx, 8);
+        eng_ensure_verts(e, e->opts.vertex_capacity ? e->opts.vertex_capacity : (1ull << 24));
+        eng_ensure_status(e, 1024);
+        eng_ensure_batch(e, 1u << 16, 1u << 16);
+        BCMC_CUDA(cudaStreamSynchronize(e->stream));
+        return BCMC_OK;
+    });
+    if (st != BCMC_OK) {
+        eng_free(e);
+        return st;
+    }
+    *out = e;
+    return BCMC_OK;
+}
+
+extern "C" void bcmc_engine_destroy(bcmc_engine* e)
+{
+    if (e) eng_free(e);
+}
+
+extern "C" bcmc_status bcmc_engine_add_volume(bcmc_engine* e, const uint8_t* zfp, size_t len, uint32_t rate,
+                                              const uint32_t dims[3], uint32_t* volume)
+{
+    if (!e || !zfp || !dims || !volume || rate == 0 || rate > 32 || !dims[0] || !dims[1] || !dims[2])
+        return BCMC_E_ARG;
+    if (e->vols.size() >= kMaxVolumes) return BCMC_E_ARG;
+    if (e->pool_slots) return BCMC_E_STATE;  // volumes are added before the first run sizes the pool
+    return eng_guarded(e, [&]() -> bcmc_status {
+        EngVolume v;
+        for (int i = 0; i < 3; ++i) v.dims[i] = dims[i];
+        v.rate = rate;
+        const uint3 nb = make_uint3(div_up(dims[0], 4u), div_up(dims[1], 4u), div_up(dims[2], 4u));
+        const uint64_t total = (uint64_t)nb.x * nb.y * nb.z;
+        if (total >= (1ull << 31)) throw std::invalid_argument("volume too large");
+        const uint64_t need = (total * 64u * rate + 7) / 8;
+        if (len < need) throw std::invalid_argument("compressed stream shorter than the volume needs");
+        v.total = (uint32_t)total;
+        v.tiles = div_up(v.total, kEngTile);
+        v.grid = make_block_grid(nb);
+        const uint64_t words = (need + 7) / 8 + 2;
+        v.words_bytes = words * 8;
+        v.words = (uint64_t*)dev_alloc(e->ctx, v.words_bytes);
+        BCMC_CUDA(cudaMemsetAsync(v.words, 0, v.words_bytes, e->stream));
+        BCMC_CUDA(cudaMemcpyAsync(v.words, zfp, need, cudaMemcpyHostToDevice, e->stream));
+        v.ranges = (float2*)dev_alloc(e->ctx, (size_t)v.total * 8);
+        v.tile_ext = (float2*)dev_alloc(e->ctx, (size_t)v.tiles * 8);
+        v.item_slots = (int32_t*)dev_alloc(e->ctx, (size_t)v.total * 4);
+        BCMC_CUDA(cudaMemsetAsync(v.item_slots, 0xff, (size_t)v.total * 4, e->stream));  // -1
+        zfp_ranges_launch(e->ctx, v.words, dims, 64u * rate, reinterpret_cast<float*>(v.ranges), e->stream);
+        k_tile_ext<<<v.tiles, kEngThreads, 0, e->stream>>>(v.ranges, v.grid, v.total, v.tile_ext);
+        count_launches(1);
+        BCMC_CUDA(cudaGetLastError());
+        BCMC_CUDA(cudaStreamSynchronize(e->stream));
+        *volume = (uint32_t)e->vols.size();
+        e->vols.push_back(v);
+        eng_upload_vols(e);
+        return BCMC_OK;
+    });
+}
+
+extern "C" bcmc_status bcmc_engine_run(bcmc_engine* e, const bcmc_query* queries, uint32_t n,
+                                       bcmc_query_result* results)
+{
+    if (!e || (n && (!queries || !results))) return BCMC_E_ARG;
+    if (e->vols.empty()) return BCMC_E_STATE;
+    return eng_guarded(e, [&]() -> bcmc_status {
+        if (!e->pool_slots) {
+            uint64_t all = 0;
+            for (auto& v : e->vols) all += v.total;
+            eng_alloc_pool(e, e->opts.pool_slots ? e->opts.pool_slots : all);
+        }
+        e->vert_used = 0;
+        for (uint32_t i = 0; i < n; i += e->max_batch) {
+            const uint32_t m = std::min(e->max_batch, n - i);
+            eng_run_chunk(e, queries + i, m, results + i);
+        }
+        ++e->stats.batches;
+        return BCMC_OK;
+    });
+}
+
+extern "C" bcmc_status bcmc_engine_vertices(bcmc_engine* e, const void** d_vertices, uint64_t* count)
+{
+    if (!e || !d_vertices || !count) return BCMC_E_ARG;
+    *d_vertices = e->verts;
+    *count = e->vert_used;
+    return BCMC_OK;
+}
+
+extern "C" bcmc_status bcmc_engine_copy_vertices(bcmc_engine* e, uint64_t first, uint64_t count, void* host)
+{
+    if (!e || (count && !host) || first > e->vert_used || count > e->vert_used - first) return BCMC_E_ARG;
+    return eng_guarded(e, [&]() -> bcmc_status {
+        if (count)
+            BCMC_CUDA(cudaMemcpyAsync(host, e->verts + first, count * sizeof(uint2), cudaMemcpyDeviceToHost, e->stream));
+        BCMC_CUDA(cudaStreamSynchronize(e->stream));
+        return BCMC_OK;
+    });
+}
+
+extern "C" bcmc_status bcmc_engine_stats_get(bcmc_engine* e, bcmc_engine_stats* out)
+{
+    if (!e || !out) return BCMC_E_ARG;
+    return eng_guarded(e, [&]() -> bcmc_status {
+        bcmc_engine_stats s = e->stats;
+        s.pool_slots = e->pool_slots;
+        if (e->pool_slots) {
+            BCMC_CUDA(cudaMemcpyAsync(e->h_pool, e->d_pool, sizeof(EngPool), cudaMemcpyDeviceToHost, e->stream));
+            BCMC_CUDA(cudaStreamSynchronize(e->stream));
+            const uint32_t head = std::min(e->h_pool->head, e->h_pool->tail);
+            s.pool_used = e->pool_slots - (e->h_pool->tail - head);
+        }
+        s.vertex_capacity = e->vert_cap;
+        s.device_bytes = e->ctx->device_bytes;
+        *out = s;
+        return BCMC_OK;
+    });
+}

@@ -1,0 +1,64 @@
+// mc_common.cuh -- tables and helpers of the marching-cubes kernels, shared
+// by the per-query MC kernel (pipeline.cu) and the batched one (engine.cu).
+// The __constant__ tables are static: each translation unit has its own copy.
+#pragma once
+
+#include "bcmc_internal.cuh"
+
+namespace bcmc {
+
+#define BCMC_TABLE_QUALIFIER static __constant__
+#include "mc_tables.inc"
+#undef BCMC_TABLE_QUALIFIER
+
+// corner i of a cell (compute_vertex_values.comp:48-57), packed x|y<<1|z<<2
+static __constant__ uint8_t c_corner[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+// cube edge -> its two corners (compute_block_vertices.comp:10-23)
+static __constant__ uint8_t c_edge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {6, 5},
+                                      {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+
+// Ghost voxels of a block's 5^3 grid (some coordinate == 4): x|y<<4|z<<8 and,
+// in bits 12-14, which +x/+y/+z neighbour holds them (kNb* order below).
+static __constant__ uint16_t c_ghost[61] = {
+#define G(x, y, z, k) (uint16_t)((x) | ((y) << 4) | ((z) << 8) | ((k) << 12))
+    G(4, 0, 0, 0), G(4, 1, 0, 0), G(4, 2, 0, 0), G(4, 3, 0, 0), G(0, 4, 0, 1), G(1, 4, 0, 1), G(2, 4, 0, 1),
+    G(3, 4, 0, 1), G(4, 4, 0, 3), G(4, 0, 1, 0), G(4, 1, 1, 0), G(4, 2, 1, 0), G(4, 3, 1, 0), G(0, 4, 1, 1),
+    G(1, 4, 1, 1), G(2, 4, 1, 1), G(3, 4, 1, 1), G(4, 4, 1, 3), G(4, 0, 2, 0), G(4, 1, 2, 0), G(4, 2, 2, 0),
+    G(4, 3, 2, 0), G(0, 4, 2, 1), G(1, 4, 2, 1), G(2, 4, 2, 1), G(3, 4, 2, 1), G(4, 4, 2, 3), G(4, 0, 3, 0),
+    G(4, 1, 3, 0), G(4, 2, 3, 0), G(4, 3, 3, 0), G(0, 4, 3, 1), G(1, 4, 3, 1), G(2, 4, 3, 1), G(3, 4, 3, 1),
+    G(4, 4, 3, 3), G(0, 0, 4, 2), G(1, 0, 4, 2), G(2, 0, 4, 2), G(3, 0, 4, 2), G(4, 0, 4, 4), G(0, 1, 4, 2),
+    G(1, 1, 4, 2), G(2, 1, 4, 2), G(3, 1, 4, 2), G(4, 1, 4, 4), G(0, 2, 4, 2), G(1, 2, 4, 2), G(2, 2, 4, 2),
+    G(3, 2, 4, 2), G(4, 2, 4, 4), G(0, 3, 4, 2), G(1, 3, 4, 2), G(2, 3, 4, 2), G(3, 3, 4, 2), G(4, 3, 4, 4),
+    G(0, 4, 4, 5), G(1, 4, 4, 5), G(2, 4, 4, 5), G(3, 4, 4, 5), G(4, 4, 4, 6)
+#undef G
+};
+// neighbour k of a block: +x, +y, +z, +xy, +xz, +yz, +xyz (packed x|y<<1|z<<2)
+static __constant__ uint8_t c_nb_off[7] = {1, 2, 4, 3, 5, 6, 7};
+enum { kNbX = 0, kNbY, kNbZ, kNbXY, kNbXZ, kNbYZ, kNbXYZ, kNbSelf };
+
+// compute_vertex_values.comp:96-156: grid extent of the block plus the ghost
+// layer taken from active +x/+y/+z neighbours, tested corner, edges, faces.
+// `act` has bit k set when neighbour k exists and is active.
+__device__ __forceinline__ uint32_t block_dims_with_ghost(uint32_t act, bool hx, bool hy, bool hz)
+{
+    uint32_t dx = hx ? 5 : 4, dy = hy ? 5 : 4, dz = hz ? 5 : 4;
+    if (dx == 5 && dy == 5 && dz == 5 && !(act >> kNbXYZ & 1u)) dx = dy = dz = 4;
+    if (dx == 5 && dy == 5 && !(act >> kNbXY & 1u)) dx = dy = 4;
+    if (dx == 5 && dz == 5 && !(act >> kNbXZ & 1u)) dx = dz = 4;
+    if (dy == 5 && dz == 5 && !(act >> kNbYZ & 1u)) dy = dz = 4;
+    if (dx == 5 && !(act >> kNbX & 1u)) dx = 4;
+    if (dy == 5 && !(act >> kNbY & 1u)) dy = 4;
+    if (dz == 5 && !(act >> kNbZ & 1u)) dz = 4;
+    return dx | (dy << 4) | (dz << 8);
+}
+
+// block_vertex_position.comp:9-17 with the f32 operations of
+// compute_block_vertices.comp:62-74,161-162 in the reference's order, each
+// rounded on its own (no contraction).
+__device__ __forceinline__ uint32_t quantize(float p)
+{
+    const float f = __fmul_rn(__fmul_rn(__fsub_rn(p, 0.5f), 0.25f), 1023.0f);
+    return __float2uint_rz(f) & 0x3ffu;  // saturating float->uint, as WGSL u32()
+}
+
+}  // namespace bcmc

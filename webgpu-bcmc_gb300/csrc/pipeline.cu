@@ -21,20 +21,12 @@
 //                  (compute_block_has_vertices.comp,
 //                  compute_block_voxel_num_verts.comp,
 //                  compute_block_vertices.comp)
+#include "active_test.cuh"
 #include "bcmc_pipeline.h"
+#include "mc_common.cuh"
 #include "zfp_device.cuh"
 
 namespace bcmc {
-
-#define BCMC_TABLE_QUALIFIER __constant__
-#include "mc_tables.inc"
-#undef BCMC_TABLE_QUALIFIER
-
-// corner i of a cell (compute_vertex_values.comp:48-57), packed x|y<<1|z<<2
-__constant__ uint8_t c_corner[8] = {0, 1, 3, 2, 4, 5, 7, 6};
-// cube edge -> its two corners (compute_block_vertices.comp:10-23)
-__constant__ uint8_t c_edge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {6, 5},
-                                      {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
 
 // Starts a query: inputs come from the arguments, or, when `from_state` is
 // set, from q->in (written by the graph's host-to-device copy).
@@ -79,83 +71,6 @@ constexpr int kSlotItems = 2;
 constexpr int kSlotTile = kActThreads * kSlotItems;  // slots per k_slots tile
 
 __device__ __forceinline__ uint32_t spad8(uint32_t i) { return i + (i >> 5); }
-
-// compute_block_active.comp:24-61.  The reference tests, for each of the 26
-// neighbours n, iso in [min(lo_b, lo_n), max(hi_b, hi_n)].  With A = (iso >=
-// lo), B = (iso <= hi) that is (A_b || A_n) && (B_b || B_n), so over all
-// neighbours (and b itself, which adds nothing new):
-//   active = (A_b && anyB) || (B_b && anyA) || any(A_n && B_n)
-// -- the same booleans, evaluated without branches or early exits.
-__device__ __forceinline__ uint32_t block_is_active(const float2* __restrict__ ranges, const BlockGrid& g,
-                                                    uint32_t b, float iso)
-{
-    const uint3 nb = g.nb;
-    const float2 r = __ldg(ranges + b);
-    const bool A = iso >= r.x, B = iso <= r.y;
-    const uint3 c = block_coords(b, g);
-    const int bx = (int)c.x, by = (int)c.y, bz = (int)c.z;
-    bool anyA = false, anyB = false, anyC = false;
-#pragma unroll
-    for (int k = -1; k < 2; ++k)
-#pragma unroll
-        for (int j = -1; j < 2; ++j)
-#pragma unroll
-            for (int i = -1; i < 2; ++i) {
-                const int cx = bx + i, cy = by + j, cz = bz + k;
-                if (cx < 0 || cy < 0 || cz < 0 || cx >= (int)nb.x || cy >= (int)nb.y || cz >= (int)nb.z) continue;
-                const float2 n = __ldg(ranges + ((uint32_t)cx + nb.x * ((uint32_t)cy + nb.y * (uint32_t)cz)));
-                const bool an = iso >= n.x, bn = iso <= n.y;
-                anyA |= an;
-                anyB |= bn;
-                anyC |= an && bn;
-            }
-    return ((A && anyB) || (B && anyA) || anyC) ? 1u : 0u;
-}
-
-__device__ __forceinline__ void range_bits(const float2 r, float iso, uint32_t& a, uint32_t& b)
-{
-    a = iso >= r.x ? 1u : 0u;
-    b = iso <= r.y ? 1u : 0u;
-}
-
-// Active flags of the 4 consecutive blocks b0..b0+3 of one x-row: the 9
-// neighbour rows (y-1..y+1, z-1..z+1) are read once for the 4 blocks (6 ranges
-// per row), 13.5 loads per block instead of 27.
-__device__ __forceinline__ uint32_t row4_active(const float2* __restrict__ ranges, const BlockGrid& g, uint3 c,
-                                                uint32_t b0, float iso)
-{
-    const uint3 nb = g.nb;
-    uint32_t anyA = 0, anyB = 0, anyC = 0, selfA = 0, selfB = 0;  // bit i = block b0+i
-#pragma unroll
-    for (int dz = -1; dz < 2; ++dz)
-#pragma unroll
-        for (int dy = -1; dy < 2; ++dy) {
-            const int yy = (int)c.y + dy, zz = (int)c.z + dz;
-            if (yy < 0 || zz < 0 || yy >= (int)nb.y || zz >= (int)nb.z) continue;
-            const int64_t shift = (int64_t)dy * nb.x + (int64_t)dz * nb.x * nb.y;
-            const float2* row = ranges + (int64_t)b0 + shift;  // position x0 of the neighbour row
-            uint32_t A = 0, B = 0;  // bit p = position x0 - 1 + p, p = 0..5
-#pragma unroll
-            for (int p = 0; p < 6; ++p) {
-                const int xx = (int)c.x - 1 + p;
-                if (xx < 0 || xx >= (int)nb.x) continue;
-                uint32_t a, b;
-                range_bits(__ldg(row + (p - 1)), iso, a, b);
-                A |= a << p;
-                B |= b << p;
-            }
-            const uint32_t C = A & B;
-            // window of block i covers positions i..i+2
-            anyA |= (A | (A >> 1) | (A >> 2)) & 15u;
-            anyB |= (B | (B >> 1) | (B >> 2)) & 15u;
-            anyC |= (C | (C >> 1) | (C >> 2)) & 15u;
-            if (dy == 0 && dz == 0) {
-                selfA = (A >> 1) & 15u;
-                selfB = (B >> 1) & 15u;
-            }
-        }
-    return ((selfA & anyB) | (selfB & anyA) | anyC) & 15u;
-}
 
 __global__ void __launch_bounds__(kActThreads) k_active(QueryState* q, ActiveArgs a)
 {
@@ -363,50 +278,6 @@ __global__ void __launch_bounds__(128) k_assign(QueryState* q, AssignArgs a)
 constexpr int kMcBlocks = 16;
 constexpr int kMcThreads = 256;
 constexpr int kMcCells = 64 * kMcBlocks;  // 4 consecutive cells per thread
-
-// Ghost voxels of a block's 5^3 grid (some coordinate == 4): x|y<<4|z<<8 and,
-// in bits 12-14, which +x/+y/+z neighbour holds them (kNb* order below).
-__constant__ uint16_t c_ghost[61] = {
-#define G(x, y, z, k) (uint16_t)((x) | ((y) << 4) | ((z) << 8) | ((k) << 12))
-    G(4, 0, 0, 0), G(4, 1, 0, 0), G(4, 2, 0, 0), G(4, 3, 0, 0), G(0, 4, 0, 1), G(1, 4, 0, 1), G(2, 4, 0, 1),
-    G(3, 4, 0, 1), G(4, 4, 0, 3), G(4, 0, 1, 0), G(4, 1, 1, 0), G(4, 2, 1, 0), G(4, 3, 1, 0), G(0, 4, 1, 1),
-    G(1, 4, 1, 1), G(2, 4, 1, 1), G(3, 4, 1, 1), G(4, 4, 1, 3), G(4, 0, 2, 0), G(4, 1, 2, 0), G(4, 2, 2, 0),
-    G(4, 3, 2, 0), G(0, 4, 2, 1), G(1, 4, 2, 1), G(2, 4, 2, 1), G(3, 4, 2, 1), G(4, 4, 2, 3), G(4, 0, 3, 0),
-    G(4, 1, 3, 0), G(4, 2, 3, 0), G(4, 3, 3, 0), G(0, 4, 3, 1), G(1, 4, 3, 1), G(2, 4, 3, 1), G(3, 4, 3, 1),
-    G(4, 4, 3, 3), G(0, 0, 4, 2), G(1, 0, 4, 2), G(2, 0, 4, 2), G(3, 0, 4, 2), G(4, 0, 4, 4), G(0, 1, 4, 2),
-    G(1, 1, 4, 2), G(2, 1, 4, 2), G(3, 1, 4, 2), G(4, 1, 4, 4), G(0, 2, 4, 2), G(1, 2, 4, 2), G(2, 2, 4, 2),
-    G(3, 2, 4, 2), G(4, 2, 4, 4), G(0, 3, 4, 2), G(1, 3, 4, 2), G(2, 3, 4, 2), G(3, 3, 4, 2), G(4, 3, 4, 4),
-    G(0, 4, 4, 5), G(1, 4, 4, 5), G(2, 4, 4, 5), G(3, 4, 4, 5), G(4, 4, 4, 6)
-#undef G
-};
-// neighbour k of a block: +x, +y, +z, +xy, +xz, +yz, +xyz (packed x|y<<1|z<<2)
-__constant__ uint8_t c_nb_off[7] = {1, 2, 4, 3, 5, 6, 7};
-enum { kNbX = 0, kNbY, kNbZ, kNbXY, kNbXZ, kNbYZ, kNbXYZ, kNbSelf };
-
-// compute_vertex_values.comp:96-156: grid extent of the block plus the ghost
-// layer taken from active +x/+y/+z neighbours, tested corner, edges, faces.
-// `act` has bit k set when neighbour k exists and is active.
-__device__ __forceinline__ uint32_t block_dims_with_ghost(uint32_t act, bool hx, bool hy, bool hz)
-{
-    uint32_t dx = hx ? 5 : 4, dy = hy ? 5 : 4, dz = hz ? 5 : 4;
-    if (dx == 5 && dy == 5 && dz == 5 && !(act >> kNbXYZ & 1u)) dx = dy = dz = 4;
-    if (dx == 5 && dy == 5 && !(act >> kNbXY & 1u)) dx = dy = 4;
-    if (dx == 5 && dz == 5 && !(act >> kNbXZ & 1u)) dx = dz = 4;
-    if (dy == 5 && dz == 5 && !(act >> kNbYZ & 1u)) dy = dz = 4;
-    if (dx == 5 && !(act >> kNbX & 1u)) dx = 4;
-    if (dy == 5 && !(act >> kNbY & 1u)) dy = 4;
-    if (dz == 5 && !(act >> kNbZ & 1u)) dz = 4;
-    return dx | (dy << 4) | (dz << 8);
-}
-
-// block_vertex_position.comp:9-17 with the f32 operations of
-// compute_block_vertices.comp:62-74,161-162 in the reference's order, each
-// rounded on its own (no contraction).
-__device__ __forceinline__ uint32_t quantize(float p)
-{
-    const float f = __fmul_rn(__fmul_rn(__fsub_rn(p, 0.5f), 0.25f), 1023.0f);
-    return __float2uint_rz(f) & 0x3ffu;  // saturating float->uint, as WGSL u32()
-}
 
 // Marching cubes over the active blocks.  Each CTA owns one contiguous range of
 // active blocks (whole 16-block tiles) and makes two passes over it:
