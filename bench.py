@@ -203,6 +203,100 @@ def decode_bench(ctx, flush, reps: int = 10) -> dict:
             "kernel": "k_decode_volume", "l2": "flushed (512 MB write) before each rep"}
 
 
+BATCH = dict(workload="c4: 256 queries over 8 resident volumes (32^3 blobs, 64^3 value noise, 96x128x80 "
+                      "spectral, 128^3 blobs, 200^3 value noise, 256^3 spectral, 384x384x256 value noise, "
+                      "512^3 spectral), ZFP rate 4, isovalues uniform within each volume's range",
+             volumes=[("blobs", (32, 32, 32)), ("ct_like", (64, 64, 64)), ("turbulence", (96, 128, 80)),
+                      ("blobs", (128, 128, 128)), ("ct_like", (200, 200, 200)), ("turbulence", (256, 256, 256)),
+                      ("ct_like", (384, 384, 256)), ("turbulence", (512, 512, 512))],
+             rate=4, queries=256, seed=4)
+
+
+def batched_bench(reps: int = 5) -> dict:
+    """The batched engine against the plain per-query path on the same 256
+    queries: iso-queries/s, per-query latency, and a bit-exact check of every
+    query's vertices."""
+    import torch
+
+    import bcmc
+    from bcmc import datasets as D
+
+    rate = BATCH["rate"]
+    ctx = bcmc.Context(0)  # plain path: the reference's initial cache of 5 % of the blocks
+    streams, ranges = [], []
+    for i, (kind, dims) in enumerate(BATCH["volumes"]):
+        f = D.make_field(kind, dims, BATCH["seed"] + i)
+        ranges.append((float(f.min()), float(f.max())))
+        w = bcmc.zfp_encode(ctx, torch.from_numpy(f).cuda(), rate)
+        torch.cuda.synchronize()
+        nb = int(np.prod([(d + 3) // 4 for d in dims]))
+        streams.append(w.cpu().numpy().view(np.uint8)[: nb * 64 * rate // 8].copy())
+        del f, w
+    rng = np.random.default_rng(BATCH["seed"])
+    qs = []
+    for i in range(BATCH["queries"]):
+        v = i % len(streams)
+        lo, hi = ranges[v]
+        qs.append((v, float(np.float32(rng.uniform(lo + 0.05 * (hi - lo), hi - 0.05 * (hi - lo))))))
+    total_blocks = sum(int(np.prod([(d + 3) // 4 for d in dims])) for _, dims in BATCH["volumes"])
+
+    # plain per-query path: one CompressedMarchingCubes per volume
+    mcs = []
+    for (kind, dims), st in zip(BATCH["volumes"], streams):
+        mc = bcmc.CompressedMarchingCubes(ctx)
+        mc.setCompressedVolume(st, rate, dims)
+        mcs.append(mc)
+    for v, iso in qs:  # warm-up: caches grow to their working size
+        mcs[v].computeSurface(iso)
+    plain_lat = []
+    t0 = time.perf_counter()
+    for v, iso in qs:
+        tq = time.perf_counter()
+        mcs[v].computeSurface(iso)
+        plain_lat.append(1000.0 * (time.perf_counter() - tq))
+    plain_s = time.perf_counter() - t0
+
+    # batched engine: every volume resident, one pool for all of them
+    eng = bcmc.Engine(ctx, pool_slots=total_blocks, max_batch=BATCH["queries"])
+    for (kind, dims), st in zip(BATCH["volumes"], streams):
+        eng.addVolume(st, rate, dims)
+    eng.run(qs)  # warm-up: decodes the blocks the batch needs
+    launches0 = bcmc._lib.load().bcmc_kernel_launches()
+    batch_ms, dev_ms = [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        res = eng.run(qs)
+        batch_ms.append(1000.0 * (time.perf_counter() - t0))
+        dev_ms.append(eng.stats()["last_batch_ms"])
+    launches = bcmc._lib.load().bcmc_kernel_launches() - launches0
+
+    # every query's vertices against the plain path, on the device
+    allv = eng.vertexBuffer.torch()
+    identical = True
+    nverts = 0
+    for i, (v, iso) in enumerate(qs):
+        n = mcs[v].computeSurface(iso)
+        r = res[i]
+        nverts += n
+        if int(r["num_vertices"]) != n:
+            identical = False
+            continue
+        if n:
+            off = int(r["vertex_offset"])
+            if not torch.equal(mcs[v].vertexBuffer.torch()[:n], allv[off: off + n]):
+                identical = False
+    bm = float(np.median(batch_ms))
+    return {"workload": BATCH["workload"], "queries": len(qs), "vertices": nverts,
+            "plain": {"queries_per_s": len(qs) / plain_s, "p50_ms": float(np.percentile(plain_lat, 50)),
+                      "p99_ms": float(np.percentile(plain_lat, 99))},
+            "batched": {"queries_per_s": len(qs) / (bm / 1000.0), "batch_ms": bm,
+                        "device_ms": float(np.median(dev_ms)), "p50_ms": bm, "p99_ms": float(np.max(batch_ms)),
+                        "gpu_launches_per_batch": launches / reps},
+            "speedup_qps": (len(qs) / (bm / 1000.0)) / (len(qs) / plain_s),
+            "identical_to_plain": identical,
+            "latency_note": "a batch's queries all complete when the batch does: per-query latency = batch wall time"}
+
+
 def algorithmic_bytes(stage: str, st: dict, rate: int, total_blocks: int) -> float:
     """Algorithmic DRAM bytes per launch of each stage's kernel."""
     if stage == "computeVertices":  # k_mc: block data + ids/slots + vertices
@@ -320,6 +414,7 @@ def run_gb300(args):
                  "computeActiveBlocks": "k_active", "cacheUpdate": "k_slots + radix sort"}
 
     decode = decode_bench(ctx, flush) if not args.no_decode else None
+    batched = batched_bench() if not args.no_batched else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -344,6 +439,7 @@ def run_gb300(args):
                                "p99": float(np.percentile(lat, 99)), "queries": len(lat),
                                "what": "host wall time of each computeSurface call (returns the vertex count)"},
                 "decode": decode,
+                "batched": batched,
                 "gpu_launches": int(launches),
                 "clocks": clk,
                 "volume_load_s": load_s,
@@ -361,6 +457,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-decode", action="store_true", help="skip the full-volume decode leg")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-engine leg")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
