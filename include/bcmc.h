@@ -269,6 +269,8 @@ typedef struct bcmc_engine bcmc_engine;
 typedef struct {
     uint64_t pool_slots;       /* decoded-block slots (256 B each); 0 = every block of every volume */
     uint64_t vertex_capacity;  /* initial vertices per batch (grows on demand); 0 = 1<<24 */
+    uint64_t vertex_budget;    /* admission: a launch sequence whose vertex count (known after its
+                                  count pass) exceeds this runs as two halves; 0 = no limit */
     uint32_t max_batch;        /* queries per launch sequence; 0 = 1024 (larger batches are split) */
     uint32_t flags;            /* reserved, 0 */
 } bcmc_engine_opts;
@@ -303,6 +305,51 @@ bcmc_status bcmc_engine_run(bcmc_engine* eng, const bcmc_query* queries, uint32_
 bcmc_status bcmc_engine_vertices(bcmc_engine* eng, const void** d_vertices, uint64_t* count);
 bcmc_status bcmc_engine_copy_vertices(bcmc_engine* eng, uint64_t first, uint64_t count, void* host);
 bcmc_status bcmc_engine_stats_get(bcmc_engine* eng, bcmc_engine_stats* out);
+
+/* ---- Isosurface server ----------------------------------------------------- */
+/* No counterpart in the reference.  A request loop over an engine: a worker
+ * thread takes every request that has arrived (up to max_batch) whenever the
+ * device is free and runs them as one batch, so requests arriving while a
+ * batch runs join the next one (continuous batching).  Each batch is admitted
+ * by the engine's slot pool and vertex budget: a batch that does not fit runs
+ * as smaller sequences.  Every request's vertices are those of the plain path.
+ * While a server exists, only the server uses its engine. */
+typedef struct bcmc_server bcmc_server;
+typedef struct {
+    uint32_t max_batch;    /* requests per batch; 0 = 256 */
+    uint32_t max_wait_us;  /* an under-full batch waits this long for more arrivals; 0 = none */
+} bcmc_server_opts;
+bcmc_status bcmc_server_create(bcmc_engine* eng, const bcmc_server_opts* opts, bcmc_server** out);
+/* Finishes the requests already submitted, then stops the worker. */
+void bcmc_server_destroy(bcmc_server* srv);
+/* Queues one request.  When host_vertices is not NULL the request's vertices
+ * (8 bytes each, at most host_capacity of them) are copied there before the
+ * request completes. */
+bcmc_status bcmc_server_submit(bcmc_server* srv, uint32_t volume, float isovalue, void* host_vertices,
+                               uint64_t host_capacity, uint64_t* ticket);
+/* Blocks until the request completes.  result->vertex_offset is 0 (batch
+ * buffers are reused); latency_ms = completion - submission, wall clock. */
+bcmc_status bcmc_server_wait(bcmc_server* srv, uint64_t ticket, bcmc_query_result* result,
+                             double* latency_ms);
+/* Open-loop load: `requests` arrivals with exponential inter-arrival times at
+ * rate_qps (seeded), each on volume volumes[i] with probability weights[i] and
+ * an isovalue uniform in [iso_lo[i], iso_hi[i]]; reports throughput and
+ * latency percentiles of the completed requests. */
+typedef struct {
+    double rate_qps;
+    uint32_t requests;
+    uint32_t num_volumes;
+    uint64_t seed;
+    const uint32_t* volumes;
+    const float* weights;
+    const float* iso_lo;
+    const float* iso_hi;
+} bcmc_load_spec;
+typedef struct {
+    double offered_qps, achieved_qps, p50_ms, p95_ms, p99_ms, mean_ms, max_ms, mean_batch, duration_s;
+    uint64_t completed, batches, vertices;
+} bcmc_load_report;
+bcmc_status bcmc_server_run_load(bcmc_server* srv, const bcmc_load_spec* spec, bcmc_load_report* out);
 
 #ifdef __cplusplus
 }

@@ -10,6 +10,8 @@ over the CUDA library libbcmc_gb300.so (C ABI: include/bcmc.h):
 * ``RadixSorter``              js/radix_sort_by_key.js
 * ``Engine``                   (no reference counterpart) batched queries over
                                several resident volumes, shared slot pool
+* ``Server``                   (no reference counterpart) continuous-batching
+                               request loop over an Engine
 
 Method names, argument meaning and return values follow the reference.  The
 WebGPU ``device`` argument becomes a CUDA device ordinal or a ``Context``;
@@ -30,7 +32,7 @@ from ._lib import BcmcError, check, dims3, scale3
 
 __all__ = ["Context", "CompressedMarchingCubes", "LRUCache", "ExclusiveScanPipeline", "ExclusiveScanner",
            "StreamCompact", "RadixSorter", "DeviceArray", "BcmcError", "zfp_encode", "zfp_decode_volume",
-           "zfp_block_ranges", "block_active", "stream_words", "Engine"]
+           "zfp_block_ranges", "block_active", "stream_words", "Engine", "Server"]
 
 
 def _torch():
@@ -525,9 +527,10 @@ class Engine:
     vertices equal what CompressedMarchingCubes.computeSurface returns for it
     on its volume, bit for bit."""
 
-    def __init__(self, device=0, pool_slots: int = 0, vertex_capacity: int = 0, max_batch: int = 0):
+    def __init__(self, device=0, pool_slots: int = 0, vertex_capacity: int = 0, max_batch: int = 0,
+                 vertex_budget: int = 0):
         self.ctx = _ctx(device)
-        o = _lib.bcmc_engine_opts(int(pool_slots), int(vertex_capacity), int(max_batch), 0)
+        o = _lib.bcmc_engine_opts(int(pool_slots), int(vertex_capacity), int(vertex_budget), int(max_batch), 0)
         h = C.c_void_p()
         check(_lib.load().bcmc_engine_create(self.ctx.handle, C.byref(o), C.byref(h)), self.ctx.handle)
         self._h = h
@@ -587,3 +590,55 @@ class Engine:
         st = _lib.bcmc_engine_stats()
         check(_lib.load().bcmc_engine_stats_get(self._h, C.byref(st)), self.ctx.handle)
         return {k: getattr(st, k) for k, _ in _lib.bcmc_engine_stats._fields_}
+
+
+class Server:
+    """Continuous-batching isosurface server over an Engine (bcmc_server_*).
+    While it exists only the server uses the engine."""
+
+    def __init__(self, engine: Engine, max_batch: int = 0, max_wait_us: int = 0):
+        self.engine = engine
+        o = _lib.bcmc_server_opts(int(max_batch), int(max_wait_us))
+        h = C.c_void_p()
+        check(_lib.load().bcmc_server_create(engine._h, C.byref(o), C.byref(h)), engine.ctx.handle)
+        self._h = h
+        self._bufs = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().bcmc_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def submit(self, volume: int, isovalue: float, max_vertices: int = 0) -> int:
+        """Queues a request; with max_vertices > 0 its vertices are copied to
+        a host array returned by wait()."""
+        t = C.c_uint64()
+        buf = np.empty((max_vertices, 2), dtype=np.uint32) if max_vertices else None
+        ptr = buf.ctypes.data_as(C.c_void_p) if buf is not None else None
+        check(_lib.load().bcmc_server_submit(self._h, int(volume), float(isovalue), ptr, int(max_vertices),
+                                             C.byref(t)), self.engine.ctx.handle)
+        self._bufs[int(t.value)] = buf
+        return int(t.value)
+
+    def wait(self, ticket: int):
+        """(num_vertices, num_active_blocks, latency_ms, vertices or None)."""
+        r = _lib.bcmc_query_result()
+        lat = C.c_double()
+        check(_lib.load().bcmc_server_wait(self._h, int(ticket), C.byref(r), C.byref(lat)), self.engine.ctx.handle)
+        buf = self._bufs.pop(int(ticket), None)
+        n = int(r.num_vertices)
+        return n, int(r.num_active_blocks), float(lat.value), (buf[: min(n, len(buf))] if buf is not None else None)
+
+    def run_load(self, rate_qps: float, requests: int, volumes, weights, iso_lo, iso_hi, seed: int = 0) -> dict:
+        nv = len(volumes)
+        v = (C.c_uint32 * nv)(*[int(x) for x in volumes])
+        w = (C.c_float * nv)(*[float(x) for x in weights])
+        lo = (C.c_float * nv)(*[float(x) for x in iso_lo])
+        hi = (C.c_float * nv)(*[float(x) for x in iso_hi])
+        spec = _lib.bcmc_load_spec(float(rate_qps), int(requests), nv, int(seed), v, w, lo, hi)
+        rep = _lib.bcmc_load_report()
+        check(_lib.load().bcmc_server_run_load(self._h, C.byref(spec), C.byref(rep)), self.engine.ctx.handle)
+        return {k: getattr(rep, k) for k, _ in _lib.bcmc_load_report._fields_}

@@ -55,8 +55,24 @@ class bcmc_lru_view(C.Structure):
 
 
 class bcmc_engine_opts(C.Structure):
-    _fields_ = [("pool_slots", C.c_uint64), ("vertex_capacity", C.c_uint64), ("max_batch", C.c_uint32),
-                ("flags", C.c_uint32)]
+    _fields_ = [("pool_slots", C.c_uint64), ("vertex_capacity", C.c_uint64), ("vertex_budget", C.c_uint64),
+                ("max_batch", C.c_uint32), ("flags", C.c_uint32)]
+
+
+class bcmc_server_opts(C.Structure):
+    _fields_ = [("max_batch", C.c_uint32), ("max_wait_us", C.c_uint32)]
+
+
+class bcmc_load_spec(C.Structure):
+    _fields_ = [("rate_qps", C.c_double), ("requests", C.c_uint32), ("num_volumes", C.c_uint32),
+                ("seed", C.c_uint64), ("volumes", C.POINTER(C.c_uint32)), ("weights", C.POINTER(C.c_float)),
+                ("iso_lo", C.POINTER(C.c_float)), ("iso_hi", C.POINTER(C.c_float))]
+
+
+class bcmc_load_report(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("offered_qps", "achieved_qps", "p50_ms", "p95_ms", "p99_ms", "mean_ms",
+                                           "max_ms", "mean_batch", "duration_s")] + \
+               [(n, C.c_uint64) for n in ("completed", "batches", "vertices")]
 
 
 class bcmc_query(C.Structure):
@@ -113,6 +129,11 @@ SIGNATURES = {
     "bcmc_engine_vertices": (C.c_int, [P, C.POINTER(P), C.POINTER(U64)]),
     "bcmc_engine_copy_vertices": (C.c_int, [P, U64, U64, P]),
     "bcmc_engine_stats_get": (C.c_int, [P, C.POINTER(bcmc_engine_stats)]),
+    "bcmc_server_create": (C.c_int, [P, C.POINTER(bcmc_server_opts), C.POINTER(P)]),
+    "bcmc_server_destroy": (None, [P]),
+    "bcmc_server_submit": (C.c_int, [P, U32, C.c_float, P, U64, C.POINTER(U64)]),
+    "bcmc_server_wait": (C.c_int, [P, U64, C.POINTER(bcmc_query_result), C.POINTER(C.c_double)]),
+    "bcmc_server_run_load": (C.c_int, [P, C.POINTER(bcmc_load_spec), C.POINTER(bcmc_load_report)]),
     "bcmc_compact_ids": (C.c_int, [P, U32, P, P, P, P]),
     "bcmc_select_ids": (C.c_int, [P, U32, P, P, P, P]),
     "bcmc_sort_aligned_size": (U32, [U32]),

@@ -47,6 +47,10 @@ void dev_free(bcmc_ctx* ctx, void* p, size_t bytes);
 void ensure_status(bcmc_ctx* ctx, size_t words);
 void ensure_scratch(bcmc_ctx* ctx, size_t words);
 
+// ---- engine.cu (for server.cu) ------------------------------------------------
+int engine_device(bcmc_engine* e);
+bcmc_ctx* engine_ctx(bcmc_engine* e);
+
 // ---- sort.cu ----------------------------------------------------------------
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 16;

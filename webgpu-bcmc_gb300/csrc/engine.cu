@@ -953,9 +953,13 @@ void eng_run_sequence(bcmc_engine* e, const bcmc_query* queries, uint32_t n, bcm
         }
         if (st.vert_overflow) {
             if (st.num_verts >= (1ull << 32)) throw std::length_error("batch above 2^32 vertices");
+            if (e->opts.vertex_budget && e->vert_used + st.num_verts > e->opts.vertex_budget)
+                throw std::length_error("batch above the vertex budget");
             eng_ensure_verts(e, e->vert_used + st.num_verts);
             continue;  // the re-run finds every block cached: no decode work repeats
         }
+        if (e->opts.vertex_budget && e->vert_used + st.num_verts > e->opts.vertex_budget)
+            throw std::length_error("batch above the vertex budget");
         break;
     }
     for (uint32_t i = 0; i < n; ++i) {
@@ -1202,3 +1206,8 @@ extern "C" bcmc_status bcmc_engine_stats_get(bcmc_engine* e, bcmc_engine_stats* 
         return BCMC_OK;
     });
 }
+
+namespace bcmc {
+int engine_device(bcmc_engine* e) { return e->ctx->device; }
+bcmc_ctx* engine_ctx(bcmc_engine* e) { return e->ctx; }
+}  // namespace bcmc
