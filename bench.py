@@ -297,6 +297,103 @@ def batched_bench(reps: int = 5) -> dict:
             "latency_note": "a batch's queries all complete when the batch does: per-query latency = batch wall time"}
 
 
+SERVED = dict(workload="c5: 1024x1024x1080 uint16-range value noise (~60% background blocks, 17,694,720 blocks) "
+                       "+ 256^3 value noise, 320^3 blobs, 384^3 spectral, 512^3 value noise; ZFP rate 4; Poisson "
+                       "arrivals, volume weighted by size, isovalue uniform in its range; 40 GB slot pool",
+              big=(1024, 1024, 1080),
+              others=[("ct_like", (256, 256, 256)), ("blobs", (320, 320, 320)), ("turbulence", (384, 384, 384)),
+                      ("ct_like", (512, 512, 512))],
+              rate=4, pool_bytes=40 << 30, seed=5, rates=(100.0, 200.0, 300.0, 400.0, 500.0, 600.0), seconds=2.5)
+
+
+def served_bench() -> dict:
+    """The continuous-batching server on the served mix against the plain
+    per-query path: plain = one query at a time, back to back; served = open-loop
+    Poisson arrivals at swept rates.  Throughput and latency percentiles."""
+    import torch
+
+    import bcmc
+    from bcmc import datasets as D
+
+    rate = SERVED["rate"]
+    ctx = bcmc.Context(0)
+    vols = []  # (dims, host stream, lo, hi)
+    big = D.ct_uint16_torch(SERVED["big"], SERVED["seed"])
+    w = bcmc.zfp_encode(ctx, big, rate)
+    torch.cuda.synchronize()
+    lo, hi = float(big.min()), float(big.max())
+    del big
+    nb = int(np.prod([(d + 3) // 4 for d in SERVED["big"]]))
+    vols.append((SERVED["big"], w.cpu().numpy().view(np.uint8)[: nb * 64 * rate // 8].copy(), lo, hi))
+    del w
+    torch.cuda.empty_cache()
+    for i, (kind, dims) in enumerate(SERVED["others"]):
+        f = D.make_field(kind, dims, SERVED["seed"] + 1 + i)
+        w = bcmc.zfp_encode(ctx, torch.from_numpy(f).cuda(), rate)
+        torch.cuda.synchronize()
+        nb = int(np.prod([(d + 3) // 4 for d in dims]))
+        vols.append((dims, w.cpu().numpy().view(np.uint8)[: nb * 64 * rate // 8].copy(), float(f.min()),
+                     float(f.max())))
+        del f, w
+    sizes = [float(np.prod(d)) for d, _, _, _ in vols]
+    weights = [x / sum(sizes) for x in sizes]
+    iso_lo = [lo + 0.05 * (hi - lo) for _, _, lo, hi in vols]
+    iso_hi = [hi - 0.05 * (hi - lo) for _, _, lo, hi in vols]
+    rng = np.random.default_rng(SERVED["seed"])
+
+    def draw(n):
+        ks = rng.choice(len(vols), size=n, p=weights)
+        return [(int(k), float(np.float32(rng.uniform(iso_lo[k], iso_hi[k])))) for k in ks]
+
+    # plain per-query path, back to back (closed loop)
+    mcs = []
+    for dims, st, _, _ in vols:
+        mc = bcmc.CompressedMarchingCubes(ctx)
+        mc.setCompressedVolume(st, rate, dims)
+        mcs.append(mc)
+    for v, iso in draw(40):  # warm-up: caches grow
+        mcs[v].computeSurface(iso)
+    plain_q = draw(100)
+    lat = []
+    t0 = time.perf_counter()
+    for v, iso in plain_q:
+        tq = time.perf_counter()
+        mcs[v].computeSurface(iso)
+        lat.append(1000.0 * (time.perf_counter() - tq))
+    plain_qps = len(plain_q) / (time.perf_counter() - t0)
+    del mcs
+    torch.cuda.empty_cache()
+
+    eng = bcmc.Engine(ctx, pool_slots=SERVED["pool_bytes"] // 256, max_batch=256, vertex_budget=1 << 31)
+    for dims, st, _, _ in vols:
+        eng.addVolume(st, rate, dims)
+    warm = draw(64)
+    while warm:  # warm-up: first decodes, graphs, buffer growth
+        _, m = eng.run_admit(warm)
+        warm = warm[m:]
+    srv = bcmc.Server(eng, max_batch=256)
+    sweeps = []
+    try:
+        for r in SERVED["rates"]:
+            n = max(50, int(r * SERVED["seconds"]))
+            rep = srv.run_load(r, n, list(range(len(vols))), weights, iso_lo, iso_hi, seed=int(r))
+            sweeps.append({k: rep[k] for k in ("offered_qps", "achieved_qps", "p50_ms", "p95_ms", "p99_ms",
+                                                "mean_batch", "completed")})
+    finally:
+        srv.close()
+    st = eng.stats()
+    p99_plain = float(np.percentile(lat, 99))
+    ok = [s for s in sweeps if s["p99_ms"] <= p99_plain and s["achieved_qps"] >= 0.95 * s["offered_qps"]]
+    best = max(ok, key=lambda s: s["achieved_qps"]) if ok else None
+    return {"workload": SERVED["workload"],
+            "plain": {"queries_per_s": plain_qps, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": p99_plain},
+            "served": sweeps,
+            "best_served_qps_at_plain_p99": best["achieved_qps"] if best else None,
+            "ratio_vs_plain_at_equal_p99": (best["achieved_qps"] / plain_qps) if best else None,
+            "pool": {"slots": st["pool_slots"], "used": st["pool_used"], "decoded_blocks": st["decoded_blocks"],
+                     "evicted_blocks": st["evicted_blocks"]}}
+
+
 def algorithmic_bytes(stage: str, st: dict, rate: int, total_blocks: int) -> float:
     """Algorithmic DRAM bytes per launch of each stage's kernel."""
     if stage == "computeVertices":  # k_mc: block data + ids/slots + vertices
@@ -415,6 +512,7 @@ def run_gb300(args):
 
     decode = decode_bench(ctx, flush) if not args.no_decode else None
     batched = batched_bench() if not args.no_batched else None
+    served = served_bench() if not args.no_served else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -440,6 +538,7 @@ def run_gb300(args):
                                "what": "host wall time of each computeSurface call (returns the vertex count)"},
                 "decode": decode,
                 "batched": batched,
+                "served": served,
                 "gpu_launches": int(launches),
                 "clocks": clk,
                 "volume_load_s": load_s,
@@ -458,6 +557,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-decode", action="store_true", help="skip the full-volume decode leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-engine leg")
+    ap.add_argument("--no-served", action="store_true", help="skip the served (continuous batching) leg")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -300,6 +300,13 @@ bcmc_status bcmc_engine_add_volume(bcmc_engine* eng, const uint8_t* zfp, size_t 
  * in the batch vertex buffer (valid until the next run on this engine). */
 bcmc_status bcmc_engine_run(bcmc_engine* eng, const bcmc_query* queries, uint32_t n,
                             bcmc_query_result* results);
+/* Admission by memory: runs the longest prefix of queries[0..n) that the slot
+ * pool and the vertex budget hold (at least queries[0], else
+ * BCMC_E_ADMISSION) and sets *admitted to its length; the caller resubmits the
+ * rest.  Vertex counts come from the count pass, before any vertex of a
+ * refused query is kept. */
+bcmc_status bcmc_engine_run_admit(bcmc_engine* eng, const bcmc_query* queries, uint32_t n,
+                                  bcmc_query_result* results, uint32_t* admitted);
 /* The batch vertex buffer of the last run: 8 bytes per vertex, laid out as the
  * plain path's (packed 10:10:10 position, block id). */
 bcmc_status bcmc_engine_vertices(bcmc_engine* eng, const void** d_vertices, uint64_t* count);

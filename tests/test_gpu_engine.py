@@ -125,3 +125,21 @@ def test_empty_and_out_of_range_queries(ctx, volumes):
     assert int(res[1]["num_vertices"]) == 0
     with pytest.raises(bcmc.BcmcError):
         eng.run([(99, 0.5)])
+
+
+def test_vertex_budget_admits_a_prefix(ctx, volumes):
+    """run_admit runs the longest prefix of the batch whose vertices (known from
+    the count pass) fit the budget; the rest is left to the caller."""
+    qs = _queries(volumes, 12, seed=8)
+    want = _plain(ctx, volumes, qs)
+    counts = [w[0] for w in want]
+    budget = sum(counts[:5]) + 1  # the first 5 fit, the 6th does not
+    assert counts[5] > 1
+    eng = _engine(ctx, volumes, vertex_budget=budget, max_batch=16)
+    res, m = eng.run_admit(qs)
+    assert m == 5
+    _check(eng, res, want[:m])
+    # the remainder in the next run
+    res2, m2 = eng.run_admit(qs[m:])
+    assert m2 >= 1
+    _check(eng, res2, want[m: m + m2])

@@ -567,6 +567,23 @@ class Engine:
             out[i] = (res[i].vertex_offset, res[i].num_vertices, res[i].num_active_blocks)
         return out
 
+    def run_admit(self, queries):
+        """Runs the longest prefix of `queries` that the slot pool and the
+        vertex budget admit; returns (results of that prefix, its length)."""
+        n = len(queries)
+        qs = (_lib.bcmc_query * max(n, 1))()
+        for i, (v, iso) in enumerate(queries):
+            qs[i].volume = int(v)
+            qs[i].isovalue = float(iso)
+        res = (_lib.bcmc_query_result * max(n, 1))()
+        adm = C.c_uint32()
+        check(_lib.load().bcmc_engine_run_admit(self._h, qs, n, res, C.byref(adm)), self.ctx.handle)
+        m = int(adm.value)
+        out = np.zeros(m, dtype=[("vertex_offset", "<u8"), ("num_vertices", "<u4"), ("num_active_blocks", "<u4")])
+        for i in range(m):
+            out[i] = (res[i].vertex_offset, res[i].num_vertices, res[i].num_active_blocks)
+        return out, m
+
     @property
     def vertexBuffer(self) -> DeviceArray:
         p = C.c_void_p()

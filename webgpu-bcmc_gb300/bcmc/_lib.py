@@ -126,6 +126,7 @@ SIGNATURES = {
     "bcmc_engine_destroy": (None, [P]),
     "bcmc_engine_add_volume": (C.c_int, [P, P, C.c_size_t, U32, U32P, U32P]),
     "bcmc_engine_run": (C.c_int, [P, C.POINTER(bcmc_query), U32, C.POINTER(bcmc_query_result)]),
+    "bcmc_engine_run_admit": (C.c_int, [P, C.POINTER(bcmc_query), U32, C.POINTER(bcmc_query_result), U32P]),
     "bcmc_engine_vertices": (C.c_int, [P, C.POINTER(P), C.POINTER(U64)]),
     "bcmc_engine_copy_vertices": (C.c_int, [P, U64, U64, P]),
     "bcmc_engine_stats_get": (C.c_int, [P, C.POINTER(bcmc_engine_stats)]),

@@ -127,6 +127,45 @@ def turbulence(dims=(512, 512, 512), seed: int = 3) -> np.ndarray:
     return (2.0 * (f - lo) / max(hi - lo, 1e-12) - 1.0).astype(np.float32)
 
 
+def ct_uint16_torch(dims, seed: int = 5, background: float = 0.60, hi: float = 4095.0, device="cuda"):
+    """ct_uint16 generated on the GPU (torch), for volumes too large for the
+    numpy path (the served 1024x1024x1080 volume): same construction --
+    smoothstep value noise (spacing 48, two octaves), the threshold below which
+    `background` of the 4^3 blocks lie, values 0-4095 -- as a float32 CUDA
+    tensor [z, y, x]."""
+    import torch
+
+    X, Y, Z = (int(d) for d in dims)
+    rng = np.random.default_rng(seed)
+    out = torch.zeros((Z, Y, X), dtype=torch.float32, device=device)
+    total_w = 0.0
+    for rel, weight in ((1.0, 1.0), (0.25, 0.35)):
+        sp = 48.0 * rel
+        g = [int(np.ceil(n / sp)) + 2 for n in (Z, Y, X)]
+        lattice = torch.from_numpy(rng.random(g, dtype=np.float64).astype(np.float32)).to(device)
+        wz, wy, wx = (torch.from_numpy(_interp_matrix(n, gn, sp).astype(np.float32)).to(device)
+                      for n, gn in zip((Z, Y, X), g))
+        f = torch.einsum("yj,kji->kyi", wy, lattice)          # [gz, Y, gx]
+        f = torch.einsum("xi,kyi->kyx", wx, f)               # [gz, Y, X]
+        for z0 in range(0, Z, 64):                           # [Z, Y, X] in slabs
+            out[z0: z0 + 64] += weight * torch.einsum("zk,kyx->zyx", wz[z0: z0 + 64], f)
+        total_w += weight
+    out /= total_w
+    lo, hi_v = float(out.min()), float(out.max())
+    out -= lo
+    out /= max(hi_v - lo, 1e-12)
+    pz, py, px = (-Z) % 4, (-Y) % 4, (-X) % 4
+    bm = torch.nn.functional.pad(out[None, None], (0, px, 0, py, 0, pz), mode="replicate")[0, 0]
+    bm = bm.reshape(bm.shape[0] // 4, 4, bm.shape[1] // 4, 4, bm.shape[2] // 4, 4).amax(dim=(1, 3, 5)).reshape(-1)
+    k = max(1, int(round(background * bm.numel())))
+    t = float(torch.kthvalue(bm.cpu(), k).values)
+    del bm
+    v = torch.clamp((out - t) / max(1.0 - t, 1e-6), 0.0, 1.0) * hi
+    v = torch.where(out >= t, torch.round(v), torch.zeros_like(v))
+    del out
+    return v
+
+
 def random_walk(n: int, seed: int, step: float = 0.02, start: float = 0.0,
                 lo: float = -1.0, hi: float = 1.0) -> np.ndarray:
     """Isovalues following a seeded +-step random walk from ``start``."""

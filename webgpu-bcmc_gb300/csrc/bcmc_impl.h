@@ -49,6 +49,7 @@ void ensure_scratch(bcmc_ctx* ctx, size_t words);
 
 // ---- engine.cu (for server.cu) ------------------------------------------------
 int engine_device(bcmc_engine* e);
+uint64_t engine_vertex_budget(bcmc_engine* e);
 bcmc_ctx* engine_ctx(bcmc_engine* e);
 
 // ---- sort.cu ----------------------------------------------------------------

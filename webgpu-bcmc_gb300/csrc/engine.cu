@@ -313,18 +313,18 @@ __global__ void __launch_bounds__(128) k_bdecode(BatchArgs a)
 __global__ void __launch_bounds__(kBmcThreads, kBmcPerSm) k_bmc(BatchArgs a)
 {
     __shared__ float s_vol[kBmcBlocks][128];
-    __shared__ int8_t s_tri[256][16];
-    __shared__ uint8_t s_cnt[256];
-    __shared__ uint8_t s_edge[12];
+    __shared__ __align__(16) uint8_t s_te[256][16];
+    __shared__ __align__(16) uint8_t s_cnt[256];
     __shared__ __align__(16) uint8_t s_case[kBmcCells];
     __shared__ uint32_t s_off[kBmcCells + 1];
     __shared__ uint32_t s_id[kBmcBlocks];
     __shared__ uint32_t s_qi[kBmcBlocks];
     __shared__ float s_iso[kBmcBlocks];
+    __shared__ uint32_t s_idx[kBmcBlocks];
     __shared__ uint32_t s_slot[kBmcBlocks][8];
     __shared__ uint32_t s_act[kBmcBlocks];
     __shared__ uint32_t s_warp[kBmcThreads / 32 + 1];
-    __shared__ uint32_t s_any, s_pv, s_cta_v, s_rank;
+    __shared__ uint32_t s_n, s_pv, s_cta_v, s_rank, s_cursor;
     __shared__ uint16_t s_ghost[64];
     __shared__ uint8_t s_nb_off[8];
 
@@ -333,6 +333,7 @@ __global__ void __launch_bounds__(kBmcThreads, kBmcPerSm) k_bmc(BatchArgs a)
     if (A == 0 || st->entry_overflow || st->pool_exhausted) return;
     const uint32_t epoch = st->epoch;
     const uint64_t cap = st->vert_capacity, vbase = st->vert_base;
+    const uint32_t slots = a.pool->capacity;
     const uint32_t t = threadIdx.x;
     const uint32_t G = gridDim.x;
     if (t == 0) s_rank = atomicAdd(&st->tiles_mc, 1u);
@@ -340,204 +341,255 @@ __global__ void __launch_bounds__(kBmcThreads, kBmcPerSm) k_bmc(BatchArgs a)
     const uint32_t rank = s_rank;
     const uint32_t range = div_up(div_up(A, G), kBmcBlocks) * kBmcBlocks;
     const uint32_t start = min(A, rank * range), end = min(A, start + range);
-    {
-        const uint4* src = reinterpret_cast<const uint4*>(&kTriEdges[0][0]);
-        uint4* dst = reinterpret_cast<uint4*>(&s_tri[0][0]);
-        for (uint32_t i = t; i < 256; i += kBmcThreads) dst[i] = src[i];
-        for (uint32_t i = t; i < 256; i += kBmcThreads) {
-            uint32_t n = 0;
-            while (n < 16 && kTriEdges[i][n] != -1) ++n;
-            s_cnt[i] = (uint8_t)n;
-        }
-        if (t < 12) s_edge[t] = (uint8_t)(c_corner[c_edge[t][0]] | (c_corner[c_edge[t][1]] << 3));
-        if (t == 0) s_cta_v = 0;
-        if (t < 61) s_ghost[t] = c_ghost[t];
-        if (t < 7) s_nb_off[t] = c_nb_off[t];
+    reinterpret_cast<uint4*>(&s_te[0][0])[t] = reinterpret_cast<const uint4*>(&c_tri.corners[0][0])[t];
+    if (t < 16) reinterpret_cast<uint4*>(s_cnt)[t] = reinterpret_cast<const uint4*>(c_tri.count)[t];
+    if (t == 0) {
+        s_cta_v = 0;
+        s_cursor = start;
     }
+    if (t < 61) s_ghost[t] = c_ghost[t];
+    if (t < 7) s_nb_off[t] = c_nb_off[t];
     const uint32_t j = t >> 4, u = t & 15u, ry = u & 3u, rz = u >> 2;
-    uint64_t pv = 0;
+    const uint32_t lane = t & 31u;
 
-    for (int pass = 0; pass < 2; ++pass) {
-        if (pass == 1) {
-            __syncthreads();
-            if (t < 32) {
-                const uint32_t p = warp_lookback(a.status_v, rank, s_cta_v, epoch, &st->error, 61u);
-                if (t == 0) s_pv = p;
-            }
-            __syncthreads();
-            // 32-bit prefix: a batch over 2^32 vertices wraps here; k_bfinish
-            // detects it from the 64-bit per-query totals and the host splits
-            pv = vbase + s_pv;
-            if (pv + s_cta_v > cap) {
-                if (t == 0) atomicOr(&st->vert_overflow, 1u);
-                break;
-            }
-        }
-        for (uint32_t base = start; base < end; base += kBmcBlocks) {
-            __syncthreads();
-            if (t == 0) s_any = 0;
-            __syncthreads();
-            if (t < kBmcBlocks) {
-                const uint32_t idx = base + t;
-                uint32_t id = 0xffffffffu, qi = 0;
-                if (idx < end && (pass == 0 || a.block_counts[idx] != 0u)) {
-                    id = __ldg(a.ent_id + idx);
-                    qi = __ldg(a.ent_q + idx);
-                }
-                s_id[t] = id;
-                s_qi[t] = qi;
-                s_iso[t] = __ldg(&a.queries[qi].iso);
-                if (id != 0xffffffffu) s_any = 1;
-            }
-            __syncthreads();
-            if (!s_any) continue;
-            if (t < kBmcBlocks * 8) {
-                const uint32_t jb = t >> 3, k = t & 7u, id = s_id[jb];
-                uint32_t slot = 0xffffffffu, act = 0;
-                if (id != 0xffffffffu) {
-                    const EngQuery* Q = a.queries + s_qi[jb];
-                    const EngVolDev& V = a.vols[__ldg(&Q->vol)];
-                    const uint3 nb = V.grid.nb;
-                    const uint3 bc = block_coords(id, V.grid);
-                    if (k == kNbSelf) {
-                        slot = (uint32_t)__ldg(V.item_slots + id);
-                        act = (bc.x + 1 < nb.x ? 0x100u : 0u) | (bc.y + 1 < nb.y ? 0x200u : 0u) |
-                              (bc.z + 1 < nb.z ? 0x400u : 0u);
-                    } else {
-                        const uint32_t o = s_nb_off[k], ox = o & 1u, oy = (o >> 1) & 1u, oz = o >> 2;
-                        if (bc.x + ox < nb.x && bc.y + oy < nb.y && bc.z + oz < nb.z) {
-                            const uint32_t nid = id + ox + nb.x * (oy + nb.y * oz);
-                            const uint32_t w = __ldg(a.bitmap + __ldg(&Q->bit0) + (nid >> 5));
-                            act = (w >> (nid & 31u)) & 1u;
-                            slot = (uint32_t)__ldg(V.item_slots + nid);
-                        }
-                    }
-                }
-                s_slot[jb][k] = slot;
-                const uint32_t bits = __ballot_sync(0xffffffffu, (act & 1u) != 0u);
-                if (k == kNbSelf) s_act[jb] = ((bits >> (t & 24u)) & 0x7fu) | act;
-            }
-            __syncthreads();
-            const uint32_t id = s_id[j];
-            const bool valid = id != 0xffffffffu;
-            const float iso = s_iso[j];
-            uint32_t dims = 0;
-            if (valid) {
-                const uint32_t act = s_act[j];
-                dims = block_dims_with_ghost(act, (act & 0x100u) != 0u, (act & 0x200u) != 0u, (act & 0x400u) != 0u);
-                const uint32_t slot = s_slot[j][kNbSelf];
-                const uint32_t slots = a.pool->capacity;
-                float4 v4 = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (slot < slots) v4 = __ldg(reinterpret_cast<const float4*>(a.cache + (uint64_t)slot * 64u) + u);
-                else atomicCAS(&st->error, 0u, 62u);
-                const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
-                float gv[4];
-                uint32_t gaddr[4];
-#pragma unroll
-                for (uint32_t r = 0; r < 4; ++r) {
-                    const uint32_t gi = u + 16u * r;
-                    gv[r] = 0.0f;
-                    gaddr[r] = 0xffffffffu;
-                    if (gi < 61) {
-                        const uint32_t g = s_ghost[gi];
-                        const uint32_t gx = g & 15u, gy = (g >> 4) & 15u, gz = (g >> 8) & 15u;
-                        if (gx < dx && gy < dy && gz < dz) {
-                            const uint32_t nslot = s_slot[j][g >> 12];
-                            if (nslot < slots) {
-                                gv[r] = __ldg(a.cache + (uint64_t)nslot * 64u + (gx & 3u) + 4u * ((gy & 3u) + 4u * (gz & 3u)));
-                                gaddr[r] = gx + 5u * (gy + 5u * gz);
-                            } else {
-                                atomicCAS(&st->error, 0u, 63u);
-                            }
-                        }
-                    }
-                }
-                float* row = &s_vol[j][5u * (ry + 5u * rz)];
-                row[0] = v4.x;
-                row[1] = v4.y;
-                row[2] = v4.z;
-                row[3] = v4.w;
-#pragma unroll
-                for (uint32_t r = 0; r < 4; ++r)
-                    if (gaddr[r] != 0xffffffffu) s_vol[j][gaddr[r]] = gv[r];
-            }
-            __syncthreads();
-            uint32_t nv[4], cs4 = 0, mysum = 0;
-            {
-                const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
-                const bool row_ok = valid && ry + 1 < dy && rz + 1 < dz;
-#pragma unroll
-                for (uint32_t x = 0; x < 4; ++x) {
-                    uint32_t cs = 0;
-                    nv[x] = 0;
-                    if (row_ok && x + 1 < dx) {
-                        const float* v = &s_vol[j][x + 5u * (ry + 5u * rz)];
-                        cs = (v[0] <= iso ? 1u : 0u) | (v[1] <= iso ? 2u : 0u) | (v[6] <= iso ? 4u : 0u) |
-                             (v[5] <= iso ? 8u : 0u) | (v[25] <= iso ? 16u : 0u) | (v[26] <= iso ? 32u : 0u) |
-                             (v[31] <= iso ? 64u : 0u) | (v[30] <= iso ? 128u : 0u);
-                        nv[x] = s_cnt[cs];
-                    }
-                    cs4 |= cs << (8u * x);
-                    mysum += nv[x];
-                }
-            }
-            uint32_t tile_v;
-            uint32_t run = cta_exclusive_scan<kBmcThreads>(mysum, s_warp, &tile_v);
-            if (pass == 0) {
-                uint32_t bsum = mysum;
-#pragma unroll
-                for (int o = 8; o; o >>= 1) bsum += __shfl_xor_sync(0xffffffffu, bsum, o);
-                if (u == 0 && valid) {
-                    a.block_counts[base + j] = bsum;
-                    if (bsum) atomicAdd(a.q_nverts + s_qi[j], bsum);
-                }
-                if (t == 0) s_cta_v += tile_v;
-                continue;
-            }
-            *reinterpret_cast<uint32_t*>(&s_case[4u * t]) = cs4;
-#pragma unroll
-            for (uint32_t x = 0; x < 4; ++x) {
-                s_off[4u * t + x] = run;
-                run += nv[x];
-            }
-            if (t == 0) s_off[kBmcCells] = tile_v;
-            __syncthreads();
-            uint2* out = a.verts + pv;
-            for (uint32_t k = t; k < tile_v; k += kBmcThreads) {
-                uint32_t cell = 0;
-#pragma unroll
-                for (uint32_t step = kBmcCells / 2; step; step >>= 1)
-                    if (s_off[cell + step] <= k) cell += step;
-                const uint32_t tt_idx = k - s_off[cell];
-                const uint32_t ed = s_edge[(uint32_t)s_tri[s_case[cell]][tt_idx]];
-                const uint32_t jb = cell >> 6, cc = cell & 63u;
-                const float biso = s_iso[jb];
-                const uint32_t x = cc & 3u, y = (cc >> 2) & 3u, z = cc >> 4;
-                const uint32_t o0 = ed & 7u, o1 = ed >> 3;
-                const uint32_t ax = o0 & 1u, ay = (o0 >> 1) & 1u, az = o0 >> 2;
-                const uint32_t bx = o1 & 1u, by = (o1 >> 1) & 1u, bz = o1 >> 2;
-                const float fa = s_vol[jb][(x + ax) + 5u * ((y + ay) + 5u * (z + az))];
-                const float fb = s_vol[jb][(x + bx) + 5u * ((y + by) + 5u * (z + bz))];
-                float tt = 0.0f;
-                if (!(fabsf(__fsub_rn(fa, fb)) < 0.001f)) tt = __fdiv_rn(__fsub_rn(biso, fa), __fsub_rn(fb, fa));
-                uint32_t qx, qy, qz;
-                if (isfinite(tt)) {
-                    const uint32_t d = (o0 ^ o1) >> 1;
-                    const uint32_t ad = (o0 >> d) & 1u, vd = d == 0 ? x : (d == 1 ? y : z);
-                    const float pd = __fadd_rn(__fadd_rn(ad ? __fsub_rn(1.0f, tt) : tt, (float)vd), 0.5f);
-                    const uint32_t qd = quantize(pd);
-                    qx = d == 0 ? qd : (((ax + x) * 1023u) >> 2);
-                    qy = d == 1 ? qd : (((ay + y) * 1023u) >> 2);
-                    qz = d == 2 ? qd : (((az + z) * 1023u) >> 2);
+    auto load_tile = [&]() -> uint32_t {
+        if (t < kBmcBlocks * 8) {
+            const uint32_t jb = t >> 3, k = t & 7u, id = s_id[jb];
+            uint32_t slot = 0xffffffffu, act = 0;
+            if (id != 0xffffffffu) {
+                const EngQuery* Q = a.queries + s_qi[jb];
+                const EngVolDev& V = a.vols[__ldg(&Q->vol)];
+                const uint3 nb = V.grid.nb;
+                const uint3 bc = block_coords(id, V.grid);
+                const uint32_t bx = bc.x, by = bc.y, bz = bc.z;
+                if (k == kNbSelf) {
+                    slot = (uint32_t)__ldg(V.item_slots + id);
+                    act = (bx + 1 < nb.x ? 0x100u : 0u) | (by + 1 < nb.y ? 0x200u : 0u) |
+                          (bz + 1 < nb.z ? 0x400u : 0u);
                 } else {
-                    qx = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)ax, __fmul_rn(tt, (float)((int)bx - (int)ax))), (float)x), 0.5f));
-                    qy = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)ay, __fmul_rn(tt, (float)((int)by - (int)ay))), (float)y), 0.5f));
-                    qz = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)az, __fmul_rn(tt, (float)((int)bz - (int)az))), (float)z), 0.5f));
+                    const uint32_t o = s_nb_off[k], ox = o & 1u, oy = (o >> 1) & 1u, oz = o >> 2;
+                    if (bx + ox < nb.x && by + oy < nb.y && bz + oz < nb.z) {
+                        const uint32_t nid = id + ox + nb.x * (oy + nb.y * oz);
+                        const uint32_t w = __ldg(a.bitmap + __ldg(&Q->bit0) + (nid >> 5));
+                        act = (w >> (nid & 31u)) & 1u;
+                        slot = (uint32_t)__ldg(V.item_slots + nid);
+                    }
                 }
-                out[k] = make_uint2((qx << 20) | (qy << 10) | qz, s_id[jb]);
             }
-            pv += tile_v;
+            s_slot[jb][k] = slot;
+            const uint32_t bits = __ballot_sync(0xffffffffu, (act & 1u) != 0u);
+            if (k == kNbSelf) s_act[jb] = ((bits >> (t & 24u)) & 0x7fu) | act;
         }
+        __syncthreads();
+        const uint32_t id = s_id[j];
+        uint32_t dims = 0;
+        if (id != 0xffffffffu) {
+            const uint32_t act = s_act[j];
+            dims = block_dims_with_ghost(act, (act & 0x100u) != 0u, (act & 0x200u) != 0u, (act & 0x400u) != 0u);
+            const uint32_t slot = s_slot[j][kNbSelf];
+            float4 v4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (slot < slots) v4 = __ldg(reinterpret_cast<const float4*>(a.cache + (uint64_t)slot * 64u) + u);
+            else atomicCAS(&st->error, 0u, 62u);
+            const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
+            float gv[4];
+            uint32_t gaddr[4];
+#pragma unroll
+            for (uint32_t r = 0; r < 4; ++r) {
+                const uint32_t gi = u + 16u * r;
+                gv[r] = 0.0f;
+                gaddr[r] = 0xffffffffu;
+                if (gi < 61) {
+                    const uint32_t g = s_ghost[gi];
+                    const uint32_t gx = g & 15u, gy = (g >> 4) & 15u, gz = (g >> 8) & 15u;
+                    if (gx < dx && gy < dy && gz < dz) {
+                        const uint32_t nslot = s_slot[j][g >> 12];
+                        if (nslot < slots) {
+                            gv[r] = __ldg(a.cache + (uint64_t)nslot * 64u + (gx & 3u) + 4u * ((gy & 3u) + 4u * (gz & 3u)));
+                            gaddr[r] = gx + 5u * (gy + 5u * gz);
+                        } else {
+                            atomicCAS(&st->error, 0u, 63u);
+                        }
+                    }
+                }
+            }
+            float* row = &s_vol[j][5u * (ry + 5u * rz)];
+            row[0] = v4.x;
+            row[1] = v4.y;
+            row[2] = v4.z;
+            row[3] = v4.w;
+#pragma unroll
+            for (uint32_t r = 0; r < 4; ++r)
+                if (gaddr[r] != 0xffffffffu) s_vol[j][gaddr[r]] = gv[r];
+        }
+        __syncthreads();
+        return dims;
+    };
+    // cases and counts of cells 4u..4u+3 (compute_block_has_vertices.comp:28-51):
+    // the 4 corner rows (y, z), (y+1, z), (y, z+1), (y+1, z+1) are tested once each
+    auto count_cells = [&](uint32_t dims, uint32_t nv[4], uint32_t& cs4) -> uint32_t {
+        const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
+        const bool row_ok = s_id[j] != 0xffffffffu && ry + 1 < dy && rz + 1 < dz;
+        const float iso = s_iso[j];
+        uint32_t rm[4];
+#pragma unroll
+        for (uint32_t r = 0; r < 4; ++r) {
+            const float* p = &s_vol[j][5u * ((ry + (r & 1u)) + 5u * (rz + (r >> 1)))];
+            uint32_t m = 0;
+#pragma unroll
+            for (uint32_t x = 0; x < 5; ++x) m |= (p[x] <= iso ? 1u : 0u) << x;
+            rm[r] = m;
+        }
+        uint32_t sum = 0;
+        cs4 = 0;
+#pragma unroll
+        for (uint32_t x = 0; x < 4; ++x) {
+            uint32_t cs = 0;
+            nv[x] = 0;
+            if (row_ok && x + 1 < dx) {
+                const uint32_t a0 = rm[0] >> x, a1 = rm[1] >> x, a2 = rm[2] >> x, a3 = rm[3] >> x;
+                cs = (a0 & 3u) | ((a1 & 2u) << 1) | ((a1 & 1u) << 3) | ((a2 & 3u) << 4) | ((a3 & 2u) << 5) |
+                     ((a3 & 1u) << 7);
+                nv[x] = s_cnt[cs];
+            }
+            cs4 |= cs << (8u * x);
+            sum += nv[x];
+        }
+        return sum;
+    };
+
+    // ---- count pass
+    for (uint32_t base = start; base < end; base += kBmcBlocks) {
+        __syncthreads();
+        if (t < kBmcBlocks) {
+            const uint32_t idx = base + t;
+            uint32_t id = 0xffffffffu, qi = 0;
+            if (idx < end) {
+                id = __ldg(a.ent_id + idx);
+                qi = __ldg(a.ent_q + idx);
+            }
+            s_id[t] = id;
+            s_qi[t] = qi;
+            s_iso[t] = __ldg(&a.queries[qi].iso);
+        }
+        __syncthreads();
+        const uint32_t dims = load_tile();
+        uint32_t nv[4], cs4;
+        uint32_t bsum = count_cells(dims, nv, cs4);
+#pragma unroll
+        for (int o = 8; o; o >>= 1) bsum += __shfl_xor_sync(0xffffffffu, bsum, o);
+        if (u == 0 && s_id[j] != 0xffffffffu) {
+            a.block_counts[base + j] = bsum;
+            if (bsum) {
+                atomicAdd(&s_cta_v, bsum);
+                atomicAdd(a.q_nverts + s_qi[j], bsum);
+            }
+        }
+    }
+    __syncthreads();
+    if (t < 32) {
+        const uint32_t p = warp_lookback(a.status_v, rank, s_cta_v, epoch, &st->error, 61u);
+        if (t == 0) s_pv = p;
+    }
+    __syncthreads();
+    // 32-bit prefix: a sequence over 2^32 vertices wraps here; k_bfinish
+    // detects it from the 64-bit per-query totals and the host splits
+    uint64_t pv = vbase + s_pv;
+    if (pv + s_cta_v > cap) {
+        if (t == 0) atomicOr(&st->vert_overflow, 1u);
+        return;
+    }
+    // ---- emit pass over tiles of the next 16 blocks that have vertices
+    for (;;) {
+        __syncthreads();
+        if (t < 32) {
+            uint32_t cur = s_cursor, filled = 0;
+            while (filled < kBmcBlocks && cur < end) {
+                const uint32_t i = cur + lane;
+                const uint32_t c = i < end ? a.block_counts[i] : 0u;
+                const uint32_t m = __ballot_sync(0xffffffffu, c != 0u);
+                const uint32_t nz = __popc(m), take = min(nz, kBmcBlocks - filled);
+                const uint32_t r = __popc(m & ((1u << lane) - 1u));
+                if (c != 0u && r < take) s_idx[filled + r] = i;
+                if (take < nz) {
+                    uint32_t mm = m;
+                    for (uint32_t k = 0; k < take; ++k) mm &= mm - 1u;
+                    cur += (uint32_t)__ffs(mm) - 1u;
+                } else {
+                    cur += 32u;
+                }
+                filled += take;
+            }
+            __syncwarp();
+            if (lane < kBmcBlocks) {
+                uint32_t id = 0xffffffffu, qi = 0;
+                if (lane < filled) {
+                    id = __ldg(a.ent_id + s_idx[lane]);
+                    qi = __ldg(a.ent_q + s_idx[lane]);
+                }
+                s_id[lane] = id;
+                s_qi[lane] = qi;
+                s_iso[lane] = __ldg(&a.queries[qi].iso);
+            }
+            if (lane == 0) {
+                s_n = filled;
+                s_cursor = min(cur, end);
+            }
+        }
+        __syncthreads();
+        const uint32_t n_sel = s_n;
+        if (n_sel == 0) break;
+        const uint32_t dims = load_tile();
+        uint32_t nv[4], cs4;
+        const uint32_t mysum = count_cells(dims, nv, cs4);
+        uint32_t tile_v;
+        uint32_t run = cta_exclusive_scan<kBmcThreads>(mysum, s_warp, &tile_v);
+        *reinterpret_cast<uint32_t*>(&s_case[4u * t]) = cs4;
+#pragma unroll
+        for (uint32_t x = 0; x < 4; ++x) {
+            s_off[4u * t + x] = run;
+            run += nv[x];
+        }
+        if (t == 0) s_off[kBmcCells] = tile_v;
+        __syncthreads();
+        uint2* out = a.verts + pv;
+        for (uint32_t k = t; k < tile_v; k += kBmcThreads) {
+            uint32_t cell = 0;
+#pragma unroll
+            for (uint32_t step = kBmcCells / 2; step; step >>= 1)
+                if (s_off[cell + step] <= k) cell += step;
+            const uint32_t ed = s_te[s_case[cell]][k - s_off[cell]];
+            const uint32_t jb = cell >> 6, cc = cell & 63u;
+            const uint32_t x = cc & 3u, y = (cc >> 2) & 3u, z = cc >> 4;
+            const uint32_t o0 = ed & 7u, o1 = ed >> 3;
+            const uint32_t ax = o0 & 1u, ay = (o0 >> 1) & 1u, az = o0 >> 2;
+            const uint32_t bx = o1 & 1u, by = (o1 >> 1) & 1u, bz = o1 >> 2;
+            const float iso = s_iso[jb];
+            const float fa = s_vol[jb][(x + ax) + 5u * ((y + ay) + 5u * (z + az))];
+            const float fb = s_vol[jb][(x + bx) + 5u * ((y + by) + 5u * (z + bz))];
+            // lerp_verts (compute_block_vertices.comp:62-74)
+            float tt = 0.0f;
+            if (!(fabsf(__fsub_rn(fa, fb)) < 0.001f)) tt = __fdiv_rn(__fsub_rn(iso, fa), __fsub_rn(fb, fa));
+            uint32_t qx, qy, qz;
+            if (isfinite(tt)) {
+                // edges are axis aligned: along the two fixed axes
+                // a + tt*0 + v + 0.5 is exactly a + v + 0.5, which
+                // quantizes to floor((a + v) * 255.75); only the edge's
+                // own axis needs the f32 arithmetic
+                const uint32_t d = (o0 ^ o1) >> 1;  // 0, 1, 2 = x, y, z
+                const uint32_t ad = (o0 >> d) & 1u, vd = d == 0 ? x : (d == 1 ? y : z);
+                const float pd = __fadd_rn(__fadd_rn(ad ? __fsub_rn(1.0f, tt) : tt, (float)vd), 0.5f);
+                const uint32_t qd = quantize(pd);
+                qx = d == 0 ? qd : (((ax + x) * 1023u) >> 2);
+                qy = d == 1 ? qd : (((ay + y) * 1023u) >> 2);
+                qz = d == 2 ? qd : (((az + z) * 1023u) >> 2);
+            } else {
+                qx = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)ax, __fmul_rn(tt, (float)((int)bx - (int)ax))), (float)x), 0.5f));
+                qy = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)ay, __fmul_rn(tt, (float)((int)by - (int)ay))), (float)y), 0.5f));
+                qz = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)az, __fmul_rn(tt, (float)((int)bz - (int)az))), (float)z), 0.5f));
+            }
+            out[k] = make_uint2((qx << 20) | (qy << 10) | qz, s_id[jb]);
+        }
+        pv += tile_v;
     }
 }
 
@@ -818,7 +870,8 @@ void eng_ensure_verts(bcmc_engine* e, uint64_t need)
 {
     if (need <= e->vert_cap) return;
     BCMC_CUDA(cudaStreamSynchronize(e->stream));
-    const uint64_t n = std::max<uint64_t>(need + need / 2, 1u << 20);
+    uint64_t n = std::max<uint64_t>(need + need / 2, 1u << 20);
+    if (e->opts.vertex_budget) n = std::max<uint64_t>(need, std::min<uint64_t>(n, e->opts.vertex_budget));
     // keep the vertices already written by earlier sequences of this run
     uint2* nv = (uint2*)dev_alloc(e->ctx, n * sizeof(uint2));
     if (e->vert_used)
@@ -884,6 +937,13 @@ uint32_t bucket_of(uint32_t n)
     while (b < n) b <<= 1;
     return b;
 }
+
+// Refusal of a launch sequence by the vertex budget: only its first `fit`
+// queries fit (their counts are known from the count pass).
+struct AdmitPrefix : std::length_error {
+    uint32_t fit;
+    explicit AdmitPrefix(uint32_t f) : std::length_error("batch above the vertex budget"), fit(f) {}
+};
 
 // Runs queries[0..n) (n <= max_batch) as one launch sequence; results go to out.
 // Throws std::length_error when the pool cannot hold the sequence's active blocks.
@@ -951,15 +1011,23 @@ void eng_run_sequence(bcmc_engine* e, const bcmc_query* queries, uint32_t n, bcm
             if (ev == 0) throw std::length_error("the slot pool cannot hold one batch's active blocks");
             continue;
         }
-        if (st.vert_overflow) {
-            if (st.num_verts >= (1ull << 32)) throw std::length_error("batch above 2^32 vertices");
-            if (e->opts.vertex_budget && e->vert_used + st.num_verts > e->opts.vertex_budget)
-                throw std::length_error("batch above the vertex budget");
-            eng_ensure_verts(e, e->vert_used + st.num_verts);
+        // vertex admission from the count pass: per-query totals are complete
+        // even when the emit pass was refused for lack of room
+        const uint64_t limit_seq = std::min<uint64_t>(
+            (1ull << 32) - 1, e->opts.vertex_budget ? e->opts.vertex_budget - std::min(e->opts.vertex_budget, e->vert_used)
+                                                    : ~0ull);
+        if (st.vert_overflow || st.num_verts > limit_seq) {
+            uint64_t cum = 0;
+            uint32_t fit = 0;
+            for (; fit < n; ++fit) {
+                const uint64_t v = e->h_results[fit].nverts;
+                if (cum + v > limit_seq) break;
+                cum += v;
+            }
+            if (fit < n) throw AdmitPrefix(fit);
+            eng_ensure_verts(e, e->vert_used + cum);
             continue;  // the re-run finds every block cached: no decode work repeats
         }
-        if (e->opts.vertex_budget && e->vert_used + st.num_verts > e->opts.vertex_budget)
-            throw std::length_error("batch above the vertex budget");
         break;
     }
     for (uint32_t i = 0; i < n; ++i) {
@@ -1089,7 +1157,9 @@ extern "C" bcmc_status bcmc_engine_create(bcmc_ctx* ctx, const bcmc_engine_opts*
         e->q_nverts = (uint32_t*)dev_alloc(ctx, e->max_batch * 4);
         e->d_pool = (EngPool*)dev_alloc(ctx, sizeof(EngPool));
         e->d_evicted = (unsigned long long*)dev_alloc(ctx, 8);
-        eng_ensure_verts(e, e->opts.vertex_capacity ? e->opts.vertex_capacity : (1ull << 24));
+        // with a vertex budget the buffer is sized for it once, up front
+        eng_ensure_verts(e, e->opts.vertex_budget ? e->opts.vertex_budget
+                                                  : (e->opts.vertex_capacity ? e->opts.vertex_capacity : (1ull << 24)));
         eng_ensure_status(e, 1024);
         eng_ensure_batch(e, 1u << 16, 1u << 16);
         BCMC_CUDA(cudaStreamSynchronize(e->stream));
@@ -1169,6 +1239,57 @@ extern "C" bcmc_status bcmc_engine_run(bcmc_engine* e, const bcmc_query* queries
     });
 }
 
+namespace {
+// Runs the longest prefix of queries[0..n) that the slot pool and the vertex
+// budget admit (halving on refusal); returns its length.  Throws
+// std::length_error when not even queries[0] alone fits.
+uint32_t eng_run_prefix(bcmc_engine* e, const bcmc_query* queries, uint32_t n, bcmc_query_result* out)
+{
+    try {
+        eng_run_sequence(e, queries, n, out);
+        return n;
+    } catch (const AdmitPrefix& x) {  // the count pass says how many fit
+        if (x.fit == 0) throw;
+        return eng_run_prefix(e, queries, x.fit, out);
+    } catch (const std::length_error&) {  // the slot pool: halve
+        if (n < 2) throw;
+        return eng_run_prefix(e, queries, n / 2, out);
+    }
+}
+}  // namespace
+
+extern "C" bcmc_status bcmc_engine_run_admit(bcmc_engine* e, const bcmc_query* queries, uint32_t n,
+                                             bcmc_query_result* results, uint32_t* admitted)
+{
+    if (!e || !admitted || (n && (!queries || !results))) return BCMC_E_ARG;
+    if (e->vols.empty()) return BCMC_E_STATE;
+    *admitted = 0;
+    return eng_guarded(e, [&]() -> bcmc_status {
+        if (!e->pool_slots) {
+            uint64_t all = 0;
+            for (auto& v : e->vols) all += v.total;
+            eng_alloc_pool(e, e->opts.pool_slots ? e->opts.pool_slots : all);
+        }
+        e->vert_used = 0;
+        uint32_t done = 0;
+        while (done < n) {
+            const uint32_t m = std::min(e->max_batch, n - done);
+            uint32_t got;
+            try {
+                got = eng_run_prefix(e, queries + done, m, results + done);
+            } catch (const std::length_error&) {
+                if (done) break;  // the rest waits for the next run
+                throw;
+            }
+            done += got;
+            if (got < m) break;
+        }
+        *admitted = done;
+        ++e->stats.batches;
+        return BCMC_OK;
+    });
+}
+
 extern "C" bcmc_status bcmc_engine_vertices(bcmc_engine* e, const void** d_vertices, uint64_t* count)
 {
     if (!e || !d_vertices || !count) return BCMC_E_ARG;
@@ -1209,5 +1330,6 @@ extern "C" bcmc_status bcmc_engine_stats_get(bcmc_engine* e, bcmc_engine_stats* 
 
 namespace bcmc {
 int engine_device(bcmc_engine* e) { return e->ctx->device; }
+uint64_t engine_vertex_budget(bcmc_engine* e) { return e->opts.vertex_budget; }
 bcmc_ctx* engine_ctx(bcmc_engine* e) { return e->ctx; }
 }  // namespace bcmc

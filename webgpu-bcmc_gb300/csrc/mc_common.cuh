@@ -7,15 +7,40 @@
 
 namespace bcmc {
 
-#define BCMC_TABLE_QUALIFIER static __constant__
+namespace mc_detail {
+#define BCMC_TABLE_QUALIFIER constexpr
 #include "mc_tables.inc"
 #undef BCMC_TABLE_QUALIFIER
-
 // corner i of a cell (compute_vertex_values.comp:48-57), packed x|y<<1|z<<2
-static __constant__ uint8_t c_corner[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+constexpr uint8_t kCorner[8] = {0, 1, 3, 2, 4, 5, 7, 6};
 // cube edge -> its two corners (compute_block_vertices.comp:10-23)
-static __constant__ uint8_t c_edge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {6, 5},
-                                      {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+constexpr uint8_t kEdge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {6, 5},
+                                  {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+
+// The case table as the kernels use it: each entry's edge as the packed
+// corner pair o0 | o1 << 3 (0xff past the case's last entry), and each
+// case's vertex count -- derived at compile time from the table above.
+struct TriCorners {
+    uint8_t corners[256][16];
+    uint8_t count[256];
+};
+constexpr TriCorners make_tri_corners()
+{
+    TriCorners t{};
+    for (int c = 0; c < 256; ++c) {
+        int n = 0;
+        for (int k = 0; k < 16; ++k) {
+            const int e = kTriEdges[c][k];
+            t.corners[c][k] = e < 0 ? (uint8_t)0xff : (uint8_t)(kCorner[kEdge[e][0]] | (kCorner[kEdge[e][1]] << 3));
+            if (e >= 0 && n == k) ++n;
+        }
+        t.count[c] = (uint8_t)n;
+    }
+    return t;
+}
+}  // namespace mc_detail
+
+static __constant__ __align__(16) mc_detail::TriCorners c_tri = mc_detail::make_tri_corners();
 
 // Ghost voxels of a block's 5^3 grid (some coordinate == 4): x|y<<4|z<<8 and,
 // in bits 12-14, which +x/+y/+z neighbour holds them (kNb* order below).

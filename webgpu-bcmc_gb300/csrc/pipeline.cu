@@ -280,36 +280,37 @@ constexpr int kMcThreads = 256;
 constexpr int kMcCells = 64 * kMcBlocks;  // 4 consecutive cells per thread
 
 // Marching cubes over the active blocks.  Each CTA owns one contiguous range of
-// active blocks (whole 16-block tiles) and makes two passes over it:
-//   count pass: per tile, one parallel round of loads fetches the active flags
-//     and cache slots of every block's 7 +x/+y/+z neighbours and its own slot,
-//     a second round fills each block's 5^3 grid in shared memory (16 B vector
-//     loads of 4 voxels per thread, ghost voxels alongside); one thread per 4
-//     cells finds the case and vertex count; block totals are kept for the
-//     emit pass and summed for the CTA;
+// active blocks and makes two passes over it:
+//   count pass: per 16-block tile, one parallel round of loads fetches the
+//     active flags and cache slots of every block's 7 +x/+y/+z neighbours and
+//     its own slot, a second round fills each block's 5^3 grid in shared
+//     memory (16 B loads of 4 voxels per thread, ghost voxels alongside); a
+//     thread tests its 4 corner rows once and derives the cases and vertex
+//     counts of its 4 cells; block totals are kept for the emit pass;
 //   one warp-cooperative decoupled look-back per CTA turns the CTA totals into
 //     its global vertex offset and its offset in the blocks-with-vertices list;
-//   emit pass: tiles are reloaded (from L2), blocks without vertices skipped;
-//     a CTA scan gives each cell's offset and the vertices are spread over the
-//     CTA -- thread k takes vertex k of the tile, finds its cell by binary
-//     search -- so lanes stay converged and stores are contiguous.
-// A CTA walks back once per launch, not once per tile, so the look-back never
-// waits on a wave of unfinished tiles.  Output order = the reference's:
-// active-block order, cell order, table order.
+//   emit pass: tiles of the next 16 blocks that have vertices (blocks without
+//     are skipped by a warp ballot over the counts), reloaded (from L2); a CTA
+//     scan gives each cell's offset and the vertices are spread over the CTA
+//     -- thread k takes vertex k of the tile, finds its cell by binary search,
+//     its edge in the precomputed corner-pair table -- so lanes stay converged
+//     and stores are contiguous.
+// A CTA walks back once per launch, not once per tile.  Output order = the
+// reference's: active-block order, cell order, table order.
 __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
 {
     __shared__ float s_vol[kMcBlocks][128];
-    __shared__ int8_t s_tri[256][16];
-    __shared__ uint8_t s_cnt[256];
-    __shared__ uint8_t s_edge[12];  // corner offsets of each edge: o0 | o1 << 3
-    __shared__ __align__(16) uint8_t s_case[kMcCells];  // written 4 cases per 32-bit store
+    __shared__ __align__(16) uint8_t s_te[256][16];
+    __shared__ __align__(16) uint8_t s_cnt[256];
+    __shared__ __align__(16) uint8_t s_case[kMcCells];
     __shared__ uint32_t s_off[kMcCells + 1];
     __shared__ uint32_t s_id[kMcBlocks];
+    __shared__ uint32_t s_idx[kMcBlocks];
     __shared__ uint32_t s_slot[kMcBlocks][8];
     __shared__ uint32_t s_act[kMcBlocks];
     __shared__ uint32_t s_warp[kMcThreads / 32 + 1];
-    __shared__ uint32_t s_any, s_pv, s_pb, s_cta_v, s_cta_b, s_rank;
-    __shared__ uint16_t s_ghost[64];  // per-lane table reads: shared, not __constant__ memory
+    __shared__ uint32_t s_n, s_pv, s_pb, s_cta_v, s_cta_b, s_rank, s_cursor;
+    __shared__ uint16_t s_ghost[64];
     __shared__ uint8_t s_nb_off[8];
 
     const uint32_t A = q->num_active;
@@ -321,231 +322,252 @@ __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
     const uint3 nb = a.nb;
     const uint32_t t = threadIdx.x;
     const uint32_t G = gridDim.x;
-    // the CTA's place in the look-back order comes from a counter, not from
-    // blockIdx: a CTA then only waits on ranges claimed by CTAs already running
     if (t == 0) s_rank = atomicAdd(&q->tiles_mc, 1u);
     __syncthreads();
     const uint32_t rank = s_rank;
     const uint32_t range = div_up(div_up(A, G), kMcBlocks) * kMcBlocks;
     const uint32_t start = min(A, rank * range), end = min(A, start + range);
-    {
-        const uint4* src = reinterpret_cast<const uint4*>(&kTriEdges[0][0]);
-        uint4* dst = reinterpret_cast<uint4*>(&s_tri[0][0]);
-        for (uint32_t i = t; i < 256; i += kMcThreads) dst[i] = src[i];
-        for (uint32_t i = t; i < 256; i += kMcThreads) {
-            uint32_t n = 0;
-            while (n < 16 && kTriEdges[i][n] != -1) ++n;
-            s_cnt[i] = (uint8_t)n;
-        }
-        if (t < 12) s_edge[t] = (uint8_t)(c_corner[c_edge[t][0]] | (c_corner[c_edge[t][1]] << 3));
-        if (t == 0) s_cta_v = s_cta_b = 0;
-        if (t < 61) s_ghost[t] = c_ghost[t];
-        if (t < 7) s_nb_off[t] = c_nb_off[t];
+    reinterpret_cast<uint4*>(&s_te[0][0])[t] = reinterpret_cast<const uint4*>(&c_tri.corners[0][0])[t];
+    if (t < 16) reinterpret_cast<uint4*>(s_cnt)[t] = reinterpret_cast<const uint4*>(c_tri.count)[t];
+    if (t == 0) {
+        s_cta_v = s_cta_b = 0;
+        s_cursor = start;
     }
-    // thread -> (block j, cells 4u..4u+3 = the x-row (y, z) = (u & 3, u >> 2))
+    if (t < 61) s_ghost[t] = c_ghost[t];
+    if (t < 7) s_nb_off[t] = c_nb_off[t];
     const uint32_t j = t >> 4, u = t & 15u, ry = u & 3u, rz = u >> 2;
-    uint32_t pv = 0, pb = 0;
+    const uint32_t lane = t & 31u;
 
-    for (int pass = 0; pass < 2; ++pass) {
-        if (pass == 1) {
-            __syncthreads();
-            if (t < 64) {  // warp 0: vertex offset, warp 1: offset among blocks with vertices
-                if (t < 32) {
-                    const uint32_t p = warp_lookback(a.status_v, rank, s_cta_v, epoch, &q->error, 40u);
-                    if (t == 0) {
-                        s_pv = p;
-                        if (rank == G - 1) q->num_verts = p + s_cta_v;
-                    }
+    auto load_tile = [&]() -> uint32_t {
+        if (t < kMcBlocks * 8) {
+            const uint32_t jb = t >> 3, k = t & 7u, id = s_id[jb];
+            uint32_t slot = 0xffffffffu, act = 0;
+            if (id != 0xffffffffu) {
+                const uint3 bc = block_coords(id, a.grid);
+                const uint32_t bx = bc.x, by = bc.y, bz = bc.z;
+                if (k == kNbSelf) {
+                    slot = (uint32_t)__ldg(a.item_slots + id);
+                    act = (bx + 1 < nb.x ? 0x100u : 0u) | (by + 1 < nb.y ? 0x200u : 0u) |
+                          (bz + 1 < nb.z ? 0x400u : 0u);
                 } else {
-                    const uint32_t p = warp_lookback(a.status_b, rank, s_cta_b, epoch, &q->error, 41u);
-                    if (t == 32) {
-                        s_pb = p;
-                        if (rank == G - 1) q->num_with_verts = p + s_cta_b;
+                    const uint32_t o = s_nb_off[k], ox = o & 1u, oy = (o >> 1) & 1u, oz = o >> 2;
+                    if (bx + ox < nb.x && by + oy < nb.y && bz + oz < nb.z) {
+                        const uint32_t nid = id + ox + nb.x * (oy + nb.y * oz);
+                        act = __ldg(a.active + nid) != 0u ? 1u : 0u;
+                        slot = (uint32_t)__ldg(a.item_slots + nid);
                     }
                 }
             }
-            __syncthreads();
-            pv = s_pv;
-            pb = s_pb;
-            if ((uint64_t)pv + s_cta_v > cap) {  // host grows the vertex buffer and re-runs
-                if (t == 0) atomicOr(&q->vert_overflow, 1u);
-                break;
-            }
+            s_slot[jb][k] = slot;
+            const uint32_t bits = __ballot_sync(0xffffffffu, (act & 1u) != 0u);
+            if (k == kNbSelf) s_act[jb] = ((bits >> (t & 24u)) & 0x7fu) | act;
         }
-        for (uint32_t base = start; base < end; base += kMcBlocks) {
-            __syncthreads();
-            if (t == 0) s_any = 0;
-            __syncthreads();
-            if (t < kMcBlocks) {
-                const uint32_t idx = base + t;
-                uint32_t id = 0xffffffffu;
-                if (idx < end && (pass == 0 || a.block_counts[idx] != 0u)) id = __ldg(a.active_ids + idx);
-                s_id[t] = id;
-                if (id != 0xffffffffu) s_any = 1;
-            }
-            __syncthreads();
-            if (!s_any) continue;  // emit pass: no block of this tile has vertices
-            // neighbour flags and slots: thread (block t >> 3, entry t & 7)
-            if (t < kMcBlocks * 8) {
-                const uint32_t jb = t >> 3, k = t & 7u, id = s_id[jb];
-                uint32_t slot = 0xffffffffu, act = 0;
-                if (id != 0xffffffffu) {
-                    const uint3 bc = block_coords(id, a.grid);
-                    const uint32_t bx = bc.x, by = bc.y, bz = bc.z;
-                    if (k == kNbSelf) {
-                        slot = (uint32_t)__ldg(a.item_slots + id);
-                        // which +x/+y/+z neighbours exist (bits 8-10 of s_act)
-                        act = (bx + 1 < nb.x ? 0x100u : 0u) | (by + 1 < nb.y ? 0x200u : 0u) |
-                              (bz + 1 < nb.z ? 0x400u : 0u);
-                    } else {
-                        const uint32_t o = s_nb_off[k], ox = o & 1u, oy = (o >> 1) & 1u, oz = o >> 2;
-                        if (bx + ox < nb.x && by + oy < nb.y && bz + oz < nb.z) {
-                            const uint32_t nid = id + ox + nb.x * (oy + nb.y * oz);
-                            act = __ldg(a.active + nid) != 0u ? 1u : 0u;
-                            slot = (uint32_t)__ldg(a.item_slots + nid);
+        __syncthreads();
+        const uint32_t id = s_id[j];
+        uint32_t dims = 0;
+        if (id != 0xffffffffu) {
+            const uint32_t act = s_act[j];
+            dims = block_dims_with_ghost(act, (act & 0x100u) != 0u, (act & 0x200u) != 0u, (act & 0x400u) != 0u);
+            const uint32_t slot = s_slot[j][kNbSelf];
+            float4 v4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (slot < slots) v4 = __ldg(reinterpret_cast<const float4*>(a.cache + (uint64_t)slot * 64u) + u);
+            else atomicCAS(&q->error, 0u, 51u);
+            const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
+            float gv[4];
+            uint32_t gaddr[4];
+#pragma unroll
+            for (uint32_t r = 0; r < 4; ++r) {
+                const uint32_t gi = u + 16u * r;
+                gv[r] = 0.0f;
+                gaddr[r] = 0xffffffffu;
+                if (gi < 61) {
+                    const uint32_t g = s_ghost[gi];
+                    const uint32_t gx = g & 15u, gy = (g >> 4) & 15u, gz = (g >> 8) & 15u;
+                    if (gx < dx && gy < dy && gz < dz) {
+                        const uint32_t nslot = s_slot[j][g >> 12];
+                        if (nslot < slots) {
+                            gv[r] = __ldg(a.cache + (uint64_t)nslot * 64u + (gx & 3u) + 4u * ((gy & 3u) + 4u * (gz & 3u)));
+                            gaddr[r] = gx + 5u * (gy + 5u * gz);
+                        } else {
+                            atomicCAS(&q->error, 0u, 52u);
                         }
                     }
                 }
-                s_slot[jb][k] = slot;
-                const uint32_t bits = __ballot_sync(0xffffffffu, (act & 1u) != 0u);  // 4 blocks per warp
-                if (k == kNbSelf) s_act[jb] = ((bits >> (t & 24u)) & 0x7fu) | act;
             }
-            __syncthreads();
-            // grid of each block (+ ghost layer) in shared memory
-            const uint32_t id = s_id[j];
-            const bool valid = id != 0xffffffffu;
-            uint32_t dims = 0;
-            if (valid) {
-                const uint32_t act = s_act[j];
-                dims = block_dims_with_ghost(act, (act & 0x100u) != 0u, (act & 0x200u) != 0u, (act & 0x400u) != 0u);
-                const uint32_t slot = s_slot[j][kNbSelf];
-                float4 v4 = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (slot < slots) v4 = __ldg(reinterpret_cast<const float4*>(a.cache + (uint64_t)slot * 64u) + u);
-                else atomicCAS(&q->error, 0u, 51u);
-                const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
-                float gv[4];
-                uint32_t gaddr[4];
+            float* row = &s_vol[j][5u * (ry + 5u * rz)];
+            row[0] = v4.x;
+            row[1] = v4.y;
+            row[2] = v4.z;
+            row[3] = v4.w;
 #pragma unroll
-                for (uint32_t r = 0; r < 4; ++r) {
-                    const uint32_t gi = u + 16u * r;
-                    gv[r] = 0.0f;
-                    gaddr[r] = 0xffffffffu;
-                    if (gi < 61) {
-                        const uint32_t g = s_ghost[gi];
-                        const uint32_t gx = g & 15u, gy = (g >> 4) & 15u, gz = (g >> 8) & 15u;
-                        if (gx < dx && gy < dy && gz < dz) {
-                            const uint32_t nslot = s_slot[j][g >> 12];
-                            if (nslot < slots) {
-                                gv[r] = __ldg(a.cache + (uint64_t)nslot * 64u + (gx & 3u) + 4u * ((gy & 3u) + 4u * (gz & 3u)));
-                                gaddr[r] = gx + 5u * (gy + 5u * gz);
-                            } else {
-                                atomicCAS(&q->error, 0u, 52u);
-                            }
-                        }
-                    }
-                }
-                float* row = &s_vol[j][5u * (ry + 5u * rz)];
-                row[0] = v4.x;
-                row[1] = v4.y;
-                row[2] = v4.z;
-                row[3] = v4.w;
-#pragma unroll
-                for (uint32_t r = 0; r < 4; ++r)
-                    if (gaddr[r] != 0xffffffffu) s_vol[j][gaddr[r]] = gv[r];
-            }
-            __syncthreads();
-            // cases and counts of cells 4t..4t+3 (compute_block_has_vertices.comp:28-51)
-            uint32_t nv[4], cs4 = 0, mysum = 0;
-            {
-                const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
-                const bool row_ok = valid && ry + 1 < dy && rz + 1 < dz;
-#pragma unroll
-                for (uint32_t x = 0; x < 4; ++x) {
-                    uint32_t cs = 0;
-                    nv[x] = 0;
-                    if (row_ok && x + 1 < dx) {
-                        const float* v = &s_vol[j][x + 5u * (ry + 5u * rz)];
-                        cs = (v[0] <= iso ? 1u : 0u) | (v[1] <= iso ? 2u : 0u) | (v[6] <= iso ? 4u : 0u) |
-                             (v[5] <= iso ? 8u : 0u) | (v[25] <= iso ? 16u : 0u) | (v[26] <= iso ? 32u : 0u) |
-                             (v[31] <= iso ? 64u : 0u) | (v[30] <= iso ? 128u : 0u);
-                        nv[x] = s_cnt[cs];
-                    }
-                    cs4 |= cs << (8u * x);
-                    mysum += nv[x];
-                }
-            }
-            uint32_t tile_v;
-            uint32_t run = cta_exclusive_scan<kMcThreads>(mysum, s_warp, &tile_v);
-            if (pass == 0) {
-                // block total = sum over its 16 threads (a half warp)
-                uint32_t bsum = mysum;
-#pragma unroll
-                for (int o = 8; o; o >>= 1) bsum += __shfl_xor_sync(0xffffffffu, bsum, o);
-                if (u == 0 && valid) {
-                    a.block_counts[base + j] = bsum;
-                    if (bsum) atomicAdd(&s_cta_b, 1u);
-                }
-                if (t == 0) s_cta_v += tile_v;
-                continue;
-            }
-            *reinterpret_cast<uint32_t*>(&s_case[4u * t]) = cs4;
-#pragma unroll
-            for (uint32_t x = 0; x < 4; ++x) {
-                s_off[4u * t + x] = run;
-                run += nv[x];
-            }
-            if (t == 0) s_off[kMcCells] = tile_v;
-            __syncthreads();
-            if (t < kMcBlocks && s_off[64 * (t + 1)] > s_off[64 * t]) {
-                uint32_t rank = 0;
-                for (uint32_t k = 0; k < t; ++k) rank += s_off[64 * (k + 1)] > s_off[64 * k] ? 1u : 0u;
-                a.with_verts[pb + rank] = base + t;
-                a.vert_offsets[pb + rank] = pv + s_off[64 * t];
-            }
-            uint2* out = a.verts + pv;
-            for (uint32_t k = t; k < tile_v; k += kMcThreads) {
-                uint32_t cell = 0;
-#pragma unroll
-                for (uint32_t step = kMcCells / 2; step; step >>= 1)
-                    if (s_off[cell + step] <= k) cell += step;
-                const uint32_t tt_idx = k - s_off[cell];
-                const uint32_t ed = s_edge[(uint32_t)s_tri[s_case[cell]][tt_idx]];
-                const uint32_t jb = cell >> 6, cc = cell & 63u;
-                const uint32_t x = cc & 3u, y = (cc >> 2) & 3u, z = cc >> 4;
-                const uint32_t o0 = ed & 7u, o1 = ed >> 3;
-                const uint32_t ax = o0 & 1u, ay = (o0 >> 1) & 1u, az = o0 >> 2;
-                const uint32_t bx = o1 & 1u, by = (o1 >> 1) & 1u, bz = o1 >> 2;
-                const float fa = s_vol[jb][(x + ax) + 5u * ((y + ay) + 5u * (z + az))];
-                const float fb = s_vol[jb][(x + bx) + 5u * ((y + by) + 5u * (z + bz))];
-                // lerp_verts (compute_block_vertices.comp:62-74)
-                float tt = 0.0f;
-                if (!(fabsf(__fsub_rn(fa, fb)) < 0.001f)) tt = __fdiv_rn(__fsub_rn(iso, fa), __fsub_rn(fb, fa));
-                uint32_t qx, qy, qz;
-                if (isfinite(tt)) {
-                    // edges are axis aligned: along the two fixed axes
-                    // a + tt*0 + v + 0.5 is exactly a + v + 0.5, which
-                    // quantizes to floor((a + v) * 255.75); only the edge's
-                    // own axis needs the f32 arithmetic
-                    const uint32_t d = (o0 ^ o1) >> 1;  // 0, 1, 2 = x, y, z
-                    const uint32_t ad = (o0 >> d) & 1u, vd = d == 0 ? x : (d == 1 ? y : z);
-                    const float pd = __fadd_rn(__fadd_rn(ad ? __fsub_rn(1.0f, tt) : tt, (float)vd), 0.5f);
-                    const uint32_t q = quantize(pd);
-                    qx = d == 0 ? q : (((ax + x) * 1023u) >> 2);
-                    qy = d == 1 ? q : (((ay + y) * 1023u) >> 2);
-                    qz = d == 2 ? q : (((az + z) * 1023u) >> 2);
-                } else {
-                    qx = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)ax, __fmul_rn(tt, (float)((int)bx - (int)ax))), (float)x), 0.5f));
-                    qy = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)ay, __fmul_rn(tt, (float)((int)by - (int)ay))), (float)y), 0.5f));
-                    qz = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)az, __fmul_rn(tt, (float)((int)bz - (int)az))), (float)z), 0.5f));
-                }
-                out[k] = make_uint2((qx << 20) | (qy << 10) | qz, s_id[jb]);
-            }
-            uint32_t tile_b = 0;
-#pragma unroll
-            for (int k = 0; k < kMcBlocks; ++k) tile_b += s_off[64 * (k + 1)] > s_off[64 * k] ? 1u : 0u;
-            pv += tile_v;
-            pb += tile_b;
+            for (uint32_t r = 0; r < 4; ++r)
+                if (gaddr[r] != 0xffffffffu) s_vol[j][gaddr[r]] = gv[r];
         }
+        __syncthreads();
+        return dims;
+    };
+    // cases and counts of cells 4u..4u+3 (compute_block_has_vertices.comp:28-51):
+    // the 4 corner rows (y, z), (y+1, z), (y, z+1), (y+1, z+1) are tested once each
+    auto count_cells = [&](uint32_t dims, uint32_t nv[4], uint32_t& cs4) -> uint32_t {
+        const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
+        const bool row_ok = s_id[j] != 0xffffffffu && ry + 1 < dy && rz + 1 < dz;
+        uint32_t rm[4];
+#pragma unroll
+        for (uint32_t r = 0; r < 4; ++r) {
+            const float* p = &s_vol[j][5u * ((ry + (r & 1u)) + 5u * (rz + (r >> 1)))];
+            uint32_t m = 0;
+#pragma unroll
+            for (uint32_t x = 0; x < 5; ++x) m |= (p[x] <= iso ? 1u : 0u) << x;
+            rm[r] = m;
+        }
+        uint32_t sum = 0;
+        cs4 = 0;
+#pragma unroll
+        for (uint32_t x = 0; x < 4; ++x) {
+            uint32_t cs = 0;
+            nv[x] = 0;
+            if (row_ok && x + 1 < dx) {
+                const uint32_t a0 = rm[0] >> x, a1 = rm[1] >> x, a2 = rm[2] >> x, a3 = rm[3] >> x;
+                cs = (a0 & 3u) | ((a1 & 2u) << 1) | ((a1 & 1u) << 3) | ((a2 & 3u) << 4) | ((a3 & 2u) << 5) |
+                     ((a3 & 1u) << 7);
+                nv[x] = s_cnt[cs];
+            }
+            cs4 |= cs << (8u * x);
+            sum += nv[x];
+        }
+        return sum;
+    };
+
+    // ---- count pass
+    for (uint32_t base = start; base < end; base += kMcBlocks) {
+        __syncthreads();
+        if (t < kMcBlocks) {
+            const uint32_t idx = base + t;
+            s_id[t] = idx < end ? __ldg(a.active_ids + idx) : 0xffffffffu;
+        }
+        __syncthreads();
+        const uint32_t dims = load_tile();
+        uint32_t nv[4], cs4;
+        uint32_t bsum = count_cells(dims, nv, cs4);
+#pragma unroll
+        for (int o = 8; o; o >>= 1) bsum += __shfl_xor_sync(0xffffffffu, bsum, o);
+        if (u == 0 && s_id[j] != 0xffffffffu) {
+            a.block_counts[base + j] = bsum;
+            if (bsum) {
+                atomicAdd(&s_cta_v, bsum);
+                atomicAdd(&s_cta_b, 1u);
+            }
+        }
+    }
+    __syncthreads();
+    if (t < 64) {
+        if (t < 32) {
+            const uint32_t p = warp_lookback(a.status_v, rank, s_cta_v, epoch, &q->error, 40u);
+            if (t == 0) {
+                s_pv = p;
+                if (rank == G - 1) q->num_verts = p + s_cta_v;
+            }
+        } else {
+            const uint32_t p = warp_lookback(a.status_b, rank, s_cta_b, epoch, &q->error, 41u);
+            if (t == 32) {
+                s_pb = p;
+                if (rank == G - 1) q->num_with_verts = p + s_cta_b;
+            }
+        }
+    }
+    __syncthreads();
+    uint32_t pv = s_pv, pb = s_pb;
+    if ((uint64_t)pv + s_cta_v > cap) {
+        if (t == 0) atomicOr(&q->vert_overflow, 1u);
+        return;
+    }
+    // ---- emit pass over tiles of the next 16 blocks that have vertices
+    for (;;) {
+        __syncthreads();
+        if (t < 32) {
+            uint32_t cur = s_cursor, filled = 0;
+            while (filled < kMcBlocks && cur < end) {
+                const uint32_t i = cur + lane;
+                const uint32_t c = i < end ? a.block_counts[i] : 0u;
+                const uint32_t m = __ballot_sync(0xffffffffu, c != 0u);
+                const uint32_t nz = __popc(m), take = min(nz, kMcBlocks - filled);
+                const uint32_t r = __popc(m & ((1u << lane) - 1u));
+                if (c != 0u && r < take) s_idx[filled + r] = i;
+                if (take < nz) {
+                    uint32_t mm = m;
+                    for (uint32_t k = 0; k < take; ++k) mm &= mm - 1u;
+                    cur += (uint32_t)__ffs(mm) - 1u;
+                } else {
+                    cur += 32u;
+                }
+                filled += take;
+            }
+            __syncwarp();
+            if (lane < kMcBlocks) s_id[lane] = lane < filled ? __ldg(a.active_ids + s_idx[lane]) : 0xffffffffu;
+            if (lane == 0) {
+                s_n = filled;
+                s_cursor = min(cur, end);
+            }
+        }
+        __syncthreads();
+        const uint32_t n_sel = s_n;
+        if (n_sel == 0) break;
+        const uint32_t dims = load_tile();
+        uint32_t nv[4], cs4;
+        const uint32_t mysum = count_cells(dims, nv, cs4);
+        uint32_t tile_v;
+        uint32_t run = cta_exclusive_scan<kMcThreads>(mysum, s_warp, &tile_v);
+        *reinterpret_cast<uint32_t*>(&s_case[4u * t]) = cs4;
+#pragma unroll
+        for (uint32_t x = 0; x < 4; ++x) {
+            s_off[4u * t + x] = run;
+            run += nv[x];
+        }
+        if (t == 0) s_off[kMcCells] = tile_v;
+        __syncthreads();
+        if (t < n_sel) {
+            a.with_verts[pb + t] = s_idx[t];
+            a.vert_offsets[pb + t] = pv + s_off[64 * t];
+        }
+        uint2* out = a.verts + pv;
+        for (uint32_t k = t; k < tile_v; k += kMcThreads) {
+            uint32_t cell = 0;
+#pragma unroll
+            for (uint32_t step = kMcCells / 2; step; step >>= 1)
+                if (s_off[cell + step] <= k) cell += step;
+            const uint32_t ed = s_te[s_case[cell]][k - s_off[cell]];
+            const uint32_t jb = cell >> 6, cc = cell & 63u;
+            const uint32_t x = cc & 3u, y = (cc >> 2) & 3u, z = cc >> 4;
+            const uint32_t o0 = ed & 7u, o1 = ed >> 3;
+            const uint32_t ax = o0 & 1u, ay = (o0 >> 1) & 1u, az = o0 >> 2;
+            const uint32_t bx = o1 & 1u, by = (o1 >> 1) & 1u, bz = o1 >> 2;
+            const float fa = s_vol[jb][(x + ax) + 5u * ((y + ay) + 5u * (z + az))];
+            const float fb = s_vol[jb][(x + bx) + 5u * ((y + by) + 5u * (z + bz))];
+            // lerp_verts (compute_block_vertices.comp:62-74)
+            float tt = 0.0f;
+            if (!(fabsf(__fsub_rn(fa, fb)) < 0.001f)) tt = __fdiv_rn(__fsub_rn(iso, fa), __fsub_rn(fb, fa));
+            uint32_t qx, qy, qz;
+            if (isfinite(tt)) {
+                // edges are axis aligned: along the two fixed axes
+                // a + tt*0 + v + 0.5 is exactly a + v + 0.5, which
+                // quantizes to floor((a + v) * 255.75); only the edge's
+                // own axis needs the f32 arithmetic
+                const uint32_t d = (o0 ^ o1) >> 1;  // 0, 1, 2 = x, y, z
+                const uint32_t ad = (o0 >> d) & 1u, vd = d == 0 ? x : (d == 1 ? y : z);
+                const float pd = __fadd_rn(__fadd_rn(ad ? __fsub_rn(1.0f, tt) : tt, (float)vd), 0.5f);
+                const uint32_t qd = quantize(pd);
+                qx = d == 0 ? qd : (((ax + x) * 1023u) >> 2);
+                qy = d == 1 ? qd : (((ay + y) * 1023u) >> 2);
+                qz = d == 2 ? qd : (((az + z) * 1023u) >> 2);
+            } else {
+                qx = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)ax, __fmul_rn(tt, (float)((int)bx - (int)ax))), (float)x), 0.5f));
+                qy = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)ay, __fmul_rn(tt, (float)((int)by - (int)ay))), (float)y), 0.5f));
+                qz = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)az, __fmul_rn(tt, (float)((int)bz - (int)az))), (float)z), 0.5f));
+            }
+            out[k] = make_uint2((qx << 20) | (qy << 10) | qz, s_id[jb]);
+        }
+        pv += tile_v;
+        pb += n_sel;
     }
 }
 

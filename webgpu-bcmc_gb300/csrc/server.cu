@@ -5,9 +5,10 @@
 // Whenever the device is free the worker takes every request that has arrived
 // (up to max_batch, after an optional short wait for company) and runs them as
 // one engine batch; requests arriving meanwhile queue for the next batch.
-// Admission by memory happens in the engine: a batch whose active blocks do
-// not fit the slot pool, or whose vertex count (known after the count pass)
-// exceeds the vertex budget, runs as smaller launch sequences.
+// Admission by memory: the engine runs the longest prefix of the batch whose
+// active blocks fit the slot pool and whose vertex count (known after the
+// count pass) fits the vertex budget; the rest goes back to the front of the
+// queue for the next batch.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -54,6 +55,7 @@ struct bcmc_server {
     bool stop = false;
     std::thread worker;
     uint64_t batches = 0, batched_requests = 0;
+    double avg_verts = 0.0;  // worker only
 };
 
 namespace {
@@ -73,14 +75,28 @@ void worker_loop(bcmc_server* s)
                 s->cv_work.wait_for(lk, std::chrono::microseconds(s->opts.max_wait_us),
                                     [&] { return s->stop || s->pending.size() >= s->opts.max_batch; });
             }
-            const size_t n = std::min<size_t>(s->pending.size(), s->opts.max_batch);
+            // size the batch so that its expected vertex count stays within the
+            // engine's vertex budget: an over-full batch would pay a count pass
+            // for requests the engine then refuses
+            size_t cap_n = s->opts.max_batch;
+            const uint64_t budget = bcmc::engine_vertex_budget(s->eng);
+            if (budget && s->avg_verts > 0.0)
+                cap_n = std::max<size_t>(1, std::min<size_t>(cap_n, (size_t)(0.8 * (double)budget / s->avg_verts)));
+            const size_t n = std::min<size_t>(s->pending.size(), cap_n);
             batch.assign(s->pending.begin(), s->pending.begin() + n);
             s->pending.erase(s->pending.begin(), s->pending.begin() + n);
         }
         qs.resize(batch.size());
         res.assign(batch.size(), bcmc_query_result{});
         for (size_t i = 0; i < batch.size(); ++i) qs[i] = bcmc_query{batch[i].volume, batch[i].iso};
-        bcmc_status st = bcmc_engine_run(s->eng, qs.data(), (uint32_t)qs.size(), res.data());
+        uint32_t admitted = 0;
+        bcmc_status st = bcmc_engine_run_admit(s->eng, qs.data(), (uint32_t)qs.size(), res.data(), &admitted);
+        if (st == BCMC_OK && admitted < batch.size()) {
+            // the rest did not fit this batch's memory: back to the front of the queue
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->pending.insert(s->pending.begin(), batch.begin() + admitted, batch.end());
+            batch.resize(admitted);
+        }
         if (st == BCMC_OK) {
             for (size_t i = 0; i < batch.size() && st == BCMC_OK; ++i) {
                 if (!batch[i].host || !res[i].num_vertices) continue;
@@ -93,6 +109,10 @@ void worker_loop(bcmc_server* s)
             std::lock_guard<std::mutex> lk(s->mu);
             ++s->batches;
             s->batched_requests += batch.size();
+            if (st == BCMC_OK)
+                for (size_t i = 0; i < batch.size(); ++i)  // running mean of vertices per request
+                    s->avg_verts = s->avg_verts == 0.0 ? (double)res[i].num_vertices + 1.0
+                                                       : 0.98 * s->avg_verts + 0.02 * (double)res[i].num_vertices;
             for (size_t i = 0; i < batch.size(); ++i) {
                 Done d;
                 d.status = st;
