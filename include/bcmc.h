@@ -249,6 +249,17 @@ uint64_t bcmc_zfp_stream_words(const uint32_t dims[3], uint32_t rate);
 bcmc_status bcmc_zfp_encode(bcmc_ctx* ctx, const float* d_field, const uint32_t dims[3],
                             uint32_t rate, uint64_t* d_words, void* stream);
 
+/* The vertex stage's position math (mc_isosurface.vert:51-60,
+ * block_vertex_position.comp:19-26) for n packed vertices of a volume of
+ * `dims` and voxel `scale` (NULL = 1): d_world receives 3 floats per vertex,
+ * scale * ((4 * block + q * 4 / 1023 + 0.5) / dims - 0.5).  When proj_view
+ * (16 floats, column-major, host memory) and d_clip are given, d_clip receives
+ * proj_view * (world, 1), 4 floats per vertex.  The render pass that consumes
+ * these in the reference is not part of this library. */
+bcmc_status bcmc_unpack_vertices(bcmc_ctx* ctx, const void* d_vertices, uint64_t n, const uint32_t dims[3],
+                                 const float scale[3], float* d_world, const float* proj_view, float* d_clip,
+                                 void* stream);
+
 /* compute_block_active.comp:24-61: u32 active flag per block. */
 bcmc_status bcmc_block_active(bcmc_ctx* ctx, const float* d_ranges, const uint32_t dims[3],
                               float isovalue, uint32_t* d_active, void* stream);

@@ -558,6 +558,37 @@ void bcmc_oracle_block_ranges(const uint64_t* words, const uint32_t dims[3], uin
 }
 
 /* ======================================================================== */
+/* mc_isosurface.vert:51-60 with block_vertex_position.comp:19-26             */
+/* ======================================================================== */
+void bcmc_oracle_unpack_vertices(const uint32_t* verts, uint64_t n, const uint32_t dims[3], const float scale[3],
+                                 const float* proj_view, float* world, float* clip)
+{
+    const uint32_t nbx = align_to(dims[0], 4) / 4, nby = align_to(dims[1], 4) / 4;
+    for (uint64_t i = 0; i < n; ++i) {
+        const uint32_t c = verts[2 * i], id = verts[2 * i + 1];
+        const uint32_t b[3] = {id % nbx, (id / nbx) % nby, id / (nbx * nby)};
+        const float q[3] = {(float)((c & 0x3ff00000u) >> 20), (float)((c & 0x000ffc00u) >> 10),
+                            (float)(c & 0x000003ffu)};
+        float w[3];
+        for (int k = 0; k < 3; ++k) {
+            const float d = (q[k] * 4.0f) / 1023.0f + 0.5f; /* decompress_position */
+            const float wp = 4.0f * (float)b[k] + d;
+            w[k] = (scale ? scale[k] : 1.0f) * (wp / (float)dims[k] - 0.5f);
+            world[3 * i + k] = w[k];
+        }
+        if (proj_view && clip) {
+            for (int r = 0; r < 4; ++r) {
+                float acc = proj_view[r] * w[0];
+                acc = acc + proj_view[4 + r] * w[1];
+                acc = acc + proj_view[8 + r] * w[2];
+                acc = acc + proj_view[12 + r] * 1.0f;
+                clip[4 * i + r] = acc;
+            }
+        }
+    }
+}
+
+/* ======================================================================== */
 /* compute_block_active.comp:24-61                                           */
 /* ======================================================================== */
 void bcmc_oracle_block_active(const float* ranges, const uint32_t dims[3], float iso,

@@ -53,6 +53,10 @@ void bcmc_oracle_decode_volume(const uint64_t* words, uint64_t nblocks, uint32_t
 void bcmc_oracle_block_ranges(const uint64_t* words, const uint32_t dims[3], uint32_t max_bits,
                               float* ranges /* [2*nblocks] */);
 
+/* ---- mc_isosurface.vert:51-60: world (3 floats) and clip (4 floats) ------- */
+void bcmc_oracle_unpack_vertices(const uint32_t* verts, uint64_t n, const uint32_t dims[3], const float scale[3],
+                                 const float* proj_view, float* world, float* clip);
+
 /* ---- compute_block_active.comp:24-61 ------------------------------------- */
 void bcmc_oracle_block_active(const float* ranges, const uint32_t dims[3], float isovalue,
                               uint32_t* active);

@@ -50,6 +50,7 @@ def lib():
         L.bcmc_oracle_decode_volume.argtypes = [u64p, C.c_uint64, C.c_uint32, f32p]
         L.bcmc_oracle_block_ranges.argtypes = [u64p, u32p, C.c_uint32, f32p]
         L.bcmc_oracle_block_active.argtypes = [f32p, u32p, C.c_float, u32p]
+        L.bcmc_oracle_unpack_vertices.argtypes = [u32p, C.c_uint64, u32p, f32p, f32p, f32p, f32p]
         L.bcmc_oracle_exclusive_scan.restype = C.c_uint32
         L.bcmc_oracle_exclusive_scan.argtypes = [u32p, C.c_uint32, C.c_uint32]
         L.bcmc_oracle_compact.argtypes = [u32p, u32p, C.c_uint32, u32p]
@@ -161,6 +162,20 @@ def block_ranges(words: np.ndarray, dims, max_bits: int) -> np.ndarray:
     out = np.zeros(2 * nb, dtype=np.float32)
     lib().bcmc_oracle_block_ranges(_p(words, u64p), _p(_dims(dims), u32p), max_bits, _p(out, f32p))
     return out
+
+
+def unpack_vertices(verts: np.ndarray, dims, scale=(1.0, 1.0, 1.0), proj_view=None):
+    """mc_isosurface.vert:51-60: world positions [n, 3] (and clip [n, 4])."""
+    v = np.ascontiguousarray(verts, dtype=np.uint32).reshape(-1, 2)
+    n = len(v)
+    world = np.zeros((n, 3), np.float32)
+    sc = np.ascontiguousarray(np.asarray(scale, np.float32))
+    clip = np.zeros((n, 4), np.float32) if proj_view is not None else None
+    pv = np.ascontiguousarray(np.asarray(proj_view, np.float32).reshape(16)) if proj_view is not None else None
+    lib().bcmc_oracle_unpack_vertices(_p(v, u32p), n, _p(_dims(dims), u32p), _p(sc, f32p),
+                                      _p(pv, f32p) if pv is not None else None, _p(world, f32p),
+                                      _p(clip, f32p) if clip is not None else None)
+    return (world, clip) if clip is not None else world
 
 
 def block_active(ranges: np.ndarray, dims, iso: float) -> np.ndarray:

@@ -33,6 +33,7 @@ _SIGS = {
     "ref_block_has_vertices": [P, F32, P, P, P, P, U32, P],
     "ref_block_num_verts": [P, F32, P, P, P, P, P, U32, P],
     "ref_block_vertices": [P, F32, P, P, P, P, P, U32, P],
+    "ref_unpack_vertices": [P, C.c_uint64, P, P, P, P, P],
 }
 
 
@@ -135,3 +136,16 @@ def surface(words, rate: int, dims, iso: float) -> dict:
     return {"ranges": ranges, "active": active, "active_ids": ids, "with_verts": with_verts,
             "block_counts": counts, "vert_offsets": offsets, "num_vertices": nverts, "vertices": verts[:nverts],
             "decoded": cache[:n]}
+
+
+def unpack_vertices(verts: np.ndarray, dims, scale=(1.0, 1.0, 1.0), proj_view=None):
+    """mc_isosurface.vert's position math per vertex: world [n, 3] (and clip [n, 4])."""
+    v = np.ascontiguousarray(verts, dtype=np.uint32).reshape(-1, 2)
+    n = len(v)
+    world = np.zeros((n, 3), np.float32)
+    sc = np.ascontiguousarray(np.asarray(scale, np.float32))
+    clip = np.zeros((n, 4), np.float32) if proj_view is not None else None
+    pv = np.ascontiguousarray(np.asarray(proj_view, np.float32).reshape(16)) if proj_view is not None else None
+    load().ref_unpack_vertices(_p(v), n, _p(_dims(dims)), _p(sc), _p(pv) if pv is not None else None, _p(world),
+                               _p(clip) if clip is not None else None)
+    return (world, clip) if clip is not None else world

@@ -23,7 +23,8 @@ The rewrites (no semantic edits to the shader bodies):
   * parameter qualifiers: `inout T x` -> `T& x`, `in T x` -> `T x`
     (array parameters are pointers in C++, which is `inout`)
   * float literals get an `f` suffix (GLSL literals are 32-bit)
-  * swizzles `.xyz/.xy/.xz/.yz` -> glsl::swz_* helpers
+  * swizzles `.xyz/.xy/.xz/.yz` -> glsl::swz_* helpers (`v.xyz = e` -> glsl::set_xyz)
+  * vertex-stage `layout(location = n) in/out T x;` -> namespace-scope variables
   * min/max/abs/ldexp -> glsl_* helpers, barrier() -> ref_barrier(), main -> main_
   * every program lives in its own namespace and translation unit
 
@@ -53,6 +54,8 @@ PROGRAMS = {
     "compute_block_has_vertices": "compute_block_has_vertices.comp",
     "compute_block_voxel_num_verts": "compute_block_voxel_num_verts.comp",
     "compute_block_vertices": "compute_block_vertices.comp",
+    # the vertex stage's position math (the render pass itself is not run)
+    "mc_isosurface_vert": "mc_isosurface.vert",
 }
 
 
@@ -101,6 +104,8 @@ def transform(text: str) -> str:
     s = re.sub(r"#version[^\n]*\n", "\n", s)
     s = re.sub(r"layout\s*\(\s*local_size[^)]*\)\s*in\s*;", "", s)
     s = convert_blocks(s)
+    # vertex-stage inputs/outputs: namespace-scope variables the harness sets/reads
+    s = re.sub(r"layout\s*\(\s*location\s*=\s*\d+\s*\)\s*(in|out)\s+(\w+)\s+(\w+)\s*;", r"\2 \3{};", s)
     s = re.sub(r"\bshared\s+", "", s)
     # arrays returned by value
     s = re.sub(r"\bfloat\s*\[\s*8\s*\]\s+(\w+)\s*\(", r"std::array<float, 8> \1(", s)
@@ -125,6 +130,7 @@ def transform(text: str) -> str:
     s = re.sub(r"(?<![\w.])(\d+\.\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])",
                r"\1f", s)
     # swizzles and built-ins
+    s = re.sub(r"\b(\w+)\.xyz\s*=(?!=)", r"glsl::set_xyz(\1) =", s)
     s = re.sub(r"\b(\w+)\.(xyz|xy|xz|yz)\b", r"glsl::swz_\2(\1)", s)
     s = re.sub(r"\b(min|max|abs|ldexp)\s*\(", r"glsl_\1(", s)
     s = re.sub(r"\bbarrier\s*\(\s*\)", "ref_barrier()", s)

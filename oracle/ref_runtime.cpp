@@ -17,6 +17,7 @@
 uvec3 gl_GlobalInvocationID;
 uvec3 gl_LocalInvocationID;
 uvec3 gl_WorkGroupID;
+vec4 gl_Position;
 
 namespace {
 

@@ -86,6 +86,15 @@ struct V : VS<T, N> {
         (*this)[2] = cvt<T>(c);
         (*this)[3] = cvt<T>(d);
     }
+    template <class U, class S, class = std::enable_if_t<std::is_arithmetic_v<S>>>
+    V(const V<U, 3>& a, S s)
+        requires(N == 4)
+    {
+        this->x = cvt<T>(a[0]);
+        this->y = cvt<T>(a[1]);
+        (*this)[2] = cvt<T>(a[2]);
+        (*this)[3] = cvt<T>(s);
+    }
     // GLSL's implicit int -> uint -> float conversions between vector types
     template <class U, class = std::enable_if_t<!std::is_same_v<U, T>>>
     V(const V<U, N>& o)
@@ -192,6 +201,43 @@ inline auto swz_xyz(const Vec& v)
 {
     return V<std::remove_cv_t<std::remove_reference_t<decltype(v[0])>>, 3>(v[0], v[1], v[2]);
 }
+// `v.xyz = e` (the target of an assignment)
+template <class Vec>
+struct SetXyz {
+    Vec& v;
+    template <class U>
+    SetXyz& operator=(const V<U, 3>& o)
+    {
+        using T = std::remove_cv_t<std::remove_reference_t<decltype(v[0])>>;
+        v[0] = cvt<T>(o[0]);
+        v[1] = cvt<T>(o[1]);
+        v[2] = cvt<T>(o[2]);
+        return *this;
+    }
+};
+template <class Vec>
+inline SetXyz<Vec> set_xyz(Vec& v)
+{
+    return {v};
+}
+
+// mat4: four vec4 columns; m * v = sum_i m[i] * v[i], added in column order
+struct mat4 {
+    V<float, 4> c[4];
+    V<float, 4>& operator[](int i) { return c[i]; }
+    const V<float, 4>& operator[](int i) const { return c[i]; }
+};
+inline V<float, 4> operator*(const mat4& m, const V<float, 4>& v)
+{
+    V<float, 4> r;
+    for (int row = 0; row < 4; ++row) {
+        float acc = m.c[0][row] * v[0];
+        for (int i = 1; i < 4; ++i) acc = acc + m.c[i][row] * v[i];
+        r[row] = acc;
+    }
+    return r;
+}
+
 template <class Vec, int I, int J>
 struct Swz2 {
     Vec& v;
@@ -273,6 +319,10 @@ typedef glsl::V<uint, 2> uvec2;
 typedef glsl::V<uint, 3> uvec3;
 typedef glsl::V<uint, 4> uvec4;
 typedef glsl::V<bool, 3> bvec3;
+typedef glsl::mat4 mat4;
+
+// vertex-stage built-in output
+extern vec4 gl_Position;
 
 // Invocation ids of the running invocation (set by the runtime before it
 // resumes each invocation) and the workgroup barrier.

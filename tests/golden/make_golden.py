@@ -11,6 +11,7 @@ reference's shaders produce for them:
                      flags, active ids, blocks with vertices, vertex offsets,
                      the packed vertex buffer
   decode_rate<r>.npz random words and the reference decoder's output, bits
+  unpack_ct44.npz    the vertex stage's world and clip positions of a mesh, bits
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -72,6 +73,22 @@ def make_decode(rate):
                         decoded_bits=dec.view(np.uint32))
 
 
+UNPACK_PROJ = (np.arange(16, dtype=np.float32).reshape(4, 4) * np.float32(0.37) - np.float32(1.1))
+
+
+def make_unpack():
+    """mc_isosurface.vert's position math on the ct44 mesh (scale != 1, a
+    view-projection matrix)."""
+    g = np.load(os.path.join(HERE, "mc_ct44_r4.npz"))
+    verts = g["vertices_0"]
+    dims = tuple(int(d) for d in g["dims"])
+    scale = (1.0, 0.5, 2.0)
+    world, clip = R.unpack_vertices(verts, dims, scale, UNPACK_PROJ)
+    np.savez_compressed(os.path.join(HERE, "unpack_ct44.npz"), dims=np.asarray(dims, np.uint32),
+                        scale=np.asarray(scale, np.float32), proj=UNPACK_PROJ, vertices=verts,
+                        world_bits=world.view(np.uint32), clip_bits=clip.view(np.uint32))
+
+
 def main():
     O.build()
     if not R.available():
@@ -80,6 +97,7 @@ def main():
         make_mc(name, *spec)
     for rate in DECODE_RATES:
         make_decode(rate)
+    make_unpack()
 
 
 if __name__ == "__main__":

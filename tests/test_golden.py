@@ -92,3 +92,10 @@ def test_oracle_matches_reference_shaders_live(oracle, kind, dims, seed, rate, i
         g = {"active_0": s["active"], "active_ids_0": s["active_ids"], "with_verts_0": s["with_verts"],
              "vert_offsets_0": s["vert_offsets"], "vertices_0": s["vertices"]}
         check_mc_against_golden(m, g, 0, n)
+
+
+def test_oracle_unpack_matches_reference_vertex_stage(oracle):
+    g = np.load(os.path.join(GOLDEN, "unpack_ct44.npz"))
+    world, clip = oracle.unpack_vertices(g["vertices"], tuple(g["dims"]), tuple(g["scale"]), g["proj"])
+    assert np.array_equal(world.view(np.uint32), g["world_bits"])
+    assert np.array_equal(clip.view(np.uint32), g["clip_bits"])

@@ -76,3 +76,15 @@ def test_full_ranges_flag(ctx, oracle):
     got = mc.views()["ranges"].numpy().reshape(-1, 2)
     assert np.array_equal(bits(got), bits(want.reshape(-1, 2)))
     assert np.array_equal(bits(got[:ref_count]), bits(g["ranges"][:ref_count]))
+
+
+def test_unpack_matches_reference_vertex_stage(ctx):
+    import torch
+
+    g = np.load(os.path.join(GOLDEN, "unpack_ct44.npz"))
+    verts = torch.from_numpy(g["vertices"].view(np.int32).copy()).cuda()
+    world, clip = bcmc.unpack_vertices(ctx, verts, tuple(int(d) for d in g["dims"]), tuple(g["scale"]), g["proj"])
+    assert np.array_equal(world.cpu().numpy().view(np.uint32), g["world_bits"])
+    assert np.array_equal(clip.cpu().numpy().view(np.uint32), g["clip_bits"])
+    w2 = bcmc.unpack_vertices(ctx, verts, tuple(int(d) for d in g["dims"]), tuple(g["scale"]))
+    assert np.array_equal(w2.cpu().numpy().view(np.uint32), g["world_bits"])

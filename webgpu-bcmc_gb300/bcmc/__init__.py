@@ -32,7 +32,7 @@ from ._lib import BcmcError, check, dims3, scale3
 
 __all__ = ["Context", "CompressedMarchingCubes", "LRUCache", "ExclusiveScanPipeline", "ExclusiveScanner",
            "StreamCompact", "RadixSorter", "DeviceArray", "BcmcError", "zfp_encode", "zfp_decode_volume",
-           "zfp_block_ranges", "block_active", "stream_words", "Engine", "Server"]
+           "zfp_block_ranges", "block_active", "stream_words", "Engine", "Server", "unpack_vertices"]
 
 
 def _torch():
@@ -499,6 +499,25 @@ def zfp_decode_volume(ctx: Context, words, nblocks: int, rate: int):
     check(_lib.load().bcmc_zfp_decode_volume(ctx.handle, C.c_void_p(_ptr(words)), int(nblocks), int(rate),
                                              C.c_void_p(out.data_ptr()), C.c_void_p(_torch_stream())), ctx.handle)
     return out
+
+
+def unpack_vertices(ctx: Context, vertices, dims, scale=(1.0, 1.0, 1.0), proj_view=None):
+    """World-space positions of packed vertices (mc_isosurface.vert:51-60):
+    float32 CUDA tensor [n, 3]; with proj_view (4x4, column-major order as the
+    reference's gl-matrix uses) also the clip positions [n, 4]."""
+    t = _torch()
+    n = int(vertices.shape[0]) if hasattr(vertices, "shape") else 0
+    world = t.empty((n, 3), dtype=t.float32, device="cuda")
+    clip = t.empty((n, 4), dtype=t.float32, device="cuda") if proj_view is not None else None
+    pv = None
+    if proj_view is not None:
+        m = np.ascontiguousarray(np.asarray(proj_view, dtype=np.float32).reshape(16))
+        pv = m.ctypes.data_as(C.POINTER(C.c_float))
+    check(_lib.load().bcmc_unpack_vertices(ctx.handle, C.c_void_p(_ptr(vertices) if n else 0), n, dims3(dims),
+                                           scale3(scale), C.c_void_p(world.data_ptr()), pv,
+                                           C.c_void_p(clip.data_ptr()) if clip is not None else None,
+                                           C.c_void_p(_torch_stream())), ctx.handle)
+    return (world, clip) if clip is not None else world
 
 
 def zfp_block_ranges(ctx: Context, words, dims, rate: int):

@@ -122,6 +122,7 @@ SIGNATURES = {
     "bcmc_scan_exclusive_u32": (C.c_int, [P, P, U32, U32, U32P]),
     "bcmc_scan_exclusive_u32_async": (C.c_int, [P, P, P, U32, P, P]),
     "bcmc_scan_exclusive_u32_noalloc": (C.c_int, [P, P, U32, P, P]),
+    "bcmc_unpack_vertices": (C.c_int, [P, P, U64, U32P, C.POINTER(C.c_float), P, C.POINTER(C.c_float), P, P]),
     "bcmc_engine_create": (C.c_int, [P, C.POINTER(bcmc_engine_opts), C.POINTER(P)]),
     "bcmc_engine_destroy": (None, [P]),
     "bcmc_engine_add_volume": (C.c_int, [P, P, C.c_size_t, U32, U32P, U32P]),

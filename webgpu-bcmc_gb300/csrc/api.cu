@@ -989,6 +989,20 @@ bcmc_status bcmc_zfp_decode_blocks(bcmc_ctx* ctx, const uint64_t* d_words, uint3
     });
 }
 
+bcmc_status bcmc_unpack_vertices(bcmc_ctx* ctx, const void* d_vertices, uint64_t n, const uint32_t dims[3],
+                                 const float scale[3], float* d_world, const float* proj_view, float* d_clip,
+                                 void* stream)
+{
+    if (!ctx || !dims || !dims[0] || !dims[1] || !dims[2] || (n && (!d_vertices || !d_world)) ||
+        (proj_view && !d_clip))
+        return BCMC_E_ARG;
+    return guarded(ctx, [&]() -> bcmc_status {
+        unpack_launch(ctx, static_cast<const uint2*>(d_vertices), n, dims, scale, proj_view, d_world, d_clip,
+                      pick(ctx, stream));
+        return BCMC_OK;
+    });
+}
+
 bcmc_status bcmc_zfp_decode_volume(bcmc_ctx* ctx, const uint64_t* d_words, uint64_t nblocks, uint32_t rate,
                                    float* d_out, void* stream)
 {

@@ -47,6 +47,10 @@ void dev_free(bcmc_ctx* ctx, void* p, size_t bytes);
 void ensure_status(bcmc_ctx* ctx, size_t words);
 void ensure_scratch(bcmc_ctx* ctx, size_t words);
 
+// ---- unpack.cu ----------------------------------------------------------------
+void unpack_launch(bcmc_ctx* ctx, const uint2* verts, uint64_t n, const uint32_t dims[3], const float scale[3],
+                   const float* proj_view, float* world, float* clip, cudaStream_t s);
+
 // ---- engine.cu (for server.cu) ------------------------------------------------
 int engine_device(bcmc_engine* e);
 uint64_t engine_vertex_budget(bcmc_engine* e);
