@@ -394,6 +394,11 @@ def served_bench() -> dict:
                      "evicted_blocks": st["evicted_blocks"]}}
 
 
+# DRAM bytes (read + write) per launch from one ncu capture of this workload's
+# launch list (profiles/ct256_launch_list.md), mean over the 16-isovalue sweep
+NCU_TRAFFIC = {"k_mc": 41.179e6}
+
+
 def algorithmic_bytes(stage: str, st: dict, rate: int, total_blocks: int) -> float:
     """Algorithmic DRAM bytes per launch of each stage's kernel."""
     if stage == "computeVertices":  # k_mc: block data + ids/slots + vertices
@@ -531,7 +536,10 @@ def run_gb300(args):
                         "d2h_bytes_per_step": d2h},
                 "roofline": {"bound": "hbm", "kernel": kernel_of[dominant], "achieved": achieved, "peak": peak,
                              "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                             "traffic": None, "avg_launch_ms": avg_ms, "algorithmic_bytes": bytes_per_launch},
+                             "traffic": NCU_TRAFFIC.get(kernel_of[dominant]), "avg_launch_ms": avg_ms,
+                             "algorithmic_bytes": bytes_per_launch,
+                             "traffic_source": "profiles/ct256_launch_list.md (ncu dram bytes read+write, "
+                                               "mean over the sweep's launches)"},
                 "stage_ms_per_query": {s: tot[s] / nq for s in stages},
                 "latency_ms": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
                                "p99": float(np.percentile(lat, 99)), "queries": len(lat),
