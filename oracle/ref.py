@@ -34,6 +34,9 @@ _SIGS = {
     "ref_block_num_verts": [P, F32, P, P, P, P, P, U32, P],
     "ref_block_vertices": [P, F32, P, P, P, P, P, U32, P],
     "ref_unpack_vertices": [P, C.c_uint64, P, P, P, P, P],
+    "ref_radix_sort_chunk": [P, P, U32, U32],
+    "ref_merge_sorted_chunks": [P, P, P, P, U32, U32],
+    "ref_reverse_buffer": [P, U32, U32],
 }
 
 
@@ -149,3 +152,40 @@ def unpack_vertices(verts: np.ndarray, dims, scale=(1.0, 1.0, 1.0), proj_view=No
     load().ref_unpack_vertices(_p(v), n, _p(_dims(dims)), _p(sc), _p(pv) if pv is not None else None, _p(world),
                                _p(clip) if clip is not None else None)
     return (world, clip) if clip is not None else world
+
+
+def _next_pow2(a: int) -> int:
+    a -= 1
+    for sh in (1, 2, 4, 8, 16):
+        a |= a >> sh
+    return a + 1
+
+
+def sort_by_key(keys: np.ndarray, values: np.ndarray, reverse: bool) -> np.ndarray:
+    """RadixSorter.sort (js/radix_sort_by_key.js:161-400) over the reference's
+    shaders: chunk sort, log2(chunks) merges ping-ponging between the buffers
+    and scratch, the reverse pass when `reverse`, and the readback of `size`
+    values from offset alignedSize - size (reverse) or 0.  Returns the sorted
+    values.  For n <= 64 the reverse pass races in the reference (64 threads
+    each swapping a pair both ways); the fibers here run it sequentially."""
+    L = load()
+    n = len(keys)
+    chunks = _next_pow2(-(-n // 64))
+    aligned = chunks * 64
+    steps = chunks.bit_length() - 1
+    buf_k = np.zeros(aligned, np.uint32)
+    buf_v = np.zeros(aligned, np.uint32)
+    buf_k[:n] = keys
+    buf_v[:n] = values
+    scr_k = np.zeros(aligned, np.uint32)
+    scr_v = np.zeros(aligned, np.uint32)
+    L.ref_radix_sort_chunk(_p(buf_k), _p(buf_v), n, chunks)
+    for i in range(steps):
+        groups = chunks // (2 << i)
+        src, dst = ((buf_k, buf_v), (scr_k, scr_v)) if i % 2 == 0 else ((scr_k, scr_v), (buf_k, buf_v))
+        L.ref_merge_sorted_chunks(_p(src[0]), _p(src[1]), _p(dst[0]), _p(dst[1]), n, groups)
+    vals = buf_v if steps % 2 == 0 else scr_v
+    if reverse:
+        L.ref_reverse_buffer(_p(vals), n, -(-chunks // 2))
+    off = aligned - n if reverse else 0
+    return vals[off: off + n].copy()

@@ -25,7 +25,9 @@ The rewrites (no semantic edits to the shader bodies):
   * float literals get an `f` suffix (GLSL literals are 32-bit)
   * swizzles `.xyz/.xy/.xz/.yz` -> glsl::swz_* helpers (`v.xyz = e` -> glsl::set_xyz)
   * vertex-stage `layout(location = n) in/out T x;` -> namespace-scope variables
-  * min/max/abs/ldexp -> glsl_* helpers, barrier() -> ref_barrier(), main -> main_
+  * min/max/abs/ldexp/ceil -> glsl_* helpers, barrier() -> ref_barrier(), main -> main_
+  * compiled with the defines shaders/embed_shaders.py passes (BLOCK_SIZE=512,
+    SORT_CHUNK_SIZE=64)
   * every program lives in its own namespace and translation unit
 
 Usage: python oracle/ref_build.py [--reference DIR]
@@ -56,7 +58,13 @@ PROGRAMS = {
     "compute_block_vertices": "compute_block_vertices.comp",
     # the vertex stage's position math (the render pass itself is not run)
     "mc_isosurface_vert": "mc_isosurface.vert",
+    # RadixSorter (js/radix_sort_by_key.js): chunk sort, merges, reverse
+    "radix_sort_chunk": "radix_sort_chunk.comp",
+    "merge_sorted_chunks": "merge_sorted_chunks.comp",
+    "reverse_buffer": "reverse_buffer.comp",
 }
+# what shaders/embed_shaders.py passes to every shader compile
+DEFINES = ["-DBLOCK_SIZE=512", "-DSORT_CHUNK_SIZE=64"]
 
 
 def reference_dir(arg: str | None) -> str:
@@ -132,7 +140,7 @@ def transform(text: str) -> str:
     # swizzles and built-ins
     s = re.sub(r"\b(\w+)\.xyz\s*=(?!=)", r"glsl::set_xyz(\1) =", s)
     s = re.sub(r"\b(\w+)\.(xyz|xy|xz|yz)\b", r"glsl::swz_\2(\1)", s)
-    s = re.sub(r"\b(min|max|abs|ldexp)\s*\(", r"glsl_\1(", s)
+    s = re.sub(r"\b(min|max|abs|ldexp|ceil)\s*\(", r"glsl_\1(", s)
     s = re.sub(r"\bbarrier\s*\(\s*\)", "ref_barrier()", s)
     s = re.sub(r"\bvoid\s+main\s*\(\s*(void)?\s*\)", "void main_()", s)
     return s
@@ -175,7 +183,7 @@ def build(ref: str | None = None, force: bool = False) -> str | None:
         return LIB
     srcs = generate(ref) + [os.path.join(HERE, "ref_runtime.cpp")]
     flags = ["g++", "-std=c++20", "-O2", "-fPIC", "-fwrapv", "-ffp-contract=off", "-fno-fast-math",
-             "-I", HERE, "-I", GEN]
+             "-I", HERE, "-I", GEN] + DEFINES
     objs = []
 
     def cc(src):

@@ -301,6 +301,7 @@ inline T glsl_max(T x, T y)
 inline float glsl_abs(float x) { return std::fabs(x); }
 inline int glsl_abs(int x) { return x < 0 ? -x : x; }
 inline float glsl_ldexp(float x, int e) { return std::ldexp(x, e); }
+inline float glsl_ceil(float x) { return std::ceil(x); }
 
 using glsl::all;
 using glsl::any;

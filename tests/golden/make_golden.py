@@ -12,6 +12,7 @@ reference's shaders produce for them:
                      the packed vertex buffer
   decode_rate<r>.npz random words and the reference decoder's output, bits
   unpack_ct44.npz    the vertex stage's world and clip positions of a mesh, bits
+  sort.npz           RadixSorter.sort results (values, ascending and descending)
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -89,6 +90,24 @@ def make_unpack():
                         world_bits=world.view(np.uint32), clip_bits=clip.view(np.uint32))
 
 
+SORT_CASES = [(65, 5), (100, 3), (1000, 50), (4097, 7), (20000, 1000), (3000, 1 << 31)]
+
+
+def make_sort():
+    """RadixSorter.sort over the reference's chunk-sort, merge and reverse
+    shaders (n > 64: below that the reference's reverse pass races)."""
+    out = {}
+    for i, (n, kmax) in enumerate(SORT_CASES):
+        rng = np.random.default_rng(500 + i)
+        keys = rng.integers(0, kmax, size=n, dtype=np.uint64).astype(np.uint32)
+        vals = rng.permutation(n).astype(np.uint32)
+        out[f"keys_{i}"] = keys
+        out[f"values_{i}"] = vals
+        out[f"asc_{i}"] = R.sort_by_key(keys, vals, False)
+        out[f"desc_{i}"] = R.sort_by_key(keys, vals, True)
+    np.savez_compressed(os.path.join(HERE, "sort.npz"), cases=np.int32(len(SORT_CASES)), **out)
+
+
 def main():
     O.build()
     if not R.available():
@@ -98,6 +117,7 @@ def main():
     for rate in DECODE_RATES:
         make_decode(rate)
     make_unpack()
+    make_sort()
 
 
 if __name__ == "__main__":

@@ -99,3 +99,22 @@ def test_oracle_unpack_matches_reference_vertex_stage(oracle):
     world, clip = oracle.unpack_vertices(g["vertices"], tuple(g["dims"]), tuple(g["scale"]), g["proj"])
     assert np.array_equal(world.view(np.uint32), g["world_bits"])
     assert np.array_equal(clip.view(np.uint32), g["clip_bits"])
+
+
+def test_oracle_sort_matches_reference_shaders(oracle):
+    g = np.load(os.path.join(GOLDEN, "sort.npz"))
+    for i in range(int(g["cases"])):
+        k, v = g[f"keys_{i}"], g[f"values_{i}"]
+        assert np.array_equal(oracle.sort_by_key(k, v, False)[1], g[f"asc_{i}"]), i
+        assert np.array_equal(oracle.sort_by_key(k, v, True)[1], g[f"desc_{i}"]), i
+
+
+def test_oracle_sort_matches_reference_shaders_live(oracle):
+    R = _ref()
+    rng = np.random.default_rng(77)
+    for _ in range(16):
+        n = int(rng.integers(65, 1200))
+        k = rng.integers(0, int(rng.choice([2, 9, 300, 2**32 - 2])), size=n, dtype=np.uint64).astype(np.uint32)
+        v = rng.permutation(n).astype(np.uint32)
+        for rev in (False, True):
+            assert np.array_equal(R.sort_by_key(k, v, rev), oracle.sort_by_key(k, v, rev)[1])

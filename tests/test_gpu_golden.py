@@ -88,3 +88,15 @@ def test_unpack_matches_reference_vertex_stage(ctx):
     assert np.array_equal(clip.cpu().numpy().view(np.uint32), g["clip_bits"])
     w2 = bcmc.unpack_vertices(ctx, verts, tuple(int(d) for d in g["dims"]), tuple(g["scale"]))
     assert np.array_equal(w2.cpu().numpy().view(np.uint32), g["world_bits"])
+
+
+def test_sort_matches_reference_shaders(ctx):
+    from gpu_util import to_host
+
+    g = np.load(os.path.join(GOLDEN, "sort.npz"))
+    for i in range(int(g["cases"])):
+        k, v = g[f"keys_{i}"], g[f"values_{i}"]
+        for rev, want in ((False, g[f"asc_{i}"]), (True, g[f"desc_{i}"])):
+            kd, vd = to_dev(k), to_dev(v)
+            bcmc.RadixSorter(ctx).sort(kd, vd, len(k), rev)
+            assert np.array_equal(to_host(vd, np.uint32), want), (i, rev)
