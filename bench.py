@@ -261,6 +261,7 @@ def batched_bench(reps: int = 5) -> dict:
     for (kind, dims), st in zip(BATCH["volumes"], streams):
         eng.addVolume(st, rate, dims)
     eng.run(qs)  # warm-up: decodes the blocks the batch needs
+    tune = eng.autotune(qs)  # launch parameters for this batch size, by timing
     launches0 = bcmc._lib.load().bcmc_kernel_launches()
     batch_ms, dev_ms = [], []
     for _ in range(reps):
@@ -292,6 +293,7 @@ def batched_bench(reps: int = 5) -> dict:
             "batched": {"queries_per_s": len(qs) / (bm / 1000.0), "batch_ms": bm,
                         "device_ms": float(np.median(dev_ms)), "p50_ms": bm, "p99_ms": float(np.max(batch_ms)),
                         "gpu_launches_per_batch": launches / reps},
+            "autotune": tune,
             "speedup_qps": (len(qs) / (bm / 1000.0)) / (len(qs) / plain_s),
             "identical_to_plain": identical,
             "latency_note": "a batch's queries all complete when the batch does: per-query latency = batch wall time"}
@@ -353,7 +355,7 @@ def served_bench() -> dict:
         mcs.append(mc)
     for v, iso in draw(40):  # warm-up: caches grow
         mcs[v].computeSurface(iso)
-    plain_q = draw(100)
+    plain_q = draw(200)
     lat = []
     t0 = time.perf_counter()
     for v, iso in plain_q:
@@ -383,13 +385,52 @@ def served_bench() -> dict:
         srv.close()
     st = eng.stats()
     p99_plain = float(np.percentile(lat, 99))
-    ok = [s for s in sweeps if s["p99_ms"] <= p99_plain and s["achieved_qps"] >= 0.95 * s["offered_qps"]]
-    best = max(ok, key=lambda s: s["achieved_qps"]) if ok else None
+
+    def plain_open_loop(rate_qps, n=2000, seed=0):
+        """The plain path as a FIFO single server under the same open-loop
+        Poisson arrivals, from its measured per-query service times: request i
+        starts at max(arrival_i, finish_{i-1}).  Exact for one FIFO server."""
+        g = np.random.default_rng(seed)
+        arrive = np.cumsum(g.exponential(1.0 / rate_qps, size=n))
+        svc = np.asarray(lat)[np.arange(n) % len(lat)] / 1000.0
+        finish = np.empty(n)
+        t = 0.0
+        for i in range(n):
+            t = max(t, arrive[i]) + svc[i]
+            finish[i] = t
+        l_ms = 1000.0 * (finish - arrive)
+        return {"offered_qps": rate_qps, "achieved_qps": n / (finish[-1] - arrive[0]),
+                "p50_ms": float(np.percentile(l_ms, 50)), "p99_ms": float(np.percentile(l_ms, 99))}
+
+    plain_sweep = [plain_open_loop(s["offered_qps"]) for s in sweeps]
+
+    def plain_rate_at(p99_ms):
+        """Highest offered rate the plain path sustains with p99 <= p99_ms."""
+        lo, hi = 1.0, plain_qps
+        for _ in range(30):
+            mid = 0.5 * (lo + hi)
+            r = plain_open_loop(mid)
+            if r["p99_ms"] <= p99_ms and r["achieved_qps"] >= 0.95 * mid:
+                lo = mid
+            else:
+                hi = mid
+        return lo
+
+    ratios = []
+    for sv in sweeps:
+        if sv["achieved_qps"] >= 0.95 * sv["offered_qps"]:
+            ratios.append({"served_qps": sv["achieved_qps"], "p99_ms": sv["p99_ms"],
+                           "plain_qps_at_same_p99": plain_rate_at(sv["p99_ms"])})
+    for r in ratios:
+        r["ratio"] = r["served_qps"] / r["plain_qps_at_same_p99"]
+    best = max(ratios, key=lambda r: r["ratio"]) if ratios else None
     return {"workload": SERVED["workload"],
-            "plain": {"queries_per_s": plain_qps, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": p99_plain},
+            "plain": {"queries_per_s": plain_qps, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": p99_plain,
+                      "what": "back to back, one query at a time (service times)"},
+            "plain_open_loop": plain_sweep,
             "served": sweeps,
-            "best_served_qps_at_plain_p99": best["achieved_qps"] if best else None,
-            "ratio_vs_plain_at_equal_p99": (best["achieved_qps"] / plain_qps) if best else None,
+            "served_vs_plain_at_equal_p99": ratios,
+            "best_ratio_at_equal_p99": best["ratio"] if best else None,
             "pool": {"slots": st["pool_slots"], "used": st["pool_used"], "decoded_blocks": st["decoded_blocks"],
                      "evicted_blocks": st["evicted_blocks"]}}
 

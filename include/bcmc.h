@@ -323,6 +323,20 @@ bcmc_status bcmc_engine_run_admit(bcmc_engine* eng, const bcmc_query* queries, u
 bcmc_status bcmc_engine_vertices(bcmc_engine* eng, const void** d_vertices, uint64_t* count);
 bcmc_status bcmc_engine_copy_vertices(bcmc_engine* eng, uint64_t first, uint64_t count, void* host);
 bcmc_status bcmc_engine_stats_get(bcmc_engine* eng, bcmc_engine_stats* out);
+/* Autotuner: for the batch-size bucket of min(n, max_batch) queries, times the
+ * launch sequence on these queries (device time, best of 3, CUDA events) over
+ * the CTAs per SM of the active test and of the MC kernel (coordinate descent
+ * from the defaults), and times a decode probe over up to 2^18 blocks of the
+ * largest volume for the decode kernel's threads per CTA and CTAs per SM.  The
+ * chosen parameters are used (and captured into that bucket's graph) from then
+ * on.  The kernels' tile shapes are compile-time constants. */
+typedef struct {
+    uint32_t bucket;
+    int32_t act_ctas_per_sm, decode_threads, decode_ctas_per_sm, mc_ctas_per_sm;
+    double batch_ms_default, batch_ms_tuned, decode_ms_default, decode_ms_tuned;
+} bcmc_tune_report;
+bcmc_status bcmc_engine_autotune(bcmc_engine* eng, const bcmc_query* queries, uint32_t n,
+                                 bcmc_tune_report* out);
 
 /* ---- Isosurface server ----------------------------------------------------- */
 /* No counterpart in the reference.  A request loop over an engine: a worker

@@ -143,3 +143,16 @@ def test_vertex_budget_admits_a_prefix(ctx, volumes):
     res2, m2 = eng.run_admit(qs[m:])
     assert m2 >= 1
     _check(eng, res2, want[m: m + m2])
+
+
+def test_autotune_keeps_results(ctx, volumes):
+    qs = _queries(volumes, 16, seed=9)
+    want = _plain(ctx, volumes, qs)
+    eng = _engine(ctx, volumes)
+    rep = eng.autotune(qs)
+    assert rep["bucket"] == 16
+    assert rep["mc_ctas_per_sm"] in (4, 5, 6) and rep["act_ctas_per_sm"] in (4, 8, 16)
+    assert rep["decode_threads"] in (64, 128, 256) and rep["decode_ctas_per_sm"] in (8, 16, 32)
+    assert rep["batch_ms_tuned"] <= rep["batch_ms_default"] + 1e-9
+    res = eng.run(qs)
+    _check(eng, res, want)

@@ -586,6 +586,18 @@ class Engine:
             out[i] = (res[i].vertex_offset, res[i].num_vertices, res[i].num_active_blocks)
         return out
 
+    def autotune(self, queries) -> dict:
+        """Chooses the launch parameters for the batch-size bucket of these
+        queries by timing them (bcmc_engine_autotune)."""
+        n = len(queries)
+        qs = (_lib.bcmc_query * max(n, 1))()
+        for i, (v, iso) in enumerate(queries):
+            qs[i].volume = int(v)
+            qs[i].isovalue = float(iso)
+        rep = _lib.bcmc_tune_report()
+        check(_lib.load().bcmc_engine_autotune(self._h, qs, n, C.byref(rep)), self.ctx.handle)
+        return {k: getattr(rep, k) for k, _ in _lib.bcmc_tune_report._fields_}
+
     def run_admit(self, queries):
         """Runs the longest prefix of `queries` that the slot pool and the
         vertex budget admit; returns (results of that prefix, its length)."""

@@ -59,6 +59,13 @@ class bcmc_engine_opts(C.Structure):
                 ("max_batch", C.c_uint32), ("flags", C.c_uint32)]
 
 
+class bcmc_tune_report(C.Structure):
+    _fields_ = [("bucket", C.c_uint32)] + [(n, C.c_int32) for n in ("act_ctas_per_sm", "decode_threads",
+                                                                     "decode_ctas_per_sm", "mc_ctas_per_sm")] + \
+               [(n, C.c_double) for n in ("batch_ms_default", "batch_ms_tuned", "decode_ms_default",
+                                          "decode_ms_tuned")]
+
+
 class bcmc_server_opts(C.Structure):
     _fields_ = [("max_batch", C.c_uint32), ("max_wait_us", C.c_uint32)]
 
@@ -131,6 +138,7 @@ SIGNATURES = {
     "bcmc_engine_vertices": (C.c_int, [P, C.POINTER(P), C.POINTER(U64)]),
     "bcmc_engine_copy_vertices": (C.c_int, [P, U64, U64, P]),
     "bcmc_engine_stats_get": (C.c_int, [P, C.POINTER(bcmc_engine_stats)]),
+    "bcmc_engine_autotune": (C.c_int, [P, C.POINTER(bcmc_query), U32, C.POINTER(bcmc_tune_report)]),
     "bcmc_server_create": (C.c_int, [P, C.POINTER(bcmc_server_opts), C.POINTER(P)]),
     "bcmc_server_destroy": (None, [P]),
     "bcmc_server_submit": (C.c_int, [P, U32, C.c_float, P, U64, C.POINTER(U64)]),

@@ -290,7 +290,8 @@ __global__ void __launch_bounds__(kEngThreads) k_bactive(BatchArgs a)
 // ---------------------------------------------------------------------------
 // k_bdecode: claimed blocks into their slots, then publish the slot
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_bdecode(BatchArgs a)
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads) k_bdecode(BatchArgs a)
 {
     const uint32_t n = a.st->num_decode;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -304,6 +305,20 @@ __global__ void __launch_bounds__(128) k_bdecode(BatchArgs a)
         a.owner_vol[slot] = v;
         a.owner_block[slot] = b;
         V.item_slots[b] = (int32_t)slot;
+    }
+}
+
+// The autotuner's decode probe: k_bdecode's inner loop into a scratch buffer.
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads) k_decode_probe(const uint64_t* __restrict__ words, uint32_t max_bits,
+                                                           uint32_t n, float* __restrict__ scratch)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float out[64];
+        zfp_decode_block<1>(words, (uint64_t)i * max_bits, max_bits, out);
+        float4* d4 = reinterpret_cast<float4*>(scratch + (uint64_t)i * 64u);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) d4[k] = make_float4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
     }
 }
 
@@ -688,6 +703,15 @@ struct EngVolume {
     BlockGrid grid;
 };
 
+// Launch parameters the autotuner chooses per batch-size bucket (the kernels'
+// tile shapes are compile-time; these are the runtime knobs).
+struct EngConfig {
+    int act_per_sm = 8;      // k_bactive CTAs per SM
+    int dec_threads = 128;   // k_bdecode threads per CTA (64, 128, 256)
+    int dec_per_sm = 16;     // k_bdecode CTAs per SM
+    int mc_per_sm = kBmcPerSm;  // k_bmc CTAs per SM (<= its residency, 6)
+};
+
 struct bcmc_engine {
     bcmc_ctx* ctx = nullptr;
     cudaStream_t stream = nullptr;
@@ -729,17 +753,21 @@ struct bcmc_engine {
     struct Graph {
         cudaGraphExec_t exec = nullptr;
         uint64_t generation = 0;
+        int cfg_key = -1;  // the launch parameters it was captured with
     };
     std::map<uint32_t, Graph> graphs;
+    std::map<uint32_t, EngConfig> tuned;  // per bucket
+    EngConfig cfg;                        // of the sequence being enqueued
     uint64_t generation = 1;
     bcmc_engine_stats stats{};
 };
 
 namespace {
 
-int eng_grid_mc(bcmc_engine* e) { return e->ctx->num_sms * kBmcPerSm; }
-int eng_grid_act(bcmc_engine* e) { return e->ctx->num_sms * 8; }
-int eng_grid_dec(bcmc_engine* e) { return e->ctx->num_sms * 16; }
+int eng_grid_mc_max(bcmc_engine* e) { return e->ctx->num_sms * kBmcPerSm; }  // sizes the status words
+int eng_grid_mc(bcmc_engine* e) { return e->ctx->num_sms * std::min(e->cfg.mc_per_sm, kBmcPerSm); }
+int eng_grid_act(bcmc_engine* e) { return e->ctx->num_sms * e->cfg.act_per_sm; }
+int eng_grid_dec(bcmc_engine* e) { return e->ctx->num_sms * e->cfg.dec_per_sm; }
 
 template <typename T>
 void eng_realloc(bcmc_engine* e, T*& p, uint64_t old_n, uint64_t new_n)
@@ -780,14 +808,14 @@ BatchArgs eng_args(bcmc_engine* e)
 void eng_ensure_status(bcmc_engine* e, uint64_t active_tiles)
 {
     const uint64_t need_a = std::max<uint64_t>(active_tiles + 1, 1024);
-    const uint64_t need = need_a + (uint64_t)eng_grid_mc(e) + 1;
+    const uint64_t need = need_a + (uint64_t)eng_grid_mc_max(e) + 1;
     if (need_a <= e->status_a_words && need <= e->status_words) return;
     BCMC_CUDA(cudaStreamSynchronize(e->stream));
-    const uint64_t words = std::max<uint64_t>(need_a * 2, 4096) + eng_grid_mc(e) + 1;
+    const uint64_t words = std::max<uint64_t>(need_a * 2, 4096) + eng_grid_mc_max(e) + 1;
     eng_realloc(e, e->status, e->status_words, words);
     BCMC_CUDA(cudaMemsetAsync(e->status, 0, words * 8, e->stream));
     e->status_words = words;
-    e->status_a_words = words - eng_grid_mc(e) - 1;
+    e->status_a_words = words - eng_grid_mc_max(e) - 1;
     ++e->generation;
 }
 
@@ -893,7 +921,9 @@ void eng_enqueue(bcmc_engine* e, uint32_t bucket)
     BCMC_CUDA(cudaEventRecordWithFlags(e->ev0, s, cudaEventRecordExternal));
     k_bbegin<<<1, 1024, 0, s>>>(e->d_st, e->q_nverts, e->q_nactive, bucket);
     k_bactive<<<eng_grid_act(e), kEngThreads, 0, s>>>(a);
-    k_bdecode<<<eng_grid_dec(e), 128, 0, s>>>(a);
+    if (e->cfg.dec_threads == 64) k_bdecode<64><<<eng_grid_dec(e), 64, 0, s>>>(a);
+    else if (e->cfg.dec_threads == 256) k_bdecode<256><<<eng_grid_dec(e), 256, 0, s>>>(a);
+    else k_bdecode<128><<<eng_grid_dec(e), 128, 0, s>>>(a);
     count_launches(3);
     k_bmc<<<eng_grid_mc(e), kBmcThreads, 0, s>>>(a);
     k_bfinish<<<1, kFinThreads, 0, s>>>(a);
@@ -906,8 +936,11 @@ void eng_enqueue(bcmc_engine* e, uint32_t bucket)
 
 void eng_launch(bcmc_engine* e, uint32_t bucket)
 {
+    auto it = e->tuned.find(bucket);
+    e->cfg = it != e->tuned.end() ? it->second : EngConfig{};
     auto& g = e->graphs[bucket];
-    if (!g.exec || g.generation != e->generation) {
+    const int key = e->cfg.act_per_sm | (e->cfg.dec_threads << 8) | (e->cfg.dec_per_sm << 18) | (e->cfg.mc_per_sm << 26);
+    if (!g.exec || g.generation != e->generation || g.cfg_key != key) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
         g.exec = nullptr;
         cudaGraph_t graph = nullptr;
@@ -926,6 +959,7 @@ void eng_launch(bcmc_engine* e, uint32_t bucket)
         cudaGraphDestroy(graph);
         BCMC_CUDA(err);
         g.generation = e->generation;
+        g.cfg_key = key;
     }
     BCMC_CUDA(cudaGraphLaunch(g.exec, e->stream));
     count_launches(5);
@@ -1257,6 +1291,112 @@ uint32_t eng_run_prefix(bcmc_engine* e, const bcmc_query* queries, uint32_t n, b
     }
 }
 }  // namespace
+
+namespace {
+// device time of one launch sequence under the current tuned config: best of 3
+double eng_time_sequence(bcmc_engine* e, const bcmc_query* qs, uint32_t n, bcmc_query_result* out)
+{
+    double best = 1e30;
+    for (int r = 0; r < 3; ++r) {
+        e->vert_used = 0;
+        eng_run_sequence(e, qs, n, out);
+        best = std::min(best, e->stats.last_batch_ms);
+    }
+    return best;
+}
+
+double eng_time_decode(bcmc_engine* e, const EngVolume& v, uint32_t nblk, float* scratch, int threads, int per_sm)
+{
+    float best = 1e30f;
+    for (int r = 0; r < 3; ++r) {
+        BCMC_CUDA(cudaEventRecord(e->ev0, e->stream));
+        const int grid = e->ctx->num_sms * per_sm;
+        if (threads == 64) k_decode_probe<64><<<grid, 64, 0, e->stream>>>(v.words, 64u * v.rate, nblk, scratch);
+        else if (threads == 256) k_decode_probe<256><<<grid, 256, 0, e->stream>>>(v.words, 64u * v.rate, nblk, scratch);
+        else k_decode_probe<128><<<grid, 128, 0, e->stream>>>(v.words, 64u * v.rate, nblk, scratch);
+        count_launches(1);
+        BCMC_CUDA(cudaGetLastError());
+        BCMC_CUDA(cudaEventRecord(e->ev1, e->stream));
+        BCMC_CUDA(cudaEventSynchronize(e->ev1));
+        float ms = 0.0f;
+        BCMC_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+        best = std::min(best, ms);
+    }
+    return best;
+}
+}  // namespace
+
+extern "C" bcmc_status bcmc_engine_autotune(bcmc_engine* e, const bcmc_query* queries, uint32_t n,
+                                            bcmc_tune_report* out)
+{
+    if (!e || !queries || !n || !out) return BCMC_E_ARG;
+    if (e->vols.empty()) return BCMC_E_STATE;
+    return eng_guarded(e, [&]() -> bcmc_status {
+        if (!e->pool_slots) {
+            uint64_t all = 0;
+            for (auto& v : e->vols) all += v.total;
+            eng_alloc_pool(e, e->opts.pool_slots ? e->opts.pool_slots : all);
+        }
+        const uint32_t m = std::min(n, e->max_batch);
+        const uint32_t bucket = std::min(bucket_of(m), e->max_batch);
+        std::vector<bcmc_query_result> res(m);
+        e->tuned.erase(bucket);
+        e->vert_used = 0;
+        eng_run_sequence(e, queries, m, res.data());  // warm-up: decodes, buffer growth, graph
+        EngConfig best{};
+        e->tuned[bucket] = best;
+        double t_best = eng_time_sequence(e, queries, m, res.data());
+        out->batch_ms_default = t_best;
+        // coordinate descent over the sequence's launch parameters
+        for (int mc : {4, 5, 6}) {
+            EngConfig c = best;
+            c.mc_per_sm = mc;
+            e->tuned[bucket] = c;
+            const double t = eng_time_sequence(e, queries, m, res.data());
+            if (t < t_best) best = c, t_best = t;
+        }
+        for (int act : {4, 8, 16}) {
+            EngConfig c = best;
+            c.act_per_sm = act;
+            e->tuned[bucket] = c;
+            const double t = eng_time_sequence(e, queries, m, res.data());
+            if (t < t_best) best = c, t_best = t;
+        }
+        out->batch_ms_tuned = t_best;
+        // decode: a probe over (up to 2^18) blocks of the largest volume
+        const EngVolume* big = &e->vols[0];
+        for (auto& v : e->vols)
+            if (v.total > big->total) big = &v;
+        const uint32_t nblk = std::min<uint32_t>(big->total, 1u << 18);
+        float* scratch = (float*)dev_alloc(e->ctx, (size_t)nblk * 256);
+        double d_best = 1e30, d_default = 0.0;
+        try {
+            for (int thr : {64, 128, 256})
+                for (int per_sm : {8, 16, 32}) {
+                    const double t = eng_time_decode(e, *big, nblk, scratch, thr, per_sm);
+                    if (thr == 128 && per_sm == 16) d_default = t;
+                    if (t < d_best) {
+                        d_best = t;
+                        best.dec_threads = thr;
+                        best.dec_per_sm = per_sm;
+                    }
+                }
+        } catch (...) {
+            dev_free(e->ctx, scratch, (size_t)nblk * 256);
+            throw;
+        }
+        dev_free(e->ctx, scratch, (size_t)nblk * 256);
+        e->tuned[bucket] = best;
+        out->decode_ms_default = d_default;
+        out->decode_ms_tuned = d_best;
+        out->act_ctas_per_sm = best.act_per_sm;
+        out->decode_threads = best.dec_threads;
+        out->decode_ctas_per_sm = best.dec_per_sm;
+        out->mc_ctas_per_sm = best.mc_per_sm;
+        out->bucket = bucket;
+        return BCMC_OK;
+    });
+}
 
 extern "C" bcmc_status bcmc_engine_run_admit(bcmc_engine* e, const bcmc_query* queries, uint32_t n,
                                              bcmc_query_result* results, uint32_t* admitted)
