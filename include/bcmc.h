@@ -254,11 +254,39 @@ bcmc_status bcmc_zfp_encode(bcmc_ctx* ctx, const float* d_field, const uint32_t 
  * `dims` and voxel `scale` (NULL = 1): d_world receives 3 floats per vertex,
  * scale * ((4 * block + q * 4 / 1023 + 0.5) / dims - 0.5).  When proj_view
  * (16 floats, column-major, host memory) and d_clip are given, d_clip receives
- * proj_view * (world, 1), 4 floats per vertex.  The render pass that consumes
- * these in the reference is not part of this library. */
+ * proj_view * (world, 1), 4 floats per vertex.  bcmc_render below is the
+ * render pass that consumes them. */
 bcmc_status bcmc_unpack_vertices(bcmc_ctx* ctx, const void* d_vertices, uint64_t n, const uint32_t dims[3],
                                  const float scale[3], float* d_world, const float* proj_view, float* d_clip,
                                  void* stream);
+
+/* Headless render pass of the mesh (js/bcmc.js:174-190,237-265,377-391 with
+ * shaders/mc_isosurface.vert/.frag): n packed vertices (n/3 triangles, in draw
+ * order) into a width x height image.  The image is cleared to (1, 1, 1, 1)
+ * and depth 1.0; a fragment is kept when its depth is in [0, 1) and less than
+ * the stored depth ("less"), the earlier triangle winning ties as in an
+ * in-order pipeline.  Pixel centres at (x + 0.5, y + 0.5), row 0 at the top
+ * (NDC y = +1), depth = NDC z; edges follow the top-left rule.  Shading:
+ * flat normal flipped toward the eye, Blinn-Phong with base colour
+ * (0.3, 0.3, 0.9) and a head light, and with `fog` the depth-cueing fog toward
+ * white from where the eye ray enters the volume's box.  A triangle with a
+ * vertex at clip w <= 1e-6 is not drawn (no near-plane clipping).
+ * d_rgba: width*height*4 floats, row-major, 16-byte aligned; d_depth (may be NULL):
+ * width*height floats; d_triangle (may be NULL): per pixel the index of the
+ * triangle drawn there, 0xFFFFFFFF for background.  Allocates its working buffers (world and clip
+ * positions, one 64-bit depth/triangle key per pixel) for the call's duration
+ * and returns after the stream has finished the pass.
+ * No counterpart as a function in the reference, whose render pass is a
+ * WebGPU render pipeline. */
+typedef struct bcmc_render_params {
+    uint32_t width, height;
+    float proj_view[16]; /* column-major, as ViewParams.proj_view */
+    float eye_pos[3];    /* ViewParams.eye_pos */
+    int32_t fog;         /* DRAW_FOG */
+} bcmc_render_params;
+bcmc_status bcmc_render(bcmc_ctx* ctx, const void* d_vertices, uint64_t n, const uint32_t dims[3],
+                        const float scale[3], const bcmc_render_params* params, float* d_rgba, float* d_depth,
+                        uint32_t* d_triangle, void* stream);
 
 /* compute_block_active.comp:24-61: u32 active flag per block. */
 bcmc_status bcmc_block_active(bcmc_ctx* ctx, const float* d_ranges, const uint32_t dims[3],

@@ -589,6 +589,235 @@ void bcmc_oracle_unpack_vertices(const uint32_t* verts, uint64_t n, const uint32
 }
 
 /* ======================================================================== */
+/* The render pass (js/bcmc.js:174-190,237-265,377-391;                      */
+/* shaders/mc_isosurface.vert:35-60, mc_isosurface.frag:15-40), headless.    */
+/* Rasterisation follows the WebGPU rules the reference relies on: pixel     */
+/* centres at +0.5, NDC y up with row 0 at the top, depth = NDC z in [0, 1], */
+/* "less" against 1.0, 1/256-pixel snapping, top-left rule; ties at equal    */
+/* depth go to the earlier triangle.  Each f32 step is one rounded operation */
+/* in the order the CUDA kernels use and the edge functions are exact        */
+/* integers, so the depth and triangle buffers are reproduced bit for bit.   */
+/* ======================================================================== */
+typedef struct {
+    float x, y, z;
+} ov3;
+
+static ov3 ov3_sub(ov3 a, ov3 b) { return (ov3){a.x - b.x, a.y - b.y, a.z - b.z}; }
+static float ov3_dot(ov3 a, ov3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static ov3 ov3_scale(ov3 a, float s) { return (ov3){a.x * s, a.y * s, a.z * s}; }
+static ov3 ov3_norm(ov3 a) /* GLSL normalize: x / length(x) */
+{
+    const float len = sqrtf(ov3_dot(a, a));
+    return (ov3){a.x / len, a.y / len, a.z / len};
+}
+static ov3 ov3_cross(ov3 a, ov3 b)
+{
+    return (ov3){a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+static float g_min(float x, float y) { return y < x ? y : x; } /* GLSL min */
+static float g_max(float x, float y) { return x < y ? y : x; } /* GLSL max */
+static float g_clamp01(float x) { return g_min(g_max(x, 0.0f), 1.0f); }
+
+void bcmc_oracle_fog_enter(const float* world, uint64_t n, const float eye[3], const float scale[3], float* tenter)
+{
+    const float o[3] = {eye[0], eye[1], eye[2]};
+    float hh[3];
+    for (int k = 0; k < 3; ++k) hh[k] = (scale ? scale[k] : 1.0f) * 0.5f;
+    for (uint64_t i = 0; i < n; ++i) {
+        const ov3 d = ov3_norm(ov3_sub((ov3){world[3 * i], world[3 * i + 1], world[3 * i + 2]}, (ov3){o[0], o[1], o[2]}));
+        const float dd[3] = {d.x, d.y, d.z};
+        float tmin[3];
+        for (int k = 0; k < 3; ++k) {
+            const float inv = 1.0f / dd[k];
+            const float ta = (-hh[k] - o[k]) * inv, tb = (hh[k] - o[k]) * inv;
+            tmin[k] = g_min(ta, tb);
+        }
+        tenter[i] = g_max(g_max(tmin[0], g_max(tmin[1], tmin[2])), 0.0f);
+    }
+}
+
+/* Screen positions snapped to 1/256 pixel, edge functions in exact 64-bit
+ * integers (watertight with the top-left rule). */
+typedef struct {
+    int x[3], y[3];
+    float z[3];
+    int idx[3];
+    long long area;
+} otri;
+
+static long long edge_fn(int ax, int ay, int bx, int by, int px, int py)
+{
+    return (long long)(bx - ax) * (long long)(py - ay) - (long long)(by - ay) * (long long)(px - ax);
+}
+static int top_left(int ax, int ay, int bx, int by) { return (ay == by && bx > ax) || (by < ay); }
+static int floor_div256(int v) { return v >= 0 ? v / 256 : -((255 - v) / 256); }
+
+/* 0 when the triangle is not drawn (w <= 1e-6, beyond +-2^21 pixels, not
+ * finite, zero area) */
+static int tri_setup(const float* c, uint32_t w, uint32_t h, otri* t)
+{
+    for (int k = 0; k < 3; ++k) {
+        const float cw = c[4 * k + 3];
+        if (!(cw > 1e-6f)) return 0;
+        const float nx = c[4 * k] / cw, ny = c[4 * k + 1] / cw;
+        const float sx = (nx * 0.5f + 0.5f) * (float)w, sy = (0.5f - ny * 0.5f) * (float)h;
+        if (!(fabsf(sx) <= 2097152.0f && fabsf(sy) <= 2097152.0f)) return 0;
+        t->x[k] = (int)rintf(sx * 256.0f);
+        t->y[k] = (int)rintf(sy * 256.0f);
+        t->z[k] = c[4 * k + 2] / cw;
+        t->idx[k] = k;
+    }
+    t->area = edge_fn(t->x[0], t->y[0], t->x[1], t->y[1], t->x[2], t->y[2]);
+    if (t->area == 0) return 0;
+    if (t->area < 0) {
+        int tmp = t->x[1];
+        t->x[1] = t->x[2];
+        t->x[2] = tmp;
+        tmp = t->y[1];
+        t->y[1] = t->y[2];
+        t->y[2] = tmp;
+        const float tz = t->z[1];
+        t->z[1] = t->z[2];
+        t->z[2] = tz;
+        t->idx[1] = 2;
+        t->idx[2] = 1;
+        t->area = -t->area;
+    }
+    return 1;
+}
+
+static void edges_at(const otri* t, int px, int py, long long e[3])
+{
+    const int cx = px * 256 + 128, cy = py * 256 + 128;
+    e[0] = edge_fn(t->x[1], t->y[1], t->x[2], t->y[2], cx, cy);
+    e[1] = edge_fn(t->x[2], t->y[2], t->x[0], t->y[0], cx, cy);
+    e[2] = edge_fn(t->x[0], t->y[0], t->x[1], t->y[1], cx, cy);
+}
+
+/* mc_isosurface.frag:15-40 for one fragment: world position, interpolated
+ * t_enter, the triangle's three world vertices (flat normal from its edges,
+ * which the frag's screen derivatives span), fog on/off -> rgba. */
+void bcmc_oracle_shade(const float wp3[3], float te, const float eye[3], const float* tri_world, int fog,
+                       float out[4])
+{
+    const ov3 wp = {wp3[0], wp3[1], wp3[2]};
+    ov3 v = ov3_sub(wp, (ov3){eye[0], eye[1], eye[2]});
+    const float dist = sqrtf(ov3_dot(v, v));
+    v = ov3_scale(ov3_norm(v), -1.0f);
+    const ov3 light = v;
+    const ov3 w0 = {tri_world[0], tri_world[1], tri_world[2]}, w1 = {tri_world[3], tri_world[4], tri_world[5]},
+              w2 = {tri_world[6], tri_world[7], tri_world[8]};
+    ov3 nrm = ov3_norm(ov3_cross(ov3_sub(w1, w0), ov3_sub(w2, w0)));
+    if (ov3_dot(nrm, light) < 0.0f) nrm = ov3_scale(nrm, -1.0f);
+    const float base[3] = {0.3f, 0.3f, 0.9f};
+    const ov3 hv = ov3_norm((ov3){v.x + light.x, v.y + light.y, v.z + light.z});
+    const float diff = 0.6f * g_clamp01(ov3_dot(light, nrm));
+    const float spec = 0.1f * powf(g_clamp01(ov3_dot(nrm, hv)), 5.0f);
+    float col[3];
+    for (int k = 0; k < 3; ++k) col[k] = (base[k] * 0.2f + diff * base[k]) + spec;
+    if (fog) {
+        const float f = expf(-1.0f * g_max(dist - (te + 0.1f), 0.0f));
+        for (int k = 0; k < 3; ++k) col[k] = f * col[k] + (1.0f - f);
+    }
+    out[0] = col[0];
+    out[1] = col[1];
+    out[2] = col[2];
+    out[3] = 1.0f;
+}
+
+int bcmc_oracle_render(const uint32_t* verts, uint64_t n, const uint32_t dims[3], const float scale[3],
+                       const float proj_view[16], const float eye[3], int fog, uint32_t width, uint32_t height,
+                       float* rgba, float* depth, uint32_t* triangle)
+{
+    const uint64_t ntri = n / 3, nv = ntri * 3, npix = (uint64_t)width * height;
+    float* world = (float*)malloc((nv ? nv : 1) * 3 * sizeof(float));
+    float* clip = (float*)malloc((nv ? nv : 1) * 4 * sizeof(float));
+    float* tenter = (float*)malloc((nv ? nv : 1) * sizeof(float));
+    uint64_t* keys = (uint64_t*)malloc((npix ? npix : 1) * sizeof(uint64_t));
+    if (!world || !clip || !tenter || !keys) {
+        free(world);
+        free(clip);
+        free(tenter);
+        free(keys);
+        return -1;
+    }
+    bcmc_oracle_unpack_vertices(verts, nv, dims, scale, proj_view, world, clip);
+    if (fog) bcmc_oracle_fog_enter(world, nv, eye, scale, tenter);
+    for (uint64_t i = 0; i < npix; ++i) keys[i] = ~(uint64_t)0;
+    for (uint64_t ti = 0; ti < ntri; ++ti) {
+        otri t;
+        if (!tri_setup(clip + 12 * ti, width, height, &t)) continue;
+        int xmin = t.x[0], xmax = t.x[0], ymin = t.y[0], ymax = t.y[0];
+        for (int k = 1; k < 3; ++k) {
+            xmin = t.x[k] < xmin ? t.x[k] : xmin;
+            xmax = t.x[k] > xmax ? t.x[k] : xmax;
+            ymin = t.y[k] < ymin ? t.y[k] : ymin;
+            ymax = t.y[k] > ymax ? t.y[k] : ymax;
+        }
+        int x0 = floor_div256(xmin - 128 + 255), x1 = floor_div256(xmax - 128);
+        int y0 = floor_div256(ymin - 128 + 255), y1 = floor_div256(ymax - 128);
+        x0 = x0 < 0 ? 0 : x0;
+        y0 = y0 < 0 ? 0 : y0;
+        x1 = x1 > (int)width - 1 ? (int)width - 1 : x1;
+        y1 = y1 > (int)height - 1 ? (int)height - 1 : y1;
+        const int tl0 = top_left(t.x[1], t.y[1], t.x[2], t.y[2]), tl1 = top_left(t.x[2], t.y[2], t.x[0], t.y[0]),
+                  tl2 = top_left(t.x[0], t.y[0], t.x[1], t.y[1]);
+        for (int py = y0; py <= y1; ++py)
+            for (int px = x0; px <= x1; ++px) {
+                long long e[3];
+                edges_at(&t, px, py, e);
+                if (!((e[0] > 0 || (e[0] == 0 && tl0)) && (e[1] > 0 || (e[1] == 0 && tl1)) &&
+                      (e[2] > 0 || (e[2] == 0 && tl2))))
+                    continue;
+                const float z = (((float)e[0] * t.z[0] + (float)e[1] * t.z[1]) + (float)e[2] * t.z[2]) / (float)t.area;
+                if (!(z >= 0.0f && z < 1.0f)) continue;
+                uint32_t zb;
+                memcpy(&zb, &z, 4);
+                const uint64_t key = ((uint64_t)zb << 32) | (uint32_t)ti;
+                uint64_t* k = keys + (uint64_t)py * width + px;
+                if (key < *k) *k = key;
+            }
+    }
+    for (uint64_t i = 0; i < npix; ++i) {
+        float out[4] = {1.0f, 1.0f, 1.0f, 1.0f}, dep = 1.0f;
+        uint32_t tri = 0xffffffffu;
+        if (keys[i] != ~(uint64_t)0) {
+            const uint64_t t = keys[i] & 0xffffffffu;
+            const uint32_t zb = (uint32_t)(keys[i] >> 32);
+            tri = (uint32_t)t;
+            memcpy(&dep, &zb, 4);
+            otri tr;
+            tri_setup(clip + 12 * t, width, height, &tr);
+            long long ee[3];
+            edges_at(&tr, (int)(i % width), (int)(i / width), ee);
+            const float e[3] = {(float)ee[0], (float)ee[1], (float)ee[2]};
+            float pw[3], psum = 0.0f;
+            for (int k = 0; k < 3; ++k) {
+                pw[k] = e[k] / clip[12 * t + 4 * tr.idx[k] + 3];
+                psum = psum + pw[k];
+            }
+            float wp[3] = {0.0f, 0.0f, 0.0f};
+            float te = 0.0f;
+            for (int k = 0; k < 3; ++k) {
+                const float b = pw[k] / psum;
+                const float* wk = world + 3 * (3 * t + tr.idx[k]);
+                for (int c = 0; c < 3; ++c) wp[c] = wp[c] + b * wk[c];
+                if (fog) te = te + b * tenter[3 * t + tr.idx[k]];
+            }
+            bcmc_oracle_shade(wp, te, eye, world + 9 * t, fog, out);
+        }
+        for (int k = 0; k < 4; ++k) rgba[4 * i + k] = out[k];
+        if (depth) depth[i] = dep;
+        if (triangle) triangle[i] = tri;
+    }
+    free(world);
+    free(clip);
+    free(tenter);
+    free(keys);
+    return 0;
+}
+
+/* ======================================================================== */
 /* compute_block_active.comp:24-61                                           */
 /* ======================================================================== */
 void bcmc_oracle_block_active(const float* ranges, const uint32_t dims[3], float iso,

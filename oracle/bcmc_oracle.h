@@ -57,6 +57,21 @@ void bcmc_oracle_block_ranges(const uint64_t* words, const uint32_t dims[3], uin
 void bcmc_oracle_unpack_vertices(const uint32_t* verts, uint64_t n, const uint32_t dims[3], const float scale[3],
                                  const float* proj_view, float* world, float* clip);
 
+/* ---- the render pass, headless (js/bcmc.js:174-190,237-265,377-391) ------ */
+/* mc_isosurface.vert:35-49 (DRAW_FOG): per vertex the distance along the eye
+ * ray where it enters the box [-scale/2, scale/2], at least 0. */
+void bcmc_oracle_fog_enter(const float* world, uint64_t n, const float eye[3], const float scale[3], float* tenter);
+/* mc_isosurface.frag:15-40 for one fragment (tri_world: the triangle's 3
+ * world vertices, whose edges give the flat normal). */
+void bcmc_oracle_shade(const float wp[3], float t_enter, const float eye[3], const float* tri_world, int fog,
+                       float rgba[4]);
+/* n packed vertices drawn as n/3 triangles into width x height: rgba (4 per
+ * pixel), depth and triangle (may be NULL; 0xFFFFFFFF = background).
+ * Returns 0, or -1 when a host allocation fails. */
+int bcmc_oracle_render(const uint32_t* verts, uint64_t n, const uint32_t dims[3], const float scale[3],
+                       const float proj_view[16], const float eye[3], int fog, uint32_t width, uint32_t height,
+                       float* rgba, float* depth, uint32_t* triangle);
+
 /* ---- compute_block_active.comp:24-61 ------------------------------------- */
 void bcmc_oracle_block_active(const float* ranges, const uint32_t dims[3], float isovalue,
                               uint32_t* active);

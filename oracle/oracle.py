@@ -51,6 +51,11 @@ def lib():
         L.bcmc_oracle_block_ranges.argtypes = [u64p, u32p, C.c_uint32, f32p]
         L.bcmc_oracle_block_active.argtypes = [f32p, u32p, C.c_float, u32p]
         L.bcmc_oracle_unpack_vertices.argtypes = [u32p, C.c_uint64, u32p, f32p, f32p, f32p, f32p]
+        L.bcmc_oracle_fog_enter.argtypes = [f32p, C.c_uint64, f32p, f32p, f32p]
+        L.bcmc_oracle_shade.argtypes = [f32p, C.c_float, f32p, f32p, C.c_int, f32p]
+        L.bcmc_oracle_render.argtypes = [u32p, C.c_uint64, u32p, f32p, f32p, f32p, C.c_int, C.c_uint32,
+                                         C.c_uint32, f32p, f32p, u32p]
+        L.bcmc_oracle_render.restype = C.c_int
         L.bcmc_oracle_exclusive_scan.restype = C.c_uint32
         L.bcmc_oracle_exclusive_scan.argtypes = [u32p, C.c_uint32, C.c_uint32]
         L.bcmc_oracle_compact.argtypes = [u32p, u32p, C.c_uint32, u32p]
@@ -176,6 +181,45 @@ def unpack_vertices(verts: np.ndarray, dims, scale=(1.0, 1.0, 1.0), proj_view=No
                                       _p(pv, f32p) if pv is not None else None, _p(world, f32p),
                                       _p(clip, f32p) if clip is not None else None)
     return (world, clip) if clip is not None else world
+
+
+def fog_enter(world: np.ndarray, eye, scale=(1.0, 1.0, 1.0)) -> np.ndarray:
+    """mc_isosurface.vert:35-49 (DRAW_FOG): per vertex where the eye ray enters the volume's box."""
+    w = np.ascontiguousarray(world, dtype=np.float32).reshape(-1, 3)
+    out = np.zeros(len(w), np.float32)
+    e = np.ascontiguousarray(np.asarray(eye, np.float32))
+    sc = np.ascontiguousarray(np.asarray(scale, np.float32))
+    lib().bcmc_oracle_fog_enter(_p(w, f32p), len(w), _p(e, f32p), _p(sc, f32p), _p(out, f32p))
+    return out
+
+
+def shade(world_pos, t_enter: float, eye, tri_world, fog: bool) -> np.ndarray:
+    """mc_isosurface.frag:15-40 for one fragment."""
+    wp = np.ascontiguousarray(np.asarray(world_pos, np.float32))
+    e = np.ascontiguousarray(np.asarray(eye, np.float32))
+    tw = np.ascontiguousarray(np.asarray(tri_world, np.float32).reshape(9))
+    out = np.zeros(4, np.float32)
+    lib().bcmc_oracle_shade(_p(wp, f32p), float(t_enter), _p(e, f32p), _p(tw, f32p), 1 if fog else 0,
+                            _p(out, f32p))
+    return out
+
+
+def render(verts: np.ndarray, dims, proj_view, eye, width: int, height: int, scale=(1.0, 1.0, 1.0),
+           fog: bool = False):
+    """The render pass, headless: (rgba [h, w, 4], depth [h, w], triangle [h, w] u32)."""
+    v = np.ascontiguousarray(verts, dtype=np.uint32).reshape(-1, 2)
+    rgba = np.zeros((height, width, 4), np.float32)
+    depth = np.zeros((height, width), np.float32)
+    tri = np.zeros((height, width), np.uint32)
+    pv = np.ascontiguousarray(np.asarray(proj_view, np.float32).reshape(16))
+    e = np.ascontiguousarray(np.asarray(eye, np.float32))
+    sc = np.ascontiguousarray(np.asarray(scale, np.float32))
+    rc = lib().bcmc_oracle_render(_p(v, u32p), len(v), _p(_dims(dims), u32p), _p(sc, f32p), _p(pv, f32p),
+                                  _p(e, f32p), 1 if fog else 0, width, height, _p(rgba, f32p), _p(depth, f32p),
+                                  _p(tri, u32p))
+    if rc != 0:
+        raise MemoryError("oracle render: host allocation failed")
+    return rgba, depth, tri
 
 
 def block_active(ranges: np.ndarray, dims, iso: float) -> np.ndarray:

@@ -34,6 +34,9 @@ _SIGS = {
     "ref_block_num_verts": [P, F32, P, P, P, P, P, U32, P],
     "ref_block_vertices": [P, F32, P, P, P, P, P, U32, P],
     "ref_unpack_vertices": [P, C.c_uint64, P, P, P, P, P],
+    "ref_vert_fog": [P, C.c_uint64, P, P, P, P, P],
+    "ref_frag": [P, P, P, P, P, C.c_uint64, P],
+    "ref_frag_fog": [P, P, P, P, P, C.c_uint64, P],
     "ref_radix_sort_chunk": [P, P, U32, U32],
     "ref_merge_sorted_chunks": [P, P, P, P, U32, U32],
     "ref_reverse_buffer": [P, U32, U32],
@@ -152,6 +155,31 @@ def unpack_vertices(verts: np.ndarray, dims, scale=(1.0, 1.0, 1.0), proj_view=No
     load().ref_unpack_vertices(_p(v), n, _p(_dims(dims)), _p(sc), _p(pv) if pv is not None else None, _p(world),
                                _p(clip) if clip is not None else None)
     return (world, clip) if clip is not None else world
+
+
+def vert_fog(verts: np.ndarray, dims, scale, eye):
+    """mc_isosurface.vert with DRAW_FOG per vertex: (world [n, 3], t_enter [n])."""
+    v = np.ascontiguousarray(verts, dtype=np.uint32).reshape(-1, 2)
+    n = len(v)
+    world = np.zeros((n, 3), np.float32)
+    te = np.zeros(n, np.float32)
+    sc = np.ascontiguousarray(np.asarray(scale, np.float32))
+    e = np.ascontiguousarray(np.asarray(eye, np.float32))
+    load().ref_vert_fog(_p(v), n, _p(_dims(dims)), _p(sc), _p(e), _p(world), _p(te))
+    return world, te
+
+
+def frag(world_pos, t_enter, eye, dfdx, dfdy, fog: bool) -> np.ndarray:
+    """mc_isosurface.frag per fragment (with DRAW_FOG when `fog`): rgba [n, 4]."""
+    wp = np.ascontiguousarray(world_pos, dtype=np.float32).reshape(-1, 3)
+    n = len(wp)
+    te = np.ascontiguousarray(np.asarray(t_enter, np.float32).reshape(n))
+    e = np.ascontiguousarray(np.asarray(eye, np.float32))
+    dx = np.ascontiguousarray(dfdx, dtype=np.float32).reshape(n, 3)
+    dy = np.ascontiguousarray(dfdy, dtype=np.float32).reshape(n, 3)
+    out = np.zeros((n, 4), np.float32)
+    (load().ref_frag_fog if fog else load().ref_frag)(_p(wp), _p(te), _p(e), _p(dx), _p(dy), n, _p(out))
+    return out
 
 
 def _next_pow2(a: int) -> int:

@@ -25,9 +25,11 @@ The rewrites (no semantic edits to the shader bodies):
   * float literals get an `f` suffix (GLSL literals are 32-bit)
   * swizzles `.xyz/.xy/.xz/.yz` -> glsl::swz_* helpers (`v.xyz = e` -> glsl::set_xyz)
   * vertex-stage `layout(location = n) in/out T x;` -> namespace-scope variables
-  * min/max/abs/ldexp/ceil -> glsl_* helpers, barrier() -> ref_barrier(), main -> main_
+  * `.rgb` -> `.xyz`, `.a` -> `.w`, `v.xyz += e` -> `v.xyz = v.xyz + (e)`
+  * min/max/abs/ldexp/ceil and the geometric/exponential built-ins and
+    dFdx/dFdy -> glsl_* helpers, barrier() -> ref_barrier(), main -> main_
   * compiled with the defines shaders/embed_shaders.py passes (BLOCK_SIZE=512,
-    SORT_CHUNK_SIZE=64)
+    SORT_CHUNK_SIZE=64), and DRAW_FOG for the fog variants of the render shaders
   * every program lives in its own namespace and translation unit
 
 Usage: python oracle/ref_build.py [--reference DIR]
@@ -56,8 +58,12 @@ PROGRAMS = {
     "compute_block_has_vertices": "compute_block_has_vertices.comp",
     "compute_block_voxel_num_verts": "compute_block_voxel_num_verts.comp",
     "compute_block_vertices": "compute_block_vertices.comp",
-    # the vertex stage's position math (the render pass itself is not run)
+    # the render pass's shaders: the vertex stage's position math, with DRAW_FOG
+    # also the fog entry distance, and the fragment shading with and without fog
     "mc_isosurface_vert": "mc_isosurface.vert",
+    "mc_isosurface_vert_fog": "mc_isosurface.vert",
+    "mc_isosurface_frag": "mc_isosurface.frag",
+    "mc_isosurface_frag_fog": "mc_isosurface.frag",
     # RadixSorter (js/radix_sort_by_key.js): chunk sort, merges, reverse
     "radix_sort_chunk": "radix_sort_chunk.comp",
     "merge_sorted_chunks": "merge_sorted_chunks.comp",
@@ -65,6 +71,8 @@ PROGRAMS = {
 }
 # what shaders/embed_shaders.py passes to every shader compile
 DEFINES = ["-DBLOCK_SIZE=512", "-DSORT_CHUNK_SIZE=64"]
+# per-program defines (js/bcmc.js builds the fog variant of the render pipeline with DRAW_FOG)
+PROGRAM_DEFINES = {"mc_isosurface_vert_fog": ["DRAW_FOG"], "mc_isosurface_frag_fog": ["DRAW_FOG"]}
 
 
 def reference_dir(arg: str | None) -> str:
@@ -137,10 +145,14 @@ def transform(text: str) -> str:
     # 32-bit float literals
     s = re.sub(r"(?<![\w.])(\d+\.\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])",
                r"\1f", s)
-    # swizzles and built-ins
+    # swizzles and built-ins (.rgb/.a are .xyz/.w; `v.xyz += e` assigns v.xyz + e)
+    s = re.sub(r"\.rgb\b", ".xyz", s)
+    s = re.sub(r"\b(\w+)\.a\b", r"\1.w", s)
+    s = re.sub(r"\b(\w+)\.xyz\s*\+=\s*([^;]+);", r"glsl::set_xyz(\1) = glsl::swz_xyz(\1) + (\2);", s)
     s = re.sub(r"\b(\w+)\.xyz\s*=(?!=)", r"glsl::set_xyz(\1) =", s)
     s = re.sub(r"\b(\w+)\.(xyz|xy|xz|yz)\b", r"glsl::swz_\2(\1)", s)
-    s = re.sub(r"\b(min|max|abs|ldexp|ceil)\s*\(", r"glsl_\1(", s)
+    s = re.sub(r"\b(min|max|abs|ldexp|ceil|dot|length|normalize|cross|clamp|pow|exp|dFdx|dFdy)\s*\(",
+               r"glsl_\1(", s)
     s = re.sub(r"\bbarrier\s*\(\s*\)", "ref_barrier()", s)
     s = re.sub(r"\bvoid\s+main\s*\(\s*(void)?\s*\)", "void main_()", s)
     return s
@@ -167,6 +179,8 @@ def generate(ref: str) -> list:
         with open(path, "w") as f:
             f.write(f"// generated from shaders/{fname} of the reference checkout by oracle/ref_build.py\n")
             f.write('#include "ref_shim.h"\n#undef UINT_MAX\n')
+            for d in PROGRAM_DEFINES.get(ns, []):
+                f.write(f"#define {d} 1\n")
             f.write(f"namespace p_{ns} {{\n{text}\n}}  // namespace p_{ns}\n")
             f.write(f'#define REF_PROGRAM_{ns} 1\n#include "tri_table.inc"\n#include "ref_glue.inc"\n')
         srcs.append(path)

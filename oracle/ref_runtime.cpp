@@ -18,6 +18,8 @@ uvec3 gl_GlobalInvocationID;
 uvec3 gl_LocalInvocationID;
 uvec3 gl_WorkGroupID;
 vec4 gl_Position;
+vec3 ref_dfdx;
+vec3 ref_dfdy;
 
 namespace {
 

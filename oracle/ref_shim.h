@@ -1,9 +1,10 @@
 // ref_shim.h -- TEST INFRASTRUCTURE ONLY.
 //
-// Just enough of GLSL 4.50 compute semantics, in C++20, to compile the
-// reference's own compute shaders (Twinklebear/webgpu-bcmc shaders/*.comp,
-// after the mechanical rewrites in ref_build.py) as host code, so that the
-// CPU oracle can be checked against the reference's shader source itself.
+// Just enough of GLSL 4.50 semantics, in C++20, to compile the reference's
+// own shaders (Twinklebear/webgpu-bcmc shaders/*.comp and the isosurface
+// vertex/fragment shaders, after the mechanical rewrites in ref_build.py) as
+// host code, so that the CPU oracle can be checked against the reference's
+// shader source itself.
 //
 // Semantics chosen to match how the reference runs (GLSL -> SPIR-V -> WGSL
 // under Dawn): uint/int are 32-bit and wrap (built with -fwrapv), f32
@@ -272,6 +273,14 @@ inline Swz2<Vec, 1, 2> swz_yz(Vec& v)
     return {v};
 }
 
+template <class T, int N>
+inline V<T, N> operator-(const V<T, N>& a)
+{
+    V<T, N> r;
+    for (int i = 0; i < N; ++i) r[i] = -a[i];
+    return r;
+}
+
 // GLSL min/max definitions: min(x, y) = y < x ? y : x, max(x, y) = x < y ? y : x
 template <class T>
 inline T min(T x, T y)
@@ -302,6 +311,21 @@ inline float glsl_abs(float x) { return std::fabs(x); }
 inline int glsl_abs(int x) { return x < 0 ? -x : x; }
 inline float glsl_ldexp(float x, int e) { return std::ldexp(x, e); }
 inline float glsl_ceil(float x) { return std::ceil(x); }
+inline float glsl_max(float x, int y) { return glsl::max(x, (float)y); }
+template <class T, int N>
+inline glsl::V<T, N> glsl_min(const glsl::V<T, N>& x, const glsl::V<T, N>& y)
+{
+    glsl::V<T, N> r;
+    for (int i = 0; i < N; ++i) r[i] = glsl::min(x[i], y[i]);
+    return r;
+}
+template <class T, int N>
+inline glsl::V<T, N> glsl_max(const glsl::V<T, N>& x, const glsl::V<T, N>& y)
+{
+    glsl::V<T, N> r;
+    for (int i = 0; i < N; ++i) r[i] = glsl::max(x[i], y[i]);
+    return r;
+}
 
 using glsl::all;
 using glsl::any;
@@ -324,6 +348,30 @@ typedef glsl::mat4 mat4;
 
 // vertex-stage built-in output
 extern vec4 gl_Position;
+
+// Geometric and exponential built-ins of the isosurface shaders, by their GLSL
+// definitions: dot sums the products in component order, length(x) =
+// sqrt(dot(x, x)), normalize(x) = x / length(x), clamp(x, a, b) =
+// min(max(x, a), b).
+inline float glsl_dot(const vec3& a, const vec3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline float glsl_length(const vec3& a) { return std::sqrt(glsl_dot(a, a)); }
+inline vec3 glsl_normalize(const vec3& a)
+{
+    const float l = glsl_length(a);
+    return vec3(a.x / l, a.y / l, a.z / l);
+}
+inline vec3 glsl_cross(const vec3& a, const vec3& b)
+{
+    return vec3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+inline float glsl_clamp(float x, float lo, float hi) { return glsl::min(glsl::max(x, lo), hi); }
+inline float glsl_pow(float x, float y) { return std::pow(x, y); }
+inline float glsl_exp(float x) { return std::exp(x); }
+// Screen-space derivatives of the fragment's world position: the harness sets
+// them for the fragment being shaded (one fragment runs at a time).
+extern vec3 ref_dfdx, ref_dfdy;
+inline vec3 glsl_dFdx(const vec3&) { return ref_dfdx; }
+inline vec3 glsl_dFdy(const vec3&) { return ref_dfdy; }
 
 // Invocation ids of the running invocation (set by the runtime before it
 // resumes each invocation) and the workgroup barrier.

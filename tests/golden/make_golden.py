@@ -13,8 +13,12 @@ reference's shaders produce for them:
   decode_rate<r>.npz random words and the reference decoder's output, bits
   unpack_ct44.npz    the vertex stage's world and clip positions of a mesh, bits
   sort.npz           RadixSorter.sort results (values, ascending and descending)
+  render_ct44.npz    the render shaders on the ct44 mesh: the fog vertex
+                     stage's t_enter per vertex, and the fragment shader's
+                     colour (with and without fog) at sampled fragments
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [name ...]
+(names: mc decode unpack sort render; default all)
 """
 from __future__ import annotations
 
@@ -108,17 +112,55 @@ def make_sort():
     np.savez_compressed(os.path.join(HERE, "sort.npz"), cases=np.int32(len(SORT_CASES)), **out)
 
 
-def main():
+RENDER_SCALE = (1.0, 0.9, 0.8)
+RENDER_EYE = (0.3, 0.4, 1.2)
+RENDER_FRAGMENTS = 400
+
+
+def make_render():
+    """mc_isosurface.vert (DRAW_FOG) per vertex of the ct44 mesh, and
+    mc_isosurface.frag at fragments inside its triangles (random barycentric
+    points; t_enter interpolated the same way; the world-position derivatives
+    are the triangle's edges, which span its plane as the screen derivatives
+    do)."""
+    g = np.load(os.path.join(HERE, "mc_ct44_r4.npz"))
+    verts = g["vertices_0"]
+    dims = tuple(int(d) for d in g["dims"])
+    world, te = R.vert_fog(verts, dims, RENDER_SCALE, RENDER_EYE)
+    rng = np.random.default_rng(77)
+    tri = rng.integers(0, len(verts) // 3, RENDER_FRAGMENTS)
+    bary = rng.dirichlet((1.0, 1.0, 1.0), RENDER_FRAGMENTS).astype(np.float32)
+    tw = world.reshape(-1, 3, 3)[tri]
+    wp = (bary[:, :, None] * tw).sum(1).astype(np.float32)
+    fte = (bary * te.reshape(-1, 3)[tri]).sum(1).astype(np.float32)
+    dx, dy = tw[:, 1] - tw[:, 0], tw[:, 2] - tw[:, 0]
+    rgba = R.frag(wp, fte, RENDER_EYE, dx, dy, False)
+    rgba_fog = R.frag(wp, fte, RENDER_EYE, dx, dy, True)
+    np.savez_compressed(os.path.join(HERE, "render_ct44.npz"), dims=np.asarray(dims, np.uint32),
+                        scale=np.asarray(RENDER_SCALE, np.float32), eye=np.asarray(RENDER_EYE, np.float32),
+                        t_enter_bits=te.view(np.uint32), frag_tri=tri.astype(np.uint32), frag_world=wp,
+                        frag_t_enter=fte, frag_rgba_bits=rgba.view(np.uint32),
+                        frag_rgba_fog_bits=rgba_fog.view(np.uint32))
+
+
+def main(names=None):
     O.build()
     if not R.available():
         sys.exit("oracle/_ref is not built (no reference checkout): cannot generate fixtures")
-    for name, spec in MC_CASES.items():
-        make_mc(name, *spec)
-    for rate in DECODE_RATES:
-        make_decode(rate)
-    make_unpack()
-    make_sort()
+    names = set(names or ["mc", "decode", "unpack", "sort", "render"])
+    if "mc" in names:
+        for name, spec in MC_CASES.items():
+            make_mc(name, *spec)
+    if "decode" in names:
+        for rate in DECODE_RATES:
+            make_decode(rate)
+    if "unpack" in names:
+        make_unpack()
+    if "sort" in names:
+        make_sort()
+    if "render" in names:
+        make_render()
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -31,7 +31,7 @@ from . import _lib
 from ._lib import BcmcError, check, dims3, scale3
 
 __all__ = ["Context", "CompressedMarchingCubes", "LRUCache", "ExclusiveScanPipeline", "ExclusiveScanner",
-           "StreamCompact", "RadixSorter", "DeviceArray", "BcmcError", "zfp_encode", "zfp_decode_volume",
+           "StreamCompact", "RadixSorter", "DeviceArray", "BcmcError", "zfp_encode", "zfp_decode_volume", "render",
            "zfp_block_ranges", "block_active", "stream_words", "Engine", "Server", "unpack_vertices"]
 
 
@@ -518,6 +518,36 @@ def unpack_vertices(ctx: Context, vertices, dims, scale=(1.0, 1.0, 1.0), proj_vi
                                            C.c_void_p(clip.data_ptr()) if clip is not None else None,
                                            C.c_void_p(_torch_stream())), ctx.handle)
     return (world, clip) if clip is not None else world
+
+
+def render(ctx: Context, vertices, n: int, dims, proj_view, eye_pos, width: int, height: int, scale=(1.0, 1.0, 1.0),
+           fog: bool = False, depth: bool = True, triangle: bool = True):
+    """The reference's render pass (js/bcmc.js:174-190,237-265,377-391 with
+    shaders/mc_isosurface.vert/.frag), headless: the first n packed vertices
+    of `vertices` (a CUDA tensor, 2 x u32 each) drawn as triangles into a
+    height x width image.  proj_view: 4x4 in column-major order (gl-matrix's
+    layout); eye_pos: the camera position.  Returns (rgba [h, w, 4] float32,
+    depth [h, w] float32 or None, triangle [h, w] int32 or None) as CUDA
+    tensors; row 0 is the top of the image, background (1, 1, 1, 1), depth 1.0
+    and triangle -1."""
+    t = _torch()
+    p = _lib.bcmc_render_params()
+    p.width, p.height = int(width), int(height)
+    m = np.asarray(proj_view, dtype=np.float32).reshape(16)
+    for i in range(16):
+        p.proj_view[i] = float(m[i])
+    for i in range(3):
+        p.eye_pos[i] = float(eye_pos[i])
+    p.fog = 1 if fog else 0
+    rgba = t.empty((height, width, 4), dtype=t.float32, device="cuda")
+    dep = t.empty((height, width), dtype=t.float32, device="cuda") if depth else None
+    tri = t.empty((height, width), dtype=t.int32, device="cuda") if triangle else None
+    check(_lib.load().bcmc_render(ctx.handle, C.c_void_p(_ptr(vertices) if n else 0), int(n), dims3(dims),
+                                  scale3(scale), C.byref(p), C.c_void_p(rgba.data_ptr()),
+                                  C.c_void_p(dep.data_ptr()) if dep is not None else None,
+                                  C.c_void_p(tri.data_ptr()) if tri is not None else None,
+                                  C.c_void_p(_torch_stream())), ctx.handle)
+    return rgba, dep, tri
 
 
 def zfp_block_ranges(ctx: Context, words, dims, rate: int):

@@ -66,6 +66,11 @@ class bcmc_tune_report(C.Structure):
                                           "decode_ms_tuned")]
 
 
+class bcmc_render_params(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("proj_view", C.c_float * 16),
+                ("eye_pos", C.c_float * 3), ("fog", C.c_int32)]
+
+
 class bcmc_server_opts(C.Structure):
     _fields_ = [("max_batch", C.c_uint32), ("max_wait_us", C.c_uint32)]
 
@@ -130,6 +135,7 @@ SIGNATURES = {
     "bcmc_scan_exclusive_u32_async": (C.c_int, [P, P, P, U32, P, P]),
     "bcmc_scan_exclusive_u32_noalloc": (C.c_int, [P, P, U32, P, P]),
     "bcmc_unpack_vertices": (C.c_int, [P, P, U64, U32P, C.POINTER(C.c_float), P, C.POINTER(C.c_float), P, P]),
+    "bcmc_render": (C.c_int, [P, P, U64, U32P, C.POINTER(C.c_float), C.POINTER(bcmc_render_params), P, P, P, P]),
     "bcmc_engine_create": (C.c_int, [P, C.POINTER(bcmc_engine_opts), C.POINTER(P)]),
     "bcmc_engine_destroy": (None, [P]),
     "bcmc_engine_add_volume": (C.c_int, [P, P, C.c_size_t, U32, U32P, U32P]),

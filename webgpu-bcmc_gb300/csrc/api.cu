@@ -1003,6 +1003,24 @@ bcmc_status bcmc_unpack_vertices(bcmc_ctx* ctx, const void* d_vertices, uint64_t
     });
 }
 
+bcmc_status bcmc_render(bcmc_ctx* ctx, const void* d_vertices, uint64_t n, const uint32_t dims[3],
+                        const float scale[3], const bcmc_render_params* params, float* d_rgba, float* d_depth,
+                        uint32_t* d_triangle, void* stream)
+{
+    if (!ctx || !dims || !dims[0] || !dims[1] || !dims[2] || !params || !d_rgba || (n && !d_vertices))
+        return BCMC_E_ARG;
+    if (params->width == 0 || params->height == 0 || params->width > 16384 || params->height > 16384)
+        return fail(ctx, BCMC_E_ARG, "render: width and height must be in [1, 16384]");
+    if (n / 3 > 0xffffffffull) return fail(ctx, BCMC_E_LIMIT, "render: more than 2^32-1 triangles");
+    if (reinterpret_cast<uintptr_t>(d_rgba) % 16 != 0 || (n && reinterpret_cast<uintptr_t>(d_vertices) % 8 != 0))
+        return fail(ctx, BCMC_E_ARG, "render: d_rgba must be 16-byte and d_vertices 8-byte aligned");
+    return guarded(ctx, [&]() -> bcmc_status {
+        render_launch(ctx, static_cast<const uint2*>(d_vertices), n, dims, scale, *params, d_rgba, d_depth, d_triangle,
+                      pick(ctx, stream));
+        return BCMC_OK;
+    });
+}
+
 bcmc_status bcmc_zfp_decode_volume(bcmc_ctx* ctx, const uint64_t* d_words, uint64_t nblocks, uint32_t rate,
                                    float* d_out, void* stream)
 {

@@ -50,6 +50,8 @@ void ensure_scratch(bcmc_ctx* ctx, size_t words);
 // ---- unpack.cu ----------------------------------------------------------------
 void unpack_launch(bcmc_ctx* ctx, const uint2* verts, uint64_t n, const uint32_t dims[3], const float scale[3],
                    const float* proj_view, float* world, float* clip, cudaStream_t s);
+void render_launch(bcmc_ctx* ctx, const uint2* verts, uint64_t n, const uint32_t dims[3], const float scale[3],
+                   const bcmc_render_params& p, float* rgba, float* depth, uint32_t* triangle, cudaStream_t s);
 
 // ---- engine.cu (for server.cu) ------------------------------------------------
 int engine_device(bcmc_engine* e);
