@@ -203,6 +203,45 @@ def decode_bench(ctx, flush, reps: int = 10) -> dict:
             "kernel": "k_decode_volume", "l2": "flushed (512 MB write) before each rep"}
 
 
+RENDER = dict(width=1920, height=1080, reps=20)
+
+
+def render_bench(mc, isos) -> dict:
+    """The render pass (bcmc_render) on the mesh of the middle isovalue of the
+    ct256 workload at 1920x1080, the reference's starting view (eye at +z,
+    50 degree field of view), with and without fog.  Each call returns after
+    its stream finished, so the host wall time per call is the frame time;
+    the launch list attributes it to the kernels."""
+    import torch
+
+    import bcmc
+    from bcmc import camera
+
+    iso = float(isos[len(isos) // 2])
+    mc.computeSurface(iso)
+    n = mc.stats()["lastNumVertices"]
+    vb = mc.vertexBuffer
+    w, h = RENDER["width"], RENDER["height"]
+    proj, eye = camera.default_view(w, h)
+    out = {"workload": f"ct256 mesh at iso {iso:g}: {n // 3} triangles, {w}x{h}, starting view",
+           "triangles": n // 3}
+    ctx = mc.ctx
+    for fog in (False, True):
+        for _ in range(3):
+            bcmc.render(ctx, vb, n, CONFIG["dims"], proj, eye, w, h, fog=fog)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(RENDER["reps"]):
+            t0 = time.perf_counter()
+            rgba, _, tri = bcmc.render(ctx, vb, n, CONFIG["dims"], proj, eye, w, h, fog=fog)
+            times.append(1000.0 * (time.perf_counter() - t0))
+        ms = float(np.median(times))
+        covered = int((tri >= 0).sum().item())
+        out["fog" if fog else "plain"] = {"ms": ms, "frames_per_s": 1000.0 / ms,
+                                          "mtriangles_per_s": n / 3 / ms / 1000.0, "covered_pixels": covered}
+    return out
+
+
 BATCH = dict(workload="c4: 256 queries over 8 resident volumes (32^3 blobs, 64^3 value noise, 96x128x80 "
                       "spectral, 128^3 blobs, 200^3 value noise, 256^3 spectral, 384x384x256 value noise, "
                       "512^3 spectral), ZFP rate 4, isovalues uniform within each volume's range",
@@ -559,6 +598,7 @@ def run_gb300(args):
     decode = decode_bench(ctx, flush) if not args.no_decode else None
     batched = batched_bench() if not args.no_batched else None
     served = served_bench() if not args.no_served else None
+    render = render_bench(mc, isos) if not args.no_render else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -588,6 +628,7 @@ def run_gb300(args):
                 "decode": decode,
                 "batched": batched,
                 "served": served,
+                "render": render,
                 "gpu_launches": int(launches),
                 "clocks": clk,
                 "volume_load_s": load_s,
@@ -607,6 +648,7 @@ def main():
     ap.add_argument("--no-decode", action="store_true", help="skip the full-volume decode leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-engine leg")
     ap.add_argument("--no-served", action="store_true", help="skip the served (continuous batching) leg")
+    ap.add_argument("--no-render", action="store_true", help="skip the render-pass leg")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

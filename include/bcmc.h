@@ -271,11 +271,12 @@ bcmc_status bcmc_unpack_vertices(bcmc_ctx* ctx, const void* d_vertices, uint64_t
  * (0.3, 0.3, 0.9) and a head light, and with `fog` the depth-cueing fog toward
  * white from where the eye ray enters the volume's box.  A triangle with a
  * vertex at clip w <= 1e-6 is not drawn (no near-plane clipping).
- * d_rgba: width*height*4 floats, row-major, 16-byte aligned; d_depth (may be NULL):
- * width*height floats; d_triangle (may be NULL): per pixel the index of the
- * triangle drawn there, 0xFFFFFFFF for background.  Allocates its working buffers (world and clip
- * positions, one 64-bit depth/triangle key per pixel) for the call's duration
- * and returns after the stream has finished the pass.
+ * d_rgba: width*height*4 floats, row-major, 16-byte aligned; d_depth (may be
+ * NULL): width*height floats; d_triangle (may be NULL): per pixel the index
+ * of the triangle drawn there, 0xFFFFFFFF for background.  The working
+ * buffers (world and clip positions, one 64-bit depth/triangle key per pixel)
+ * are the context's, grown on demand and kept; the call returns after the
+ * stream has finished the pass, so calls on one context must not overlap. 
  * No counterpart as a function in the reference, whose render pass is a
  * WebGPU render pipeline. */
 typedef struct bcmc_render_params {

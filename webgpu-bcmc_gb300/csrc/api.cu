@@ -100,6 +100,7 @@ static void ctx_release(bcmc_ctx* ctx)
     dev_free(ctx, ctx->d_prim, sizeof(QueryState));
     dev_free(ctx, ctx->d_status, ctx->status_words * 8);
     dev_free(ctx, ctx->d_scratch, ctx->scratch_words * 4);
+    dev_free(ctx, ctx->d_render, ctx->render_bytes);
     if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;

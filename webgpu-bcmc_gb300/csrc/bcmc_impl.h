@@ -23,6 +23,8 @@ struct bcmc_ctx {
     uint32_t* d_scratch = nullptr;  // sort ping-pong buffers for primitives
     size_t scratch_words = 0;
     uint32_t* h_pinned = nullptr;   // small pinned host staging
+    void* d_render = nullptr;       // render pass working buffers (grow-only)
+    size_t render_bytes = 0;
     uint64_t device_bytes = 0;
     // volumes and caches made from this context; bcmc_ctx_destroy defers the
     // release until the last of them is destroyed

@@ -296,30 +296,30 @@ void render_launch(bcmc_ctx* ctx, const uint2* verts, uint64_t n, const uint32_t
                    const bcmc_render_params& p, float* rgba, float* depth, uint32_t* triangle, cudaStream_t s)
 {
     const uint64_t ntri = n / 3, nv = ntri * 3, npix = (uint64_t)p.width * p.height;
-    float* world = nullptr;
-    float* clip = nullptr;
-    float* tenter = nullptr;
-    unsigned long long* keys = nullptr;
-    uint32_t* big = nullptr;  // ntri triangle indices, then the counter
-    auto release = [&]() {
-        cudaStreamSynchronize(s);
-        dev_free(ctx, world, nv * 12);
-        dev_free(ctx, clip, nv * 16);
-        dev_free(ctx, tenter, nv * 4);
-        dev_free(ctx, keys, npix * 8);
-        dev_free(ctx, big, (ntri + 1) * 4);
-    };
+    // working buffers, carved from one grow-only context allocation: world and
+    // clip positions, fog entry distances, the per-pixel keys, the list of
+    // large triangles and its counter
+    auto up = [](uint64_t b) { return (b + 255) & ~uint64_t(255); };
+    const uint64_t b_world = up(nv * 12), b_clip = up(nv * 16), b_tenter = p.fog ? up(nv * 4) : 0,
+                   b_keys = up(npix * 8), b_big = up((ntri + 1) * 4);
+    const uint64_t need = b_world + b_clip + b_tenter + b_keys + b_big;
+    if (need > ctx->render_bytes) {
+        dev_free(ctx, ctx->d_render, ctx->render_bytes);
+        ctx->d_render = nullptr;
+        ctx->render_bytes = 0;
+        ctx->d_render = dev_alloc(ctx, need);
+        ctx->render_bytes = need;
+    }
+    char* base = static_cast<char*>(ctx->d_render);
+    float* world = reinterpret_cast<float*>(base);
+    float* clip = reinterpret_cast<float*>(base + b_world);
+    float* tenter = p.fog ? reinterpret_cast<float*>(base + b_world + b_clip) : nullptr;
+    unsigned long long* keys = reinterpret_cast<unsigned long long*>(base + b_world + b_clip + b_tenter);
+    uint32_t* big = reinterpret_cast<uint32_t*>(base + b_world + b_clip + b_tenter + b_keys);
     try {
-        if (nv) {
-            world = (float*)dev_alloc(ctx, nv * 12);
-            clip = (float*)dev_alloc(ctx, nv * 16);
-            if (p.fog) tenter = (float*)dev_alloc(ctx, nv * 4);
-            big = (uint32_t*)dev_alloc(ctx, (ntri + 1) * 4);
-            BCMC_CUDA(cudaMemsetAsync(big + ntri, 0, 4, s));
-        }
-        keys = (unsigned long long*)dev_alloc(ctx, npix * 8);
         BCMC_CUDA(cudaMemsetAsync(keys, 0xff, npix * 8, s));
         if (nv) {
+            BCMC_CUDA(cudaMemsetAsync(big + ntri, 0, 4, s));
             unpack_launch(ctx, verts, nv, dims, scale, p.proj_view, world, clip, s);
             if (p.fog) {
                 const float3 half = make_float3((scale ? scale[0] : 1.0f) * 0.5f, (scale ? scale[1] : 1.0f) * 0.5f,
@@ -343,7 +343,7 @@ void render_launch(bcmc_ctx* ctx, const uint2* verts, uint64_t n, const uint32_t
         a.depth = depth;
         a.triangle = triangle;
         a.big = big;
-        a.nbig = reinterpret_cast<unsigned int*>(big ? big + ntri : nullptr);
+        a.nbig = reinterpret_cast<unsigned int*>(big + ntri);
         if (ntri) {
             k_raster<<<grid_of(ctx, ntri), 256, 0, s>>>(a);
             k_raster_big<<<ctx->num_sms * 4, 256, 0, s>>>(a);
@@ -352,11 +352,11 @@ void render_launch(bcmc_ctx* ctx, const uint2* verts, uint64_t n, const uint32_t
         k_resolve<<<grid_of(ctx, npix), 256, 0, s>>>(a);
         count_launches(1);
         BCMC_CUDA(cudaGetLastError());
+        BCMC_CUDA(cudaStreamSynchronize(s));  // the working buffers are free again when this returns
     } catch (...) {
-        release();
+        cudaStreamSynchronize(s);
         throw;
     }
-    release();
 }
 
 }  // namespace bcmc
