@@ -78,15 +78,22 @@ __device__ __forceinline__ uint64_t lb_pack(uint32_t epoch, uint64_t flag, uint3
     return ((((uint64_t)epoch << 2) | flag) << 32) | value;
 }
 
+// Status words are published with relaxed stores: a reader uses only the
+// flag and value carried in the word itself (never other data the writer
+// wrote before it), so no release fence is needed, and a fence per publish
+// would wait for every earlier store of the thread to reach L2.
 __device__ __forceinline__ void lb_store(uint64_t* p, uint64_t v)
 {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+// Read side of the same: a relaxed load.  (An acquire load would also order
+// every later load after it: the loads of a look-back window would complete
+// one after another instead of together.)
 __device__ __forceinline__ uint64_t lb_load(const uint64_t* p)
 {
     uint64_t v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
 
@@ -136,12 +143,15 @@ __device__ __forceinline__ uint32_t lookback_exclusive(uint64_t* status, uint32_
 }
 
 // Warp-cooperative look-back, called by all 32 lanes of one warp: each round
-// reads the status words of 32 predecessors at once, finds the nearest one
+// reads the status words of 32 * kPer predecessors at once (a round trip to
+// L2 costs microseconds when hundreds of tiles poll, so callers with many
+// tiles widen the window), finds the nearest one
 // holding an inclusive prefix with a ballot and sums the window with a warp
 // reduction, so a walk past k unfinished predecessors costs k/32 round trips.
 // Lane 0 publishes the aggregate first and the inclusive prefix at the end.
 // Returns the exclusive prefix in every lane.  A timed-out wait records
 // `site` in *err and stops the walk.
+template <int kPer = 4>
 __device__ __forceinline__ uint32_t warp_lookback(uint64_t* status, uint32_t tile, uint32_t aggregate,
                                                   uint32_t epoch, uint32_t* err, uint32_t site,
                                                   uint32_t stride = 1)
@@ -152,9 +162,8 @@ __device__ __forceinline__ uint32_t warp_lookback(uint64_t* status, uint32_t til
         return 0;
     }
     if (lane == 0) lb_store(status + (uint64_t)tile * stride, lb_pack(epoch, kFlagAggregate, aggregate));
-    // each lane owns 4 consecutive predecessors per round (nearest first):
-    // 128 status words per round trip
-    constexpr int kPer = 4;
+    // each lane owns kPer consecutive predecessors per round (nearest first):
+    // 32 * kPer status words per round trip
     uint32_t exclusive = 0;
     int64_t tail = (int64_t)tile - 1;
     uint32_t spins = 0;
@@ -208,13 +217,13 @@ __device__ __forceinline__ uint32_t warp_lookback(uint64_t* status, uint32_t til
     return exclusive;
 }
 
-// Per-thread look-back that keeps 8 predecessor loads in flight per round
+// Per-thread look-back that keeps W predecessor loads in flight per round
 // (used where every thread owns its own chain, e.g. one radix digit each).
+template <int W = 8>
 __device__ __forceinline__ uint32_t lookback_exclusive_w8(uint64_t* status, uint32_t tile, uint32_t aggregate,
                                                           uint32_t epoch, uint32_t* err, uint32_t site,
                                                           uint32_t stride)
 {
-    constexpr int W = 8;
     if (tile == 0) {
         lb_store(status, lb_pack(epoch, kFlagPrefix, aggregate));
         return 0;

@@ -72,6 +72,164 @@ constexpr int kSlotTile = kActThreads * kSlotItems;  // slots per k_slots tile
 
 __device__ __forceinline__ uint32_t spad8(uint32_t i) { return i + (i >> 5); }
 
+// The last tile of the active test: totals, and the cache growth decision.
+__device__ __forceinline__ void active_finish(QueryState* q, uint32_t A, uint32_t N, uint32_t total)
+{
+    q->num_active = A;
+    q->num_new = N;
+    const uint32_t old = q->cache_size;
+    uint32_t new_size = old;
+    if (A > 0 && N > 0) {
+        const uint32_t kept = A - N;
+        const uint32_t avail = old - kept;
+        if (avail < N) {  // js/lru_cache.js:519-522
+            uint64_t grown = (uint64_t)old + (3ull * (N - avail) + 1ull) / 2ull;
+            if (grown > total) grown = total;
+            new_size = align_up((uint32_t)grown, 32u);
+        }
+        q->display_slots_available = new_size - A;
+    }
+    q->old_cache_size = old;
+    q->new_cache_size = new_size;
+    if (new_size > q->capacity) {  // host grows the buffers and re-runs the query
+        q->grow_needed = new_size;
+        q->num_avail = 0;
+    } else {
+        q->cache_size = new_size;
+        q->num_avail = (A > 0 && N > 0) ? new_size - (A - N) : 0u;
+    }
+}
+
+// k_active over the block ranges (the MC path), 4 consecutive blocks per
+// thread, 1024 threads per tile.  The tile's ranges and all their 3x3x3 neighbours are
+// staged once in shared memory as 2-bit flags (bit 0: iso >= lo, bit 1:
+// iso <= hi): for each z-offset dz in {-1, 0, 1}, the window of block ids
+// [B0 + dz*NX*NY - NX - 1, B0 + 4096 + dz*NX*NY + NX + 1) around the tile's
+// blocks [B0, B0 + 4096) (stage_len = 4096 + 2*NX + 2 entries each).
+// Neighbour (dx, dy, dz) of local block l sits at
+// (dz+1)*stage_len + l + (dy+1)*NX + dx + 1.  Staging turns 27 dependent
+// global loads per block into one round of independent loads per tile, and
+// 4096-block tiles keep the look-back to one window at common sizes.
+constexpr int kActRThreads = 1024;
+constexpr int kActRItems = 4;                          // consecutive blocks per thread
+constexpr int kActRTile = kActRThreads * kActRItems;  // blocks per tile
+constexpr int kActRStage = 5;  // staged ranges per thread and window in one round (5 * 1024 >= 4096 + 2*NX + 2 for NX <= 511)
+
+__global__ void __launch_bounds__(kActRThreads, 1) k_active_ranges(QueryState* q, ActiveArgs a, uint32_t stage_len)
+{
+    __shared__ uint32_t s_warp[kActRThreads / 32 + 1];
+    __shared__ uint32_t s_tile, s_pa, s_pn;
+    extern __shared__ uint8_t s_bits[];  // 3 * stage_len flag bytes
+    const uint32_t total = a.total;
+    const uint32_t ntiles = div_up(total, kActRTile);
+    const uint32_t epoch = q->epoch;
+    const float iso = q->isovalue;
+    const uint3 nb = a.grid.nb;
+    const uint32_t nx = nb.x, nxy = nb.x * nb.y;
+    const uint32_t t = threadIdx.x;
+    for (;;) {
+        if (t == 0) s_tile = atomicAdd(&q->tiles_active, 1u);
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        if (tile >= ntiles) break;
+        // all of a thread's loads first (up to kActRStage per window, in
+        // flight together), then the flags
+        for (uint32_t i0 = 0; i0 < stage_len; i0 += kActRStage * kActRThreads) {
+            float2 r[3][kActRStage];
+#pragma unroll
+            for (int dz = 0; dz < 3; ++dz) {
+                const int64_t start = (int64_t)tile * kActRTile + (int64_t)(dz - 1) * nxy - nx - 1;
+#pragma unroll
+                for (int k = 0; k < kActRStage; ++k) {
+                    const uint32_t i = i0 + k * kActRThreads + t;
+                    const int64_t id = start + i;
+                    r[dz][k] = (i < stage_len && id >= 0 && id < (int64_t)total) ? __ldg(a.ranges + id)
+                                                                                 : make_float2(NAN, NAN);
+                }
+            }
+#pragma unroll
+            for (int dz = 0; dz < 3; ++dz)
+#pragma unroll
+                for (int k = 0; k < kActRStage; ++k) {
+                    const uint32_t i = i0 + k * kActRThreads + t;
+                    if (i < stage_len) {
+                        uint32_t ra, rb;
+                        range_bits(r[dz][k], iso, ra, rb);  // NaN (outside the volume): no flags
+                        s_bits[(uint32_t)dz * stage_len + i] = (uint8_t)(ra | (rb << 1));
+                    }
+                }
+        }
+        __syncthreads();
+        const uint32_t l0 = kActRItems * t, b0 = tile * kActRTile + l0;
+        uint32_t act = 0, need = 0;  // bit j = block b0 + j
+#pragma unroll
+        for (int j = 0; j < kActRItems; ++j) {
+            const uint32_t b = b0 + j, l = l0 + j;
+            if (b >= total) break;
+            const uint3 c = block_coords(b, a.grid);
+            // valid neighbour offsets per axis: bit (d + 1) for d in {-1, 0, 1}
+            const uint32_t mx = (c.x > 0 ? 1u : 0u) | 2u | (c.x + 1 < nb.x ? 4u : 0u);
+            const uint32_t my = (c.y > 0 ? 1u : 0u) | 2u | (c.y + 1 < nb.y ? 4u : 0u);
+            const uint32_t mz = (c.z > 0 ? 1u : 0u) | 2u | (c.z + 1 < nb.z ? 4u : 0u);
+            const uint32_t self = s_bits[stage_len + l + nx + 1];
+            uint32_t orv = 0, anyc = 0;
+#pragma unroll
+            for (int dz = 0; dz < 3; ++dz)
+#pragma unroll
+                for (int dy = 0; dy < 3; ++dy) {
+                    if (!((mz >> dz) & (my >> dy) & 1u)) continue;
+                    const uint8_t* row = s_bits + (uint32_t)dz * stage_len + l + (uint32_t)dy * nx;
+#pragma unroll
+                    for (int dx = 0; dx < 3; ++dx) {
+                        const uint32_t v = (mx >> dx) & 1u ? (uint32_t)row[dx] : 0u;
+                        orv |= v;
+                        anyc |= (v + 1u) >> 2;  // 1 when both flags are set
+                    }
+                }
+            // compute_block_active.comp:24-61 (see block_is_active)
+            act |= (((self & (orv >> 1)) | ((self >> 1) & orv) | anyc) & 1u) << j;
+        }
+        if (kActRItems == 4 && b0 + kActRItems <= total) {
+            *reinterpret_cast<uint4*>(a.active_out + b0) =
+                make_uint4(act & 1u, (act >> 1) & 1u, (act >> 2) & 1u, (act >> 3) & 1u);
+            if (act && a.item_slots) {
+                const int4 s4 = __ldg(reinterpret_cast<const int4*>(a.item_slots + b0));
+                need = ((s4.x < 0 ? 1u : 0u) | (s4.y < 0 ? 2u : 0u) | (s4.z < 0 ? 4u : 0u) | (s4.w < 0 ? 8u : 0u)) & act;
+            }
+        } else {
+            for (uint32_t j = 0; j < (uint32_t)kActRItems && b0 + j < total; ++j) {
+                a.active_out[b0 + j] = (act >> j) & 1u;
+                if ((act >> j & 1u) && a.item_slots && a.item_slots[b0 + j] < 0) need |= 1u << j;
+            }
+        }
+        uint32_t tot;
+        const uint32_t excl =
+            cta_exclusive_scan<kActRThreads>((uint32_t)__popc(act) | ((uint32_t)__popc(need) << 16), s_warp, &tot);
+        if (t < 32) {
+            const uint32_t p = warp_lookback(a.status_a, tile, tot & 0xffffu, epoch, &q->error, 30u);
+            if (t == 0) s_pa = p;
+        } else if (t < 64) {
+            const uint32_t p = warp_lookback(a.status_n, tile, tot >> 16, epoch, &q->error, 31u);
+            if (t == 32) s_pn = p;
+        }
+        __syncthreads();
+        uint32_t pa = s_pa + (excl & 0xffffu), pn = s_pn + (excl >> 16);
+#pragma unroll
+        for (int j = 0; j < kActRItems; ++j) {
+            if (act >> j & 1u) {
+                if (a.active_ids) a.active_ids[pa] = b0 + j;
+                ++pa;
+            }
+            if (need >> j & 1u) {
+                if (a.new_ids) a.new_ids[pn] = b0 + j;
+                ++pn;
+            }
+        }
+        if (tile == ntiles - 1 && t == 0) active_finish(q, s_pa + (tot & 0xffffu), s_pn + (tot >> 16), total);
+        __syncthreads();
+    }
+}
+
 __global__ void __launch_bounds__(kActThreads) k_active(QueryState* q, ActiveArgs a)
 {
     __shared__ uint32_t s_warp[kActThreads / 32 + 1];
@@ -138,32 +296,7 @@ __global__ void __launch_bounds__(kActThreads) k_active(QueryState* q, ActiveArg
                 ++pn;
             }
         }
-        if (tile == ntiles - 1 && threadIdx.x == 0) {
-            const uint32_t A = s_pa + (tot & 0xffffu), N = s_pn + (tot >> 16);
-            q->num_active = A;
-            q->num_new = N;
-            const uint32_t old = q->cache_size;
-            uint32_t new_size = old;
-            if (A > 0 && N > 0) {
-                const uint32_t kept = A - N;
-                const uint32_t avail = old - kept;
-                if (avail < N) {  // js/lru_cache.js:519-522
-                    uint64_t grown = (uint64_t)old + (3ull * (N - avail) + 1ull) / 2ull;
-                    if (grown > total) grown = total;
-                    new_size = align_up((uint32_t)grown, 32u);
-                }
-                q->display_slots_available = new_size - A;
-            }
-            q->old_cache_size = old;
-            q->new_cache_size = new_size;
-            if (new_size > q->capacity) {  // host grows the buffers and re-runs the query
-                q->grow_needed = new_size;
-                q->num_avail = 0;
-            } else {
-                q->cache_size = new_size;
-                q->num_avail = (A > 0 && N > 0) ? new_size - (A - N) : 0u;
-            }
-        }
+        if (tile == ntiles - 1 && threadIdx.x == 0) active_finish(q, s_pa + (tot & 0xffffu), s_pn + (tot >> 16), total);
         __syncthreads();
     }
 }
@@ -590,6 +723,16 @@ void query_begin_launch(QueryState* q, float iso, int mc_only, uint32_t capacity
 
 void active_launch(bcmc_ctx* ctx, QueryState* q, const ActiveArgs& a, cudaStream_t s)
 {
+    // the staged kernel within the 48 KB of dynamic shared memory a launch
+    // gets without opting in: 3 windows of kActRTile + 2*NX + 2 bytes
+    const uint32_t stage_len = kActRTile + 2u * a.grid.nb.x + 2u;
+    if (a.ranges && 3u * stage_len <= 48u * 1024u) {
+        k_active_ranges<<<pgrid(ctx, div_up(a.total, kActRTile), 2), kActRThreads, 3u * stage_len, s>>>(q, a,
+                                                                                                        stage_len);
+        count_launches(1);
+        BCMC_CUDA(cudaGetLastError());
+        return;
+    }
     k_active<<<pgrid(ctx, div_up(a.total, kActiveTile), 8), kActThreads, 0, s>>>(q, a);
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
