@@ -231,6 +231,10 @@ bcmc_status bcmc_sort_pairs_u32(bcmc_ctx* ctx, uint32_t* d_keys, uint32_t* d_val
                                 int reverse, void* stream);
 
 /* ---- ZFP fixed-rate float32 codec (shaders/zfp_decompress.comp) ---------- */
+/* d_words in the calls below is a device buffer of at least
+ * (blocks in the volume) * rate 64-bit words: block b occupies words
+ * [b*rate, (b+1)*rate).  There is no length argument -- the kernels read every
+ * block they are asked for -- so a shorter buffer is read out of bounds. */
 /* zfp_compute_block_range.comp:19-61: vec2(min,max) of every block over the
  * voxels inside dims. */
 bcmc_status bcmc_zfp_block_ranges(bcmc_ctx* ctx, const uint64_t* d_words, const uint32_t dims[3],

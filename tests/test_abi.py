@@ -67,3 +67,20 @@ def test_context_without_device_reports_an_error(lib_built):
     out = C.c_void_p()
     rc = L.bcmc_ctx_create(None, C.byref(out))
     assert rc in (1, 3) and not out.value
+
+
+def test_short_stream_is_refused_before_the_kernel():
+    """The decode wrappers check the device stream's length (the C calls take
+    none); a short buffer raises before anything is launched."""
+    import bcmc
+
+    class Fake:  # stands in for a device tensor: only its size is looked at
+        def numel(self):
+            return 10
+
+        def element_size(self):
+            return 8
+
+    with pytest.raises(ValueError):
+        bcmc._check_stream(Fake(), 8, 2)  # 8 blocks at rate 2 need 16 words
+    bcmc._check_stream(Fake(), 5, 2)

@@ -493,7 +493,17 @@ def zfp_encode(ctx: Context, field, rate: int):
     return words
 
 
+def _check_stream(words, nblocks: int, rate: int):
+    """The kernels read rate 64-bit words per block and take no length: refuse
+    a device stream shorter than that before it reaches them."""
+    have = int(words.numel()) * int(words.element_size()) if hasattr(words, "numel") else None
+    if have is not None and have < int(nblocks) * int(rate) * 8:
+        raise ValueError(f"compressed stream holds {have} bytes; {nblocks} blocks at rate {rate} need "
+                         f"{int(nblocks) * int(rate) * 8}")
+
+
 def zfp_decode_volume(ctx: Context, words, nblocks: int, rate: int):
+    _check_stream(words, nblocks, rate)
     t = _torch()
     out = t.empty(nblocks * 64, dtype=t.float32, device="cuda")
     check(_lib.load().bcmc_zfp_decode_volume(ctx.handle, C.c_void_p(_ptr(words)), int(nblocks), int(rate),
@@ -553,6 +563,7 @@ def render(ctx: Context, vertices, n: int, dims, proj_view, eye_pos, width: int,
 def zfp_block_ranges(ctx: Context, words, dims, rate: int):
     t = _torch()
     nb = int(np.prod([(d + 3) // 4 for d in dims]))
+    _check_stream(words, nb, rate)
     out = t.empty(2 * nb, dtype=t.float32, device="cuda")
     check(_lib.load().bcmc_zfp_block_ranges(ctx.handle, C.c_void_p(_ptr(words)), dims3(dims), int(rate),
                                             C.c_void_p(out.data_ptr()), C.c_void_p(_torch_stream())), ctx.handle)
