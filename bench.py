@@ -242,7 +242,7 @@ def render_bench(mc, isos) -> dict:
     return out
 
 
-BATCH = dict(workload="c4: 256 queries over 8 resident volumes (32^3 blobs, 64^3 value noise, 96x128x80 "
+BATCH = dict(workload="256 queries over 8 resident volumes (32^3 blobs, 64^3 value noise, 96x128x80 "
                       "spectral, 128^3 blobs, 200^3 value noise, 256^3 spectral, 384x384x256 value noise, "
                       "512^3 spectral), ZFP rate 4, isovalues uniform within each volume's range",
              volumes=[("blobs", (32, 32, 32)), ("ct_like", (64, 64, 64)), ("turbulence", (96, 128, 80)),
@@ -338,7 +338,7 @@ def batched_bench(reps: int = 5) -> dict:
             "latency_note": "a batch's queries all complete when the batch does: per-query latency = batch wall time"}
 
 
-SERVED = dict(workload="c5: 1024x1024x1080 uint16-range value noise (~60% background blocks, 17,694,720 blocks) "
+SERVED = dict(workload="1024x1024x1080 uint16-range value noise (~60% background blocks, 17,694,720 blocks) "
                        "+ 256^3 value noise, 320^3 blobs, 384^3 spectral, 512^3 value noise; ZFP rate 4; Poisson "
                        "arrivals, volume weighted by size, isovalue uniform in its range; 40 GB slot pool",
               big=(1024, 1024, 1080),

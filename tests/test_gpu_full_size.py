@@ -97,7 +97,7 @@ def test_c5_block_offsets_past_2_24(ctx, oracle):
     for i, b in enumerate(sample):
         want = oracle.decode_block(host, b, max_bits)
         assert np.array_equal(got[i].view(np.uint32), want.view(np.uint32)), b
-        # all C5 blocks are whole (dims multiples of 4): the range folds the 64
+        # all blocks of this volume are whole (dims multiples of 4): the range folds the 64
         # values in block order into (1e20, -1e20) with GLSL min/max
         # (zfp_compute_block_range.comp:47-59)
         lo, hi = np.float32(1e20), np.float32(-1e20)

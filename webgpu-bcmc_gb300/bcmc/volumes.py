@@ -93,7 +93,7 @@ def open_dataset(key: str, root: str, device=0):
     return mc, ds
 
 
-# The seeded synthetic volumes of bcmc.datasets (configurations C1-C3); the
+# The seeded synthetic volumes of bcmc.datasets (64^3 blobs, 256^3 CT-like, 512^3 spectral); the
 # files themselves are written by write_synthetic().
 register("blobs64", Dataset("blobs64_64x64x64_float32.gen.crate8", 8, (0.0, 1.5)))
 register("ct256", Dataset("ct256_256x256x256_float32.gen.crate4", 4, (20.0, 255.0)))
