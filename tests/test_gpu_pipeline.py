@@ -84,6 +84,15 @@ def test_ct256_config(ctx, oracle):
     _run(ctx, oracle, f, (256, 256, 256), 4, np.linspace(30.0, 220.0, 16), 0.5, check_state=False)
 
 
+def test_rows_wider_than_the_staged_active_test(ctx, oracle):
+    """24,600 voxels in x (6,150 blocks per row): the active test's shared-memory
+    windows would exceed 48 KB, so the row-load kernel runs instead."""
+    dims = (24600, 8, 4)
+    f = D.blobs(dims, 9, n_blobs=40)
+    isos = np.linspace(float(f.min()), float(f.max()), 5)[1:-1]
+    _run(ctx, oracle, f, dims, 4, isos, 0.5)
+
+
 def test_empty_and_full_queries(ctx, oracle):
     f = D.blobs((32, 32, 32), 4)
     _run(ctx, oracle, f, (32, 32, 32), 4, [1e9, -1e9, float(np.median(f)), 1e9], 0.05)
