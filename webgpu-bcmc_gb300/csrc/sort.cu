@@ -46,13 +46,20 @@ __global__ void __launch_bounds__(256) k_sort_hist(QueryState* q, const uint32_t
     const uint32_t n = d_n ? *d_n : n_host;
     for (int i = threadIdx.x; i < 1024; i += 256) h[i] = 0;
     __syncthreads();
-    for (uint32_t i = blockIdx.x * 256u + threadIdx.x; i < n; i += gridDim.x * 256u) {
-        uint32_t k = keys[i];
+    // one shared atomic per distinct digit and warp: keys such as cache-slot
+    // ages take few distinct values, and per-key atomics on them serialise
+    for (uint32_t i0 = blockIdx.x * 256u; i0 < n; i0 += gridDim.x * 256u) {
+        const uint32_t i = i0 + threadIdx.x;
+        const bool valid = i < n;
+        uint32_t k = valid ? keys[i] : 0u;
         if (reverse) k = ~k;
-        atomicAdd(&h[k & 255u], 1u);
-        atomicAdd(&h[256 + ((k >> 8) & 255u)], 1u);
-        atomicAdd(&h[512 + ((k >> 16) & 255u)], 1u);
-        atomicAdd(&h[768 + (k >> 24)], 1u);
+#pragma unroll
+        for (int d = 0; d < 4; ++d) {
+            const uint32_t digit = valid ? (k >> (8 * d)) & 255u : 256u;
+            const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+            if (valid && (threadIdx.x & 31u) == (uint32_t)__ffs(peers) - 1u)
+                atomicAdd(&h[256 * d + digit], (uint32_t)__popc(peers));
+        }
     }
     __syncthreads();
     uint32_t* gh = &q->sort_hist[0][0];
@@ -65,9 +72,11 @@ __global__ void __launch_bounds__(256) k_sort_hist(QueryState* q, const uint32_t
     if (!is_last) return;
     __threadfence();
     // plan: which digit passes run, bucket offsets, buffer ping-pong
-    uint32_t run[4];
+    uint32_t run[4], hv[4];
+#pragma unroll
+    for (int d = 0; d < 4; ++d) hv[d] = __ldcg(gh + d * 256 + threadIdx.x);  // all four in flight
     for (int d = 0; d < 4; ++d) {
-        const uint32_t v = __ldcg(gh + d * 256 + threadIdx.x);
+        const uint32_t v = hv[d];
         const int full = __syncthreads_or(n > 0 && v == n);
         run[d] = (n > 0 && !full) ? 1u : 0u;
         uint32_t tot;
