@@ -373,8 +373,9 @@ struct bcmc_vol {
     // the query as one CUDA graph: inputs copied from pinned memory, state
     // copied back to pinned memory; re-captured when a buffer is regrown
     QueryInputs* h_in = nullptr;  // pinned
-    cudaGraphExec_t graph = nullptr;
-    uint64_t graph_key[4]{};
+    // [0]: without the stage-timing events, [1]: with them (a perf tracker)
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    uint64_t graph_key[2][4]{};
     uint64_t graph_kernels = 0;
 };
 
@@ -394,7 +395,8 @@ static void vol_free(bcmc_vol* v)
     lru_delete(v->lru);
     for (auto& e : v->ev)
         if (e) cudaEventDestroy(e);
-    if (v->graph) cudaGraphExecDestroy(v->graph);
+    for (auto& g : v->graph)
+        if (g) cudaGraphExecDestroy(g);
     if (v->h_in) cudaFreeHost(v->h_in);
     delete v;
     ctx_child_removed(ctx);
@@ -564,7 +566,7 @@ bcmc_status bcmc_volume_create_device(bcmc_ctx* ctx, const void* d_zfp, size_t l
 void bcmc_volume_destroy(bcmc_vol* v) { vol_free(v); }
 
 // The kernels of one query, in order, on stream s (captured into the graph).
-static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_state)
+static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_state, bool events)
 {
     bcmc_ctx* ctx = v->ctx;
     bcmc_lru* c = v->lru;
@@ -577,30 +579,31 @@ static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_s
     SlotArgs sa{v->active, c->slot_age, c->slot_avail, c->slot_item, c->avail_ids, c->avail_keys, c->st_slots, 1u};
     AssignArgs as{c->new_ids, c->sort_bv, c->sort_cv, c->slot_age, c->slot_avail, c->slot_item,
                   c->item_slots, v->words, v->max_bits, reinterpret_cast<float*>(c->cache)};
-    BCMC_CUDA(cudaEventRecordWithFlags(v->ev[0], s, cudaEventRecordExternal));
+    if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[0], s, cudaEventRecordExternal));
     query_begin_launch(c->q, iso, 0, c->capacity, v->vert_capacity, s, from_state);
     active_launch(ctx, c->q, aa, s);
-    BCMC_CUDA(cudaEventRecordWithFlags(v->ev[1], s, cudaEventRecordExternal));
+    if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[1], s, cudaEventRecordExternal));
     slots_launch(ctx, c->q, sa, c->capacity, s);
     sort_launch(ctx, c->q, &c->q->num_avail, c->capacity, lru_sort_buffers(c), 1, s);
-    BCMC_CUDA(cudaEventRecordWithFlags(v->ev[2], s, cudaEventRecordExternal));
+    if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[2], s, cudaEventRecordExternal));
     assign_launch(ctx, c->q, as, v->total, s);
-    BCMC_CUDA(cudaEventRecordWithFlags(v->ev[3], s, cudaEventRecordExternal));
+    if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[3], s, cudaEventRecordExternal));
     mc_launch(ctx, c->q, ma, v->total, s);
-    BCMC_CUDA(cudaEventRecordWithFlags(v->ev[4], s, cudaEventRecordExternal));
+    if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[4], s, cudaEventRecordExternal));
     BCMC_CUDA(cudaMemcpyAsync(c->h_q, c->q, sizeof(QueryState), cudaMemcpyDeviceToHost, s));
 }
 
 // Captures the query into a CUDA graph if the buffers it refers to changed.
-static void vol_ensure_graph(bcmc_vol* v)
+static void vol_ensure_graph(bcmc_vol* v, int events)
 {
     bcmc_lru* c = v->lru;
     const uint64_t key[4] = {c->capacity, v->vert_capacity, (uint64_t)(uintptr_t)v->verts,
                              (uint64_t)(uintptr_t)c->cache};
-    if (v->graph && std::memcmp(key, v->graph_key, sizeof(key)) == 0) return;
-    if (v->graph) {
-        cudaGraphExecDestroy(v->graph);
-        v->graph = nullptr;
+    cudaGraphExec_t& graph = v->graph[events];
+    if (graph && std::memcmp(key, v->graph_key[events], sizeof(key)) == 0) return;
+    if (graph) {
+        cudaGraphExecDestroy(graph);
+        graph = nullptr;
     }
     cudaStream_t s = v->ctx->stream;
     const uint64_t before = g_kernel_launches.load();
@@ -608,20 +611,20 @@ static void vol_ensure_graph(bcmc_vol* v)
     cudaGraph_t g = nullptr;
     try {
         BCMC_CUDA(cudaMemcpyAsync(&c->q->in, v->h_in, sizeof(QueryInputs), cudaMemcpyHostToDevice, s));
-        vol_enqueue_query(v, s, 0.0f, 1);
+        vol_enqueue_query(v, s, 0.0f, 1, events != 0);
     } catch (...) {
         cudaStreamEndCapture(s, &g);
         if (g) cudaGraphDestroy(g);
         throw;
     }
     BCMC_CUDA(cudaStreamEndCapture(s, &g));
-    const cudaError_t e = cudaGraphInstantiate(&v->graph, g, 0);
+    const cudaError_t e = cudaGraphInstantiate(&graph, g, 0);
     cudaGraphDestroy(g);
     BCMC_CUDA(e);
     // captured launches did not run: count them per replay instead
     v->graph_kernels = g_kernel_launches.load() - before;
     g_kernel_launches.fetch_sub(v->graph_kernels);
-    std::memcpy(v->graph_key, key, sizeof(key));
+    std::memcpy(v->graph_key[events], key, sizeof(key));
 }
 
 bcmc_status bcmc_compute_surface(bcmc_vol* v, float iso, bcmc_perf* perf, uint32_t* num_vertices)
@@ -632,10 +635,11 @@ bcmc_status bcmc_compute_surface(bcmc_vol* v, float iso, bcmc_perf* perf, uint32
         bcmc_lru* c = v->lru;
         cudaStream_t s = ctx->stream;
         for (int attempt = 0;; ++attempt) {
-            vol_ensure_graph(v);
+            const int with_events = perf ? 1 : 0;
+            vol_ensure_graph(v, with_events);
             lru_epoch_tick(c, s);
             *v->h_in = QueryInputs{iso, c->capacity, v->vert_capacity, 0u};
-            BCMC_CUDA(cudaGraphLaunch(v->graph, s));
+            BCMC_CUDA(cudaGraphLaunch(v->graph[with_events], s));
             count_launches(v->graph_kernels);
             BCMC_CUDA(cudaStreamSynchronize(s));
             if (c->h_q->error) return fail(ctx, BCMC_E_TIMEOUT, "device wait timed out (site " + std::to_string(c->h_q->error) + ")");
