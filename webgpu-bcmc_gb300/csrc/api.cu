@@ -580,7 +580,7 @@ static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_s
     AssignArgs as{c->new_ids, c->sort_bv, c->sort_cv, c->slot_age, c->slot_avail, c->slot_item,
                   c->item_slots, v->words, v->max_bits, reinterpret_cast<float*>(c->cache)};
     if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[0], s, cudaEventRecordExternal));
-    query_begin_launch(c->q, iso, 0, c->capacity, v->vert_capacity, s, from_state);
+    query_begin_launch(c->q, iso, 0, c->capacity, v->vert_capacity, s, from_state ? v->h_in : nullptr);
     active_launch(ctx, c->q, aa, s);
     if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[1], s, cudaEventRecordExternal));
     slots_launch(ctx, c->q, sa, c->capacity, s);
@@ -590,7 +590,7 @@ static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_s
     if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[3], s, cudaEventRecordExternal));
     mc_launch(ctx, c->q, ma, v->total, s);
     if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[4], s, cudaEventRecordExternal));
-    BCMC_CUDA(cudaMemcpyAsync(c->h_q, c->q, sizeof(QueryState), cudaMemcpyDeviceToHost, s));
+    query_end_launch(c->q, c->h_q, s);
 }
 
 // Captures the query into a CUDA graph if the buffers it refers to changed.
@@ -610,7 +610,6 @@ static void vol_ensure_graph(bcmc_vol* v, int events)
     BCMC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     cudaGraph_t g = nullptr;
     try {
-        BCMC_CUDA(cudaMemcpyAsync(&c->q->in, v->h_in, sizeof(QueryInputs), cudaMemcpyHostToDevice, s));
         vol_enqueue_query(v, s, 0.0f, 1, events != 0);
     } catch (...) {
         cudaStreamEndCapture(s, &g);

@@ -18,8 +18,8 @@ constexpr uint32_t kSpinLimit = 1u << 22;  // bounded device-side waits
 // query is a fixed sequence of launches with no host round trip in between;
 // the host reads this struct once at the end of the query.
 // ---------------------------------------------------------------------------
-// Inputs of one query as the host writes them (pinned memory, copied in by the
-// first node of a query's CUDA graph).
+// Inputs of one query as the host writes them (pinned memory, read directly by
+// the first kernel of a query's CUDA graph).
 struct QueryInputs {
     float isovalue;
     uint32_t capacity;
@@ -28,7 +28,6 @@ struct QueryInputs {
 };
 
 struct QueryState {
-    QueryInputs in;  // copy of the host inputs (graph launches)
     // inputs written by the host (or the query-init kernel)
     float isovalue;
     uint32_t epoch;          // tags the decoupled-lookback status words

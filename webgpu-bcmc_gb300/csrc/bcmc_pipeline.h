@@ -62,7 +62,8 @@ struct McArgs {
 };
 
 void query_begin_launch(QueryState* q, float iso, int mc_only, uint32_t capacity, uint32_t vert_capacity,
-                        cudaStream_t s, int from_state = 0);
+                        cudaStream_t s, const QueryInputs* in = nullptr);
+void query_end_launch(const QueryState* q, QueryState* host, cudaStream_t s);
 void active_launch(bcmc_ctx* ctx, QueryState* q, const ActiveArgs& a, cudaStream_t s);
 void slots_launch(bcmc_ctx* ctx, QueryState* q, const SlotArgs& a, uint32_t max_slots, cudaStream_t s);
 void assign_launch(bcmc_ctx* ctx, QueryState* q, const AssignArgs& a, uint32_t max_new, cudaStream_t s);

@@ -28,17 +28,18 @@
 
 namespace bcmc {
 
-// Starts a query: inputs come from the arguments, or, when `from_state` is
-// set, from q->in (written by the graph's host-to-device copy).
+// Starts a query: inputs come from the arguments, or, when `in` is set, from
+// the host's pinned copy, read directly (a query graph reuses the pointer and
+// needs no copy node for its inputs).
 __global__ void k_query_begin(QueryState* q, float iso, int mc_only, uint32_t capacity, uint32_t vert_capacity,
-                              int from_state)
+                              const QueryInputs* in)
 {
     const int t = threadIdx.x;
-    if (from_state) {
-        iso = q->in.isovalue;
-        mc_only = (int)q->in.mc_only;
-        capacity = q->in.capacity;
-        vert_capacity = q->in.vert_capacity;
+    if (in) {
+        iso = __ldcv(&in->isovalue);
+        mc_only = (int)__ldcv(&in->mc_only);
+        capacity = __ldcv(&in->capacity);
+        vert_capacity = __ldcv(&in->vert_capacity);
     }
     if (t == 0) {
         q->epoch += 1;
@@ -59,6 +60,22 @@ __global__ void k_query_begin(QueryState* q, float iso, int mc_only, uint32_t ca
     }
     if (!mc_only)
         for (int i = t; i < 1024; i += blockDim.x) (&q->sort_hist[0][0])[i] = 0;
+}
+
+// Ends a query graph: the query state into the host's pinned copy (stores
+// to mapped host memory from one CTA instead of a copy node).
+__global__ void k_query_end(const QueryState* q, QueryState* host)
+{
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(q);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(host);
+    for (uint32_t i = threadIdx.x; i < sizeof(QueryState) / 4; i += blockDim.x) dst[i] = __ldcg(src + i);
+}
+
+void query_end_launch(const QueryState* q, QueryState* host, cudaStream_t s)
+{
+    k_query_end<<<1, 256, 0, s>>>(q, host);
+    count_launches(1);
+    BCMC_CUDA(cudaGetLastError());
 }
 
 // ---------------------------------------------------------------------------
@@ -714,9 +731,9 @@ static int pgrid(bcmc_ctx* ctx, uint32_t tiles, uint32_t per_sm)
 }
 
 void query_begin_launch(QueryState* q, float iso, int mc_only, uint32_t capacity, uint32_t vert_capacity,
-                        cudaStream_t s, int from_state)
+                        cudaStream_t s, const QueryInputs* in)
 {
-    k_query_begin<<<1, 256, 0, s>>>(q, iso, mc_only, capacity, vert_capacity, from_state);
+    k_query_begin<<<1, 256, 0, s>>>(q, iso, mc_only, capacity, vert_capacity, in);
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
 }
