@@ -11,7 +11,8 @@ Lines printed (one JSON line on rank 0):
   value   iso-queries/s, volume resident in HBM, timed with CUDA events on the
           library's stream (L2 flushed with a 512 MB write between steps);
           computeSurface is called without a perf tracker, as by default
-  e2e     the same through the C ABI with a host copy of every vertex buffer
+  e2e     the same through the C ABI with every query's vertices delivered
+          into pinned host memory (bcmc_compute_surface_host)
   roofline  the dominant kernel's algorithmic bytes / its CUDA-event time,
           from a second timed pass with a perf tracker (its stage events
           slow each query down, so the headline pass runs without them)
@@ -520,12 +521,15 @@ def run_gb300(args):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
     L = bcmc._lib.load()
 
-    def step(perf=None, copy_out=None, lat=None):
+    def step(perf=None, copy_out=None, lat=None, to_host=None):
         mc.lruCache.reset()
         n_tot = 0
         for iso in isos:
             t_q = time.perf_counter()
-            n = mc.computeSurface(float(iso), perf)
+            if to_host is not None:
+                n = mc.computeSurfaceToHost(float(iso), to_host)
+            else:
+                n = mc.computeSurface(float(iso), perf)
             if lat is not None:
                 lat.append(1000.0 * (time.perf_counter() - t_q))
             if copy_out is not None:
@@ -577,19 +581,27 @@ def run_gb300(args):
         ms = float(t.item())
     value = world * len(isos) / (ms / 1000.0)
 
-    # e2e: every query's vertex buffer copied to pinned host memory
+    # e2e: every query's vertices in pinned host memory, through the C ABI:
+    # bcmc_compute_surface_host (the kernels store the vertices into the host
+    # buffer), and for comparison bcmc_compute_surface + bcmc_copy_vertices
     vmax = 1 << 24
     pinned = torch.empty((vmax, 2), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
-    e2e_times, d2h = [], 0
-    for _ in range(args.steps):
-        flush.fill_(1)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        n_tot = step(None, pinned)
-        e2e_times.append(time.perf_counter() - t0)
-        d2h = n_tot * 8
-    e2e_ms = 1000.0 * float(np.mean(e2e_times))
-    e2e_value = world * len(isos) / (e2e_ms / 1000.0)
+
+    def e2e_pass(**kw):
+        times, d2h = [], 0
+        for _ in range(max(args.warmup, 3)):
+            step(**kw)
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            n_tot = step(**kw)
+            times.append(time.perf_counter() - t0)
+            d2h = n_tot * 8
+        return world * len(isos) / float(np.mean(times)), d2h
+
+    e2e_value, d2h = e2e_pass(to_host=pinned)
+    e2e_copy_value, _ = e2e_pass(copy_out=pinned)
 
     # roofline of the dominant stage (CUDA-event stage times of the stage pass)
     stages = ("computeActiveBlocks", "cacheUpdate", "decompression", "computeVertices")
@@ -631,7 +643,11 @@ def run_gb300(args):
                 "config": {"workload": CONFIG["workload"], "l2": "flushed (512 MB write) between steps",
                            "parallelism": f"replicas x{world}"},
                 "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": 4 * len(isos),
-                        "d2h_bytes_per_step": d2h},
+                        "d2h_bytes_per_step": d2h,
+                        "what": "bcmc_compute_surface_host per query: vertices stored into pinned host memory "
+                                "by the kernels (host wall time per step)",
+                        "compute_then_copy": {"value": e2e_copy_value,
+                                              "what": "bcmc_compute_surface + bcmc_copy_vertices per query"}},
                 "roofline": {"bound": "hbm", "kernel": kernel_of[dominant], "achieved": achieved, "peak": peak,
                              "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                              "traffic": NCU_TRAFFIC.get(kernel_of[dominant]), "avg_launch_ms": avg_ms,

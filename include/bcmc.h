@@ -102,14 +102,30 @@ typedef struct {
 
 /* computeSurface(isovalue, perfTracker) -> numVertices
  * (js/compressed_marching_cubes.js:580-809).  Blocks until the vertex count is
- * known.  `perf` may be NULL (no per-stage timing). */
+ * known.  `perf` may be NULL (no per-stage timing); passing one adds the
+ * stage-timing events to the query (some tens of microseconds). */
 bcmc_status bcmc_compute_surface(bcmc_vol* vol, float isovalue, bcmc_perf* perf,
                                  uint32_t* num_vertices);
+
+/* The same query with the vertices written by the kernels straight into host
+ * memory: host_vertices must be page-locked (cudaMallocHost or
+ * cudaHostRegister) and 8-byte aligned, with room for `capacity` vertices.
+ * The device-to-host transfer overlaps the vertex computation, which a
+ * bcmc_compute_surface + bcmc_copy_vertices pair runs one after the other.
+ * The volume's device vertex buffer is not written: bcmc_vertices and
+ * bcmc_copy_vertices return BCMC_E_STATE until the next bcmc_compute_surface.
+ * When the query has more than `capacity` vertices, returns BCMC_E_LIMIT with
+ * *num_vertices set to the count needed (the buffer's contents are then
+ * unspecified); the cache state has advanced as for a completed query.
+ * No counterpart in the reference, whose vertices stay in a GPU buffer. */
+bcmc_status bcmc_compute_surface_host(bcmc_vol* vol, float isovalue, void* host_vertices, uint64_t capacity,
+                                      uint32_t* num_vertices);
 
 /* The vertex buffer (this.vertexBuffer, :781-784): numVertices entries of
  * 8 bytes, {uint32 packed 10:10:10 position within the block, uint32 block id}
  * (compute_block_vertices.comp:164).  The pointer stays valid until the next
- * bcmc_compute_surface on this volume. */
+ * bcmc_compute_surface on this volume; BCMC_E_STATE after a
+ * bcmc_compute_surface_host. */
 bcmc_status bcmc_vertices(bcmc_vol* vol, const void** d_vertices, uint64_t* bytes);
 /* Copies the vertex buffer into host memory (bytes <= 8*numVertices). */
 bcmc_status bcmc_copy_vertices(bcmc_vol* vol, void* host, uint64_t bytes);

@@ -109,3 +109,37 @@ def test_perf_tracker_and_memory_report(ctx, oracle):
     assert len(perf["computeVertices"]) == 2 and perf["totalBlocks"] == 512
     mc_text, cache_text, total, use = mc.reportMemoryUse()
     assert "compressedData" in mc_text and "cache" in cache_text and use["cache"]["cache"] > 0
+
+
+def test_surface_straight_to_host(ctx, oracle):
+    """computeSurfaceToHost gives the same vertices as computeSurface +
+    copyVertices, refuses a buffer that is too small (reporting the size
+    needed) and pageable memory, and leaves the cache state as a normal query."""
+    import torch
+
+    dims = (64, 64, 64)
+    f = D.blobs(dims, 1)
+    w = oracle.zfp_encode(f, 8)
+    stream = w.view(np.uint8)[: 4096 * 64].copy()
+    a = bcmc.CompressedMarchingCubes(bcmc.Context(ctx.device, initial_cache_fraction=0.3))
+    a.setCompressedVolume(stream, 8, dims)
+    b = bcmc.CompressedMarchingCubes(bcmc.Context(ctx.device, initial_cache_fraction=0.3))
+    b.setCompressedVolume(stream, 8, dims)
+    pinned = torch.empty((1 << 20, 2), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    for iso in (0.5, 0.3, 0.9, 5.0, 0.5):
+        n = a.computeSurface(iso)
+        want = a.copyVertices().copy()
+        m = b.computeSurfaceToHost(iso, pinned)
+        assert m == n
+        assert np.array_equal(pinned[:m], want), iso
+        assert a.stats() == b.stats()
+        assert np.array_equal(a.lruCache.state()["item_slots"], b.lruCache.state()["item_slots"])
+    with pytest.raises(bcmc.BcmcError):
+        b.vertexBuffer  # noqa: B018 -- the last query went to host memory
+    n = a.computeSurface(0.5)
+    small = pinned[:10]
+    with pytest.raises(bcmc.BcmcError):
+        b.computeSurfaceToHost(0.5, small)
+    with pytest.raises(bcmc.BcmcError):
+        b.computeSurfaceToHost(0.5, np.zeros((n, 2), np.uint32))  # pageable
+    assert b.computeSurface(0.5) == n and np.array_equal(b.copyVertices(), a.copyVertices())

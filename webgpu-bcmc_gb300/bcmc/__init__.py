@@ -275,6 +275,20 @@ class CompressedMarchingCubes:
             perfTracker["computeVertices"].append(perf.computeVertices)
         return int(n.value)
 
+    def computeSurfaceToHost(self, isovalue: float, out: np.ndarray) -> int:
+        """computeSurface with the vertices written by the kernels straight into
+        `out`, a page-locked host array (e.g. from torch.empty(...,
+        pin_memory=True).numpy()) of shape (capacity, 2) uint32: the transfer
+        overlaps the vertex computation.  Returns the vertex count; raises
+        BcmcError (BCMC_E_LIMIT) when the query has more vertices than `out`
+        holds.  The device vertexBuffer is not written by this call."""
+        if out.dtype.itemsize * out.size < 8 or out.ctypes.data % 8:
+            raise ValueError("out must be an 8-byte aligned array of packed vertices")
+        n = C.c_uint32()
+        check(_lib.load().bcmc_compute_surface_host(self._vol, float(isovalue), out.ctypes.data_as(C.c_void_p),
+                                                    out.nbytes // 8, C.byref(n)), self.ctx.handle)
+        return int(n.value)
+
     def stats(self) -> dict:
         s = _lib.bcmc_stats()
         check(_lib.load().bcmc_stats_get(self._vol, C.byref(s)), self.ctx.handle)

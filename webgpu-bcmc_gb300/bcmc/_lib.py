@@ -119,6 +119,7 @@ SIGNATURES = {
     "bcmc_volume_create_device": (C.c_int, [P, P, C.c_size_t, U32, U32P, C.POINTER(C.c_float), C.POINTER(P)]),
     "bcmc_volume_destroy": (None, [P]),
     "bcmc_compute_surface": (C.c_int, [P, C.c_float, C.POINTER(bcmc_perf), U32P]),
+    "bcmc_compute_surface_host": (C.c_int, [P, C.c_float, P, U64, C.POINTER(U32)]),
     "bcmc_vertices": (C.c_int, [P, C.POINTER(P), C.POINTER(U64)]),
     "bcmc_copy_vertices": (C.c_int, [P, P, U64]),
     "bcmc_stats_get": (C.c_int, [P, C.POINTER(bcmc_stats)]),

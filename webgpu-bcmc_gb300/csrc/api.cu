@@ -373,9 +373,11 @@ struct bcmc_vol {
     // the query as one CUDA graph: inputs copied from pinned memory, state
     // copied back to pinned memory; re-captured when a buffer is regrown
     QueryInputs* h_in = nullptr;  // pinned
-    // [0]: without the stage-timing events, [1]: with them (a perf tracker)
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    uint64_t graph_key[2][4]{};
+    // [0]: without the stage-timing events, [1]: with them (a perf tracker),
+    // [2]: vertices written straight into a page-locked host buffer
+    cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+    uint64_t graph_key[3][4]{};
+    bool last_on_host = false;  // the last query's vertices went to host memory only
     uint64_t graph_kernels = 0;
 };
 
@@ -566,7 +568,7 @@ bcmc_status bcmc_volume_create_device(bcmc_ctx* ctx, const void* d_zfp, size_t l
 void bcmc_volume_destroy(bcmc_vol* v) { vol_free(v); }
 
 // The kernels of one query, in order, on stream s (captured into the graph).
-static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_state, bool events)
+static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_state, bool events, uint2* out)
 {
     bcmc_ctx* ctx = v->ctx;
     bcmc_lru* c = v->lru;
@@ -575,7 +577,7 @@ static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_s
     ActiveArgs aa{reinterpret_cast<const float2*>(v->ranges), nb, grid, nullptr, v->active, c->item_slots,
                   v->total, v->active_ids, c->new_ids, c->st_active_a, c->st_active_n};
     McArgs ma{v->active, v->active_ids, c->item_slots, reinterpret_cast<const float*>(c->cache), nb, grid,
-              v->with_verts, v->vert_offsets, v->block_counts, v->verts, c->st_mc_v, c->st_mc_b};
+              v->with_verts, v->vert_offsets, v->block_counts, out, c->st_mc_v, c->st_mc_b};
     SlotArgs sa{v->active, c->slot_age, c->slot_avail, c->slot_item, c->avail_ids, c->avail_keys, c->st_slots, 1u};
     AssignArgs as{c->new_ids, c->sort_bv, c->sort_cv, c->slot_age, c->slot_avail, c->slot_item,
                   c->item_slots, v->words, v->max_bits, reinterpret_cast<float*>(c->cache)};
@@ -594,13 +596,16 @@ static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_s
 }
 
 // Captures the query into a CUDA graph if the buffers it refers to changed.
-static void vol_ensure_graph(bcmc_vol* v, int events)
+// mode 0/1: the volume's vertex buffer without/with stage events; mode 2: the
+// vertices go to `out` (the device address of a page-locked host buffer).
+static void vol_ensure_graph(bcmc_vol* v, int mode, uint2* out = nullptr)
 {
     bcmc_lru* c = v->lru;
-    const uint64_t key[4] = {c->capacity, v->vert_capacity, (uint64_t)(uintptr_t)v->verts,
+    if (mode != 2) out = v->verts;
+    const uint64_t key[4] = {c->capacity, mode == 2 ? 0u : v->vert_capacity, (uint64_t)(uintptr_t)out,
                              (uint64_t)(uintptr_t)c->cache};
-    cudaGraphExec_t& graph = v->graph[events];
-    if (graph && std::memcmp(key, v->graph_key[events], sizeof(key)) == 0) return;
+    cudaGraphExec_t& graph = v->graph[mode];
+    if (graph && std::memcmp(key, v->graph_key[mode], sizeof(key)) == 0) return;
     if (graph) {
         cudaGraphExecDestroy(graph);
         graph = nullptr;
@@ -610,7 +615,7 @@ static void vol_ensure_graph(bcmc_vol* v, int events)
     BCMC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     cudaGraph_t g = nullptr;
     try {
-        vol_enqueue_query(v, s, 0.0f, 1, events != 0);
+        vol_enqueue_query(v, s, 0.0f, 1, mode == 1, out);
     } catch (...) {
         cudaStreamEndCapture(s, &g);
         if (g) cudaGraphDestroy(g);
@@ -623,22 +628,26 @@ static void vol_ensure_graph(bcmc_vol* v, int events)
     // captured launches did not run: count them per replay instead
     v->graph_kernels = g_kernel_launches.load() - before;
     g_kernel_launches.fetch_sub(v->graph_kernels);
-    std::memcpy(v->graph_key[events], key, sizeof(key));
+    std::memcpy(v->graph_key[mode], key, sizeof(key));
 }
 
-bcmc_status bcmc_compute_surface(bcmc_vol* v, float iso, bcmc_perf* perf, uint32_t* num_vertices)
+// One query: into the volume's vertex buffer (host_out null), or straight
+// into a page-locked host buffer of host_cap vertices (host_out = its device
+// address).
+static bcmc_status vol_query(bcmc_vol* v, float iso, bcmc_perf* perf, uint32_t* num_vertices, uint2* host_out,
+                             uint64_t host_cap)
 {
-    if (!v) return BCMC_E_ARG;
     bcmc_ctx* ctx = v->ctx;
     return guarded(ctx, [&]() -> bcmc_status {
         bcmc_lru* c = v->lru;
         cudaStream_t s = ctx->stream;
+        const int mode = host_out ? 2 : (perf ? 1 : 0);
+        const uint32_t out_cap = host_out ? (uint32_t)std::min<uint64_t>(host_cap, 0xffffffffull) : v->vert_capacity;
         for (int attempt = 0;; ++attempt) {
-            const int with_events = perf ? 1 : 0;
-            vol_ensure_graph(v, with_events);
+            vol_ensure_graph(v, mode, host_out);
             lru_epoch_tick(c, s);
-            *v->h_in = QueryInputs{iso, c->capacity, v->vert_capacity, 0u};
-            BCMC_CUDA(cudaGraphLaunch(v->graph[with_events], s));
+            *v->h_in = QueryInputs{iso, c->capacity, out_cap, 0u};
+            BCMC_CUDA(cudaGraphLaunch(v->graph[mode], s));
             count_launches(v->graph_kernels);
             BCMC_CUDA(cudaStreamSynchronize(s));
             if (c->h_q->error) return fail(ctx, BCMC_E_TIMEOUT, "device wait timed out (site " + std::to_string(c->h_q->error) + ")");
@@ -654,6 +663,14 @@ bcmc_status bcmc_compute_surface(bcmc_vol* v, float iso, bcmc_perf* perf, uint32
                   make_block_grid(nb), v->with_verts, v->vert_offsets, v->block_counts, v->verts, c->st_mc_v,
                   c->st_mc_b};
         QueryState& h = *c->h_q;
+        v->last_on_host = host_out != nullptr;
+        if (host_out && h.num_active > 0 && h.num_verts > 0 && h.vert_overflow) {
+            // the host buffer is the caller's: report the size it needs
+            if (num_vertices) *num_vertices = h.num_verts;
+            c->cache_size = h.cache_size;
+            return fail(ctx, BCMC_E_LIMIT, "the host buffer holds " + std::to_string(host_cap) + " vertices; the query has " +
+                                               std::to_string(h.num_verts));
+        }
         if (h.num_active > 0 && h.num_verts > 0 && h.vert_overflow) {
             vol_grow_verts(v, h.num_verts);
             lru_begin(c, s, iso, 1, v->vert_capacity);
@@ -703,9 +720,30 @@ bcmc_status bcmc_compute_surface(bcmc_vol* v, float iso, bcmc_perf* perf, uint32
     });
 }
 
+bcmc_status bcmc_compute_surface(bcmc_vol* v, float iso, bcmc_perf* perf, uint32_t* num_vertices)
+{
+    if (!v) return BCMC_E_ARG;
+    return vol_query(v, iso, perf, num_vertices, nullptr, 0);
+}
+
+bcmc_status bcmc_compute_surface_host(bcmc_vol* v, float iso, void* host_vertices, uint64_t capacity,
+                                      uint32_t* num_vertices)
+{
+    if (!v || !host_vertices || capacity == 0 || reinterpret_cast<uintptr_t>(host_vertices) % 8 != 0)
+        return BCMC_E_ARG;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, host_vertices) != cudaSuccess || at.type != cudaMemoryTypeHost ||
+        !at.devicePointer) {
+        cudaGetLastError();
+        return fail(v->ctx, BCMC_E_ARG, "the host buffer must be page-locked (cudaMallocHost or cudaHostRegister)");
+    }
+    return vol_query(v, iso, nullptr, num_vertices, static_cast<uint2*>(at.devicePointer), capacity);
+}
+
 bcmc_status bcmc_vertices(bcmc_vol* v, const void** d_vertices, uint64_t* bytes)
 {
     if (!v || !d_vertices || !bytes) return BCMC_E_ARG;
+    if (v->last_on_host) return fail(v->ctx, BCMC_E_STATE, "the last query wrote its vertices to host memory");
     *d_vertices = v->verts;
     *bytes = (uint64_t)v->stats.lastNumVertices * 8u;
     return BCMC_OK;
@@ -715,6 +753,7 @@ bcmc_status bcmc_copy_vertices(bcmc_vol* v, void* host, uint64_t bytes)
 {
     if (!v || (!host && bytes)) return BCMC_E_ARG;
     if (bytes > (uint64_t)v->stats.lastNumVertices * 8u) return fail(v->ctx, BCMC_E_ARG, "more bytes than vertices");
+    if (v->last_on_host && bytes) return fail(v->ctx, BCMC_E_STATE, "the last query wrote its vertices to host memory");
     if (bytes == 0) return BCMC_OK;
     return guarded(v->ctx, [&]() -> bcmc_status {
         BCMC_CUDA(cudaMemcpyAsync(host, v->verts, bytes, cudaMemcpyDeviceToHost, v->ctx->stream));
