@@ -61,8 +61,8 @@ uint64_t engine_vertex_budget(bcmc_engine* e);
 bcmc_ctx* engine_ctx(bcmc_engine* e);
 
 // ---- sort.cu ----------------------------------------------------------------
-constexpr int kSortThreads = 256;
-constexpr int kSortItems = 16;
+constexpr int kSortThreads = 512;
+constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 keys per tile
 // Plan + onesweep passes over n (device-resident) pairs.  Input arrays are in
 // natural order; the first pass applies the reference's tie-order permutation

@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(QueryState* q, const
 {
     __shared__ uint32_t s_keys[kSortTile];
     __shared__ uint32_t s_vals[kSortTile];
-    __shared__ uint32_t s_whist[kSortThreads / 32][256];
+    __shared__ uint16_t s_whist[kSortThreads / 32][256];  // per warp and digit: < 2^16
     __shared__ uint32_t s_start[256];
     __shared__ uint32_t s_gbase[256];
     __shared__ uint32_t s_warp_sums[kSortThreads / 32 + 1];
@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(QueryState* q, const
             const uint32_t peers = __match_any_sync(0xffffffffu, digit);
             const uint32_t cnt = digit < 256u ? s_whist[warp][digit] : 0u;
             __syncwarp();
-            if (digit < 256u && lane == __ffs(peers) - 1) s_whist[warp][digit] = cnt + __popc(peers);
+            if (digit < 256u && lane == __ffs(peers) - 1) s_whist[warp][digit] = (uint16_t)(cnt + __popc(peers));
             __syncwarp();
             rank[j] = cnt + __popc(peers & lt_mask);
         }
@@ -162,17 +162,21 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(QueryState* q, const
         // thread t owns digit t: warp-exclusive offsets and the tile count
         const uint32_t t = threadIdx.x;
         uint32_t run = 0;
+        if (t < 256) {
 #pragma unroll
-        for (int w = 0; w < kSortThreads / 32; ++w) {
-            const uint32_t c = s_whist[w][t];
-            s_whist[w][t] = run;
-            run += c;
+            for (int w = 0; w < kSortThreads / 32; ++w) {
+                const uint32_t c = s_whist[w][t];
+                s_whist[w][t] = (uint16_t)run;
+                run += c;
+            }
         }
         uint32_t tile_total;
         const uint32_t start = cta_exclusive_scan<kSortThreads>(run, s_warp_sums, &tile_total);
-        s_start[t] = start;
-        const uint32_t excl = lookback_exclusive_w8(b.status + t, tile, run, epoch, &q->error, 20u + pass, 256u);
-        s_gbase[t] = bucket[t] + excl - start;
+        if (t < 256) {
+            s_start[t] = start;
+            const uint32_t excl = lookback_exclusive_w8(b.status + t, tile, run, epoch, &q->error, 20u + pass, 256u);
+            s_gbase[t] = bucket[t] + excl - start;
+        }
         __syncthreads();
 #pragma unroll
         for (int j = 0; j < kSortItems; ++j) {
