@@ -61,6 +61,25 @@ static __constant__ uint16_t c_ghost[61] = {
 static __constant__ uint8_t c_nb_off[7] = {1, 2, 4, 3, 5, 6, 7};
 enum { kNbX = 0, kNbY, kNbZ, kNbXY, kNbXZ, kNbYZ, kNbXYZ, kNbSelf };
 
+// Ghost voxel c_ghost[gi] decoded for the loads: bits 0-2 the axes on which
+// it lies in a neighbour (its coordinate 4 there), bits 3-8 its voxel in that
+// neighbour's block, bits 9-15 its index in the 5^3 grid, bits 16+ which
+// neighbour (kNb*).  MC kernels decode the table once per CTA.
+__device__ __forceinline__ uint32_t ghost_desc(uint32_t g)
+{
+    const uint32_t gx = g & 15u, gy = (g >> 4) & 15u, gz = (g >> 8) & 15u;
+    const uint32_t need = (gx == 4u ? 1u : 0u) | (gy == 4u ? 2u : 0u) | (gz == 4u ? 4u : 0u);
+    const uint32_t src = (gx & 3u) + 4u * ((gy & 3u) + 4u * (gz & 3u));
+    return need | (src << 3) | ((gx + 5u * (gy + 5u * gz)) << 9) | ((g >> 12) << 16);
+}
+
+// The axes on which a grid of `dims` (block_dims_with_ghost) takes the
+// neighbour's layer: ghost voxel d is in the grid when (d & 7 & ~axes) == 0.
+__device__ __forceinline__ uint32_t ghost_axes(uint32_t dims)
+{
+    return ((dims & 15u) == 5u ? 1u : 0u) | (((dims >> 4) & 15u) == 5u ? 2u : 0u) | ((dims >> 8) == 5u ? 4u : 0u);
+}
+
 // compute_vertex_values.comp:96-156: grid extent of the block plus the ghost
 // layer taken from active +x/+y/+z neighbours, tested corner, edges, faces.
 // `act` has bit k set when neighbour k exists and is active.

@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
     __shared__ uint32_t s_act[kMcBlocks];
     __shared__ uint32_t s_warp[kMcThreads / 32 + 1];
     __shared__ uint32_t s_n, s_pv, s_pb, s_cta_v, s_cta_b, s_rank, s_cursor;
-    __shared__ uint16_t s_ghost[64];
+    __shared__ uint32_t s_gdesc[64];  // ghost_desc of each ghost voxel
     __shared__ uint8_t s_nb_off[8];
 
     const uint32_t A = q->num_active;
@@ -483,7 +483,7 @@ __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
         s_cta_v = s_cta_b = 0;
         s_cursor = start;
     }
-    if (t < 61) s_ghost[t] = c_ghost[t];
+    if (t < 61) s_gdesc[t] = ghost_desc(c_ghost[t]);
     if (t < 7) s_nb_off[t] = c_nb_off[t];
     const uint32_t j = t >> 4, u = t & 15u, ry = u & 3u, rz = u >> 2;
     const uint32_t lane = t & 31u;
@@ -522,7 +522,7 @@ __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
             float4 v4 = make_float4(0.f, 0.f, 0.f, 0.f);
             if (slot < slots) v4 = __ldg(reinterpret_cast<const float4*>(a.cache + (uint64_t)slot * 64u) + u);
             else atomicCAS(&q->error, 0u, 51u);
-            const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
+            const uint32_t has = ghost_axes(dims);
             float gv[4];
             uint32_t gaddr[4];
 #pragma unroll
@@ -531,13 +531,12 @@ __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
                 gv[r] = 0.0f;
                 gaddr[r] = 0xffffffffu;
                 if (gi < 61) {
-                    const uint32_t g = s_ghost[gi];
-                    const uint32_t gx = g & 15u, gy = (g >> 4) & 15u, gz = (g >> 8) & 15u;
-                    if (gx < dx && gy < dy && gz < dz) {
-                        const uint32_t nslot = s_slot[j][g >> 12];
+                    const uint32_t d = s_gdesc[gi];
+                    if ((d & 7u & ~has) == 0u) {
+                        const uint32_t nslot = s_slot[j][d >> 16];
                         if (nslot < slots) {
-                            gv[r] = __ldg(a.cache + (uint64_t)nslot * 64u + (gx & 3u) + 4u * ((gy & 3u) + 4u * (gz & 3u)));
-                            gaddr[r] = gx + 5u * (gy + 5u * gz);
+                            gv[r] = __ldg(a.cache + (uint64_t)nslot * 64u + ((d >> 3) & 63u));
+                            gaddr[r] = (d >> 9) & 127u;
                         } else {
                             atomicCAS(&q->error, 0u, 52u);
                         }
