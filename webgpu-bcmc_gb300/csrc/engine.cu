@@ -328,6 +328,7 @@ __global__ void __launch_bounds__(kThreads) k_decode_probe(const uint64_t* __res
 __global__ void __launch_bounds__(kBmcThreads, kBmcPerSm) k_bmc(BatchArgs a)
 {
     __shared__ float s_vol[kBmcBlocks][128];
+    __shared__ uint8_t s_rm[kBmcBlocks][32];  // corner-row masks of each block (count_cells)
     __shared__ __align__(16) uint8_t s_te[256][16];
     __shared__ __align__(16) uint8_t s_cnt[256];
     __shared__ __align__(16) uint8_t s_case[kBmcCells];
@@ -444,15 +445,22 @@ __global__ void __launch_bounds__(kBmcThreads, kBmcPerSm) k_bmc(BatchArgs a)
         const uint32_t dx = dims & 15u, dy = (dims >> 4) & 15u, dz = dims >> 8;
         const bool row_ok = s_id[j] != 0xffffffffu && ry + 1 < dy && rz + 1 < dz;
         const float iso = s_iso[j];
-        uint32_t rm[4];
+        // the 25 corner rows (y, z) of the block's grid, row y + 5z, two per
+        // thread of the block's 16 (one warp half): masks of value <= iso
 #pragma unroll
-        for (uint32_t r = 0; r < 4; ++r) {
-            const float* p = &s_vol[j][5u * ((ry + (r & 1u)) + 5u * (rz + (r >> 1)))];
-            uint32_t m = 0;
+        for (uint32_t h = 0; h < 2; ++h) {
+            const uint32_t i = u + 16u * h;
+            if (i < 25u) {
+                const float* p = &s_vol[j][5u * i];
+                uint32_t m = 0;
 #pragma unroll
-            for (uint32_t x = 0; x < 5; ++x) m |= (p[x] <= iso ? 1u : 0u) << x;
-            rm[r] = m;
+                for (uint32_t x = 0; x < 5; ++x) m |= (p[x] <= iso ? 1u : 0u) << x;
+                s_rm[j][i] = (uint8_t)m;
+            }
         }
+        __syncwarp();
+        const uint32_t r0 = ry + 5u * rz;
+        const uint32_t rm[4] = {s_rm[j][r0], s_rm[j][r0 + 1u], s_rm[j][r0 + 5u], s_rm[j][r0 + 6u]};
         uint32_t sum = 0;
         cs4 = 0;
 #pragma unroll
