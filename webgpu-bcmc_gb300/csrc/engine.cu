@@ -329,6 +329,7 @@ __global__ void __launch_bounds__(kBmcThreads, kBmcPerSm) k_bmc(BatchArgs a)
 {
     __shared__ float s_vol[kBmcBlocks][128];
     __shared__ uint8_t s_rm[kBmcBlocks][32];  // corner-row masks of each block (count_cells)
+    __shared__ uint32_t s_pair[32], s_pair_sw[32];  // 5-bit row mask -> per-cell corner pairs
     __shared__ __align__(16) uint8_t s_te[256][16];
     __shared__ __align__(16) uint8_t s_cnt[256];
     __shared__ __align__(16) uint8_t s_case[kBmcCells];
@@ -364,6 +365,17 @@ __global__ void __launch_bounds__(kBmcThreads, kBmcPerSm) k_bmc(BatchArgs a)
         s_cursor = start;
     }
     if (t < 61) s_gdesc[t] = ghost_desc(c_ghost[t]);
+    if (t < 32) {
+        uint32_t w = 0, ws = 0;
+#pragma unroll
+        for (uint32_t x = 0; x < 4; ++x) {
+            const uint32_t pr = (t >> x) & 3u;
+            w |= pr << (8u * x);
+            ws |= (((pr & 1u) << 1) | (pr >> 1)) << (8u * x);
+        }
+        s_pair[t] = w;
+        s_pair_sw[t] = ws;
+    }
     if (t < 7) s_nb_off[t] = c_nb_off[t];
     const uint32_t j = t >> 4, u = t & 15u, ry = u & 3u, rz = u >> 2;
     const uint32_t lane = t & 31u;
@@ -460,20 +472,18 @@ __global__ void __launch_bounds__(kBmcThreads, kBmcPerSm) k_bmc(BatchArgs a)
         }
         __syncwarp();
         const uint32_t r0 = ry + 5u * rz;
-        const uint32_t rm[4] = {s_rm[j][r0], s_rm[j][r0 + 1u], s_rm[j][r0 + 5u], s_rm[j][r0 + 6u]};
+        // the four cases at once, one byte per cell: s_pair[m] puts bits x and
+        // x+1 of a row mask into byte x, s_pair_sw the same pair swapped; the
+        // corner order of the case (compute_vertex_values.comp:48-57) is
+        // (x,y,z) (x+1,y,z) (x+1,y+1,z) (x,y+1,z), then the same at z+1
+        cs4 = s_pair[s_rm[j][r0]] | (s_pair_sw[s_rm[j][r0 + 1u]] << 2) | (s_pair[s_rm[j][r0 + 5u]] << 4) |
+              (s_pair_sw[s_rm[j][r0 + 6u]] << 6);
+        // cells past the grid (the last one when dims.x is 4) or in rows past it: no case
+        cs4 &= row_ok ? (dx == 5u ? 0xffffffffu : 0x00ffffffu) : 0u;
         uint32_t sum = 0;
-        cs4 = 0;
 #pragma unroll
         for (uint32_t x = 0; x < 4; ++x) {
-            uint32_t cs = 0;
-            nv[x] = 0;
-            if (row_ok && x + 1 < dx) {
-                const uint32_t a0 = rm[0] >> x, a1 = rm[1] >> x, a2 = rm[2] >> x, a3 = rm[3] >> x;
-                cs = (a0 & 3u) | ((a1 & 2u) << 1) | ((a1 & 1u) << 3) | ((a2 & 3u) << 4) | ((a3 & 2u) << 5) |
-                     ((a3 & 1u) << 7);
-                nv[x] = s_cnt[cs];
-            }
-            cs4 |= cs << (8u * x);
+            nv[x] = s_cnt[(cs4 >> (8u * x)) & 255u];
             sum += nv[x];
         }
         return sum;
