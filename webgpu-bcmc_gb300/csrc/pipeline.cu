@@ -62,18 +62,21 @@ __global__ void k_query_begin(QueryState* q, float iso, int mc_only, uint32_t ca
         for (int i = t; i < 1024; i += blockDim.x) (&q->sort_hist[0][0])[i] = 0;
 }
 
-// Ends a query graph: the query state into the host's pinned copy (stores
-// to mapped host memory from one CTA instead of a copy node).
+// Ends a query graph: the query state the host reads (the fields before the
+// sort histograms) into the host's pinned copy, stored to mapped host memory
+// by one warp instead of a copy node.
+constexpr uint32_t kHostStateWords = offsetof(QueryState, sort_hist) / 4;
+
 __global__ void k_query_end(const QueryState* q, QueryState* host)
 {
     const uint32_t* src = reinterpret_cast<const uint32_t*>(q);
     uint32_t* dst = reinterpret_cast<uint32_t*>(host);
-    for (uint32_t i = threadIdx.x; i < sizeof(QueryState) / 4; i += blockDim.x) dst[i] = __ldcg(src + i);
+    for (uint32_t i = threadIdx.x; i < kHostStateWords; i += blockDim.x) dst[i] = __ldcg(src + i);
 }
 
 void query_end_launch(const QueryState* q, QueryState* host, cudaStream_t s)
 {
-    k_query_end<<<1, 256, 0, s>>>(q, host);
+    k_query_end<<<1, 64, 0, s>>>(q, host);
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
 }
