@@ -334,9 +334,9 @@ static void lru_enqueue_update(bcmc_lru* c, cudaStream_t s, const uint32_t* need
                                uint32_t max_bits)
 {
     bcmc_ctx* ctx = c->ctx;
-    SlotArgs sa{needed, c->slot_age, c->slot_avail, c->slot_item, c->avail_ids, c->avail_keys, c->st_slots, 0u};
+    SlotArgs sa{needed, c->slot_age, c->slot_avail, c->slot_item, c->avail_ids, c->avail_keys, c->st_slots, 0u, 1u};
     slots_launch(ctx, c->q, sa, c->capacity, s);
-    sort_launch(ctx, c->q, &c->q->num_avail, c->capacity, lru_sort_buffers(c), 1, s);
+    sort_launch(ctx, c->q, &c->q->num_avail, c->capacity, lru_sort_buffers(c), 1, s, /*plan_ready=*/1);
     AssignArgs aa{c->new_ids, c->sort_bv,   c->sort_cv, c->slot_age, c->slot_avail, c->slot_item,
                   c->item_slots, words, max_bits, reinterpret_cast<float*>(c->cache)};
     assign_launch(ctx, c->q, aa, c->total, s);
@@ -578,7 +578,7 @@ static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_s
                   v->total, v->active_ids, c->new_ids, c->st_active_a, c->st_active_n};
     McArgs ma{v->active, v->active_ids, c->item_slots, reinterpret_cast<const float*>(c->cache), nb, grid,
               v->with_verts, v->vert_offsets, v->block_counts, out, c->st_mc_v, c->st_mc_b};
-    SlotArgs sa{v->active, c->slot_age, c->slot_avail, c->slot_item, c->avail_ids, c->avail_keys, c->st_slots, 1u};
+    SlotArgs sa{v->active, c->slot_age, c->slot_avail, c->slot_item, c->avail_ids, c->avail_keys, c->st_slots, 1u, 1u};
     AssignArgs as{c->new_ids, c->sort_bv, c->sort_cv, c->slot_age, c->slot_avail, c->slot_item,
                   c->item_slots, v->words, v->max_bits, reinterpret_cast<float*>(c->cache)};
     if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[0], s, cudaEventRecordExternal));
@@ -586,7 +586,7 @@ static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_s
     active_launch(ctx, c->q, aa, s);
     if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[1], s, cudaEventRecordExternal));
     slots_launch(ctx, c->q, sa, c->capacity, s);
-    sort_launch(ctx, c->q, &c->q->num_avail, c->capacity, lru_sort_buffers(c), 1, s);
+    sort_launch(ctx, c->q, &c->q->num_avail, c->capacity, lru_sort_buffers(c), 1, s, /*plan_ready=*/1);
     if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[2], s, cudaEventRecordExternal));
     assign_launch(ctx, c->q, as, v->total, s);
     if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[3], s, cudaEventRecordExternal));

@@ -77,8 +77,10 @@ struct SortBuffers {
     uint32_t* c_vals;
     uint64_t* status;  // kSortTileStatus words per tile (256 per tile)
 };
+// plan_ready: the keys' producer already made the pass plan and bucket
+// offsets in q (sort_plan), so the histogram kernel is not launched.
 void sort_launch(bcmc_ctx* ctx, QueryState* q, const uint32_t* d_n, uint32_t n_max,
-                 const SortBuffers& bufs, int reverse, cudaStream_t s);
+                 const SortBuffers& bufs, int reverse, cudaStream_t s, int plan_ready = 0);
 // Copies the sorted pairs back to (keys, values) with the inverse key transform.
 void sort_writeback(bcmc_ctx* ctx, QueryState* q, const uint32_t* d_n, uint32_t n_max,
                     const SortBuffers& bufs, uint32_t* keys, uint32_t* vals, int reverse,

@@ -298,6 +298,41 @@ __device__ __forceinline__ uint32_t cta_exclusive_scan(uint32_t v, uint32_t* war
     return r;
 }
 
+// The radix sort's pass plan, made by the last of the CTAs that accumulated
+// the four raw 8-bit digit histograms in q->sort_hist (256 threads, after a
+// fence): a digit pass is skipped when every one of the n keys has the same
+// digit; the histograms become exclusive bucket offsets; the passes that run
+// ping-pong between the two sort buffers, the first reading the input.
+__device__ __forceinline__ void sort_plan(QueryState* q, uint32_t n, uint32_t* warp_sums)
+{
+    uint32_t* gh = &q->sort_hist[0][0];
+    uint32_t run[4], hv[4];
+#pragma unroll
+    for (int d = 0; d < 4; ++d) hv[d] = __ldcg(gh + d * 256 + threadIdx.x);  // all four in flight
+    for (int d = 0; d < 4; ++d) {
+        const uint32_t v = hv[d];
+        const int full = __syncthreads_or(n > 0 && v == n);
+        run[d] = (n > 0 && !full) ? 1u : 0u;
+        uint32_t tot;
+        const uint32_t ex = cta_exclusive_scan<256>(v, warp_sums, &tot);
+        gh[d * 256 + threadIdx.x] = ex;
+    }
+    if (threadIdx.x == 0) {
+        if (n > 0 && !(run[0] | run[1] | run[2] | run[3])) run[0] = 1;  // permutation still applies
+        uint32_t cur = 0, first = 4;
+        for (int d = 0; d < 4; ++d) {
+            q->sort_run[d] = run[d];
+            q->sort_src[d] = cur;
+            if (run[d]) {
+                if (first == 4) first = d;
+                cur = (cur == 1u) ? 2u : 1u;
+            }
+        }
+        q->sort_first = first;
+        q->sort_final = cur == 0 ? 1u : cur;
+    }
+}
+
 // Division by a run-time invariant divisor as a multiply-high and shifts
 // (Granlund & Montgomery, "Division by invariant integers using
 // multiplication", PLDI 1994): exact for every 32-bit dividend.

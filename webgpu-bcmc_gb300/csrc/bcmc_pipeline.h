@@ -31,6 +31,10 @@ struct SlotArgs {
     // computeSurface skips the cache update when no block is active
     // (compressed_marching_cubes.js:630-641); LRUCache.update itself always ages
     uint32_t skip_when_inactive;
+    // 1: also accumulate the digit histograms of ~age (the descending sort's
+    // keys) and make the sort's pass plan in the last CTA, so the sort that
+    // follows runs without its histogram kernel
+    uint32_t plan;
 };
 
 struct AssignArgs {

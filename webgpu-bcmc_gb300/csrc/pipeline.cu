@@ -56,6 +56,10 @@ __global__ void k_query_begin(QueryState* q, float iso, int mc_only, uint32_t ca
             for (int i = 0; i < 4; ++i) q->tiles_sort[i] = 0;
             q->num_active = q->num_new = q->num_avail = 0;
             q->grow_needed = 0;
+            // the sort plan of zero keys (k_slots replaces it when it sorts)
+            for (int i = 0; i < 4; ++i) q->sort_run[i] = q->sort_src[i] = 0;
+            q->sort_first = 4;
+            q->sort_final = 1;
         }
     }
     if (!mc_only)
@@ -330,9 +334,15 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
     __shared__ uint8_t s_flags[kSlotTile + kSlotTile / 32];
     __shared__ uint32_t s_warp[kActThreads / 32 + 1];
     __shared__ uint32_t s_tile, s_prefix;
+    __shared__ uint32_t s_hist[4][256];
+    __shared__ bool s_last;
     if ((a.skip_when_inactive && q->num_active == 0) || q->grow_needed) return;
     const uint32_t old = q->old_cache_size, nsz = q->new_cache_size;
     const bool compact = q->num_new > 0;
+    const bool hist = compact && a.plan != 0u;
+    const uint32_t lane = threadIdx.x & 31u;
+    if (hist)
+        for (int i = threadIdx.x; i < 1024; i += kActThreads) (&s_hist[0][0])[i] = 0;
     const uint32_t ntiles = div_up(nsz, kSlotTile);
     const uint32_t epoch = q->epoch;
     for (;;) {
@@ -380,16 +390,44 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
             uint32_t p = s_prefix + excl;
             const uint32_t first = base + threadIdx.x * kSlotItems;
 #pragma unroll
-            for (int j = 0; j < kSlotItems; ++j)
+            for (int j = 0; j < kSlotItems; ++j) {
+                uint32_t age = 0;
                 if (fl[j]) {
                     const uint32_t s = first + j;
+                    age = a.slot_age[s];
                     a.avail_ids[p] = s;
-                    a.avail_keys[p] = a.slot_age[s];
+                    a.avail_keys[p] = age;
                     ++p;
                 }
+                if (hist) {  // one shared atomic per distinct digit of ~age and warp
+                    const uint32_t k = ~age;
+#pragma unroll
+                    for (int d = 0; d < 4; ++d) {
+                        const uint32_t digit = fl[j] ? (k >> (8 * d)) & 255u : 256u;
+                        const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+                        if (fl[j] && lane == (uint32_t)__ffs(peers) - 1u)
+                            atomicAdd(&s_hist[d][digit], (uint32_t)__popc(peers));
+                    }
+                }
+            }
         }
         __syncthreads();
     }
+    if (!hist) return;
+    // this CTA's histograms into q->sort_hist; the last CTA to finish makes
+    // the sort's pass plan (what k_sort_hist's last CTA does)
+    uint32_t* gh = &q->sort_hist[0][0];
+    for (int i = threadIdx.x; i < 1024; i += kActThreads) {
+        const uint32_t c = (&s_hist[0][0])[i];
+        if (c) atomicAdd(gh + i, c);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&q->tiles_sort_hist, 1u) == gridDim.x - 1u;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    sort_plan(q, q->num_avail, s_warp);
 }
 
 // ---------------------------------------------------------------------------

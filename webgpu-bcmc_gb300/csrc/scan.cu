@@ -24,6 +24,9 @@ __global__ void k_prim_begin(QueryState* q)
         q->num_with_verts = q->num_verts = 0;
         q->grow_needed = 0;
         q->vert_overflow = 0;
+        for (int i = 0; i < 4; ++i) q->sort_run[i] = q->sort_src[i] = 0;  // the plan of zero keys
+        q->sort_first = 4;
+        q->sort_final = 1;
     }
     for (int i = t; i < 1024; i += blockDim.x) (&q->sort_hist[0][0])[i] = 0;
 }

@@ -71,32 +71,7 @@ __global__ void __launch_bounds__(256) k_sort_hist(QueryState* q, const uint32_t
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    // plan: which digit passes run, bucket offsets, buffer ping-pong
-    uint32_t run[4], hv[4];
-#pragma unroll
-    for (int d = 0; d < 4; ++d) hv[d] = __ldcg(gh + d * 256 + threadIdx.x);  // all four in flight
-    for (int d = 0; d < 4; ++d) {
-        const uint32_t v = hv[d];
-        const int full = __syncthreads_or(n > 0 && v == n);
-        run[d] = (n > 0 && !full) ? 1u : 0u;
-        uint32_t tot;
-        const uint32_t ex = cta_exclusive_scan<256>(v, warp_sums, &tot);
-        gh[d * 256 + threadIdx.x] = ex;
-    }
-    if (threadIdx.x == 0) {
-        if (n > 0 && !(run[0] | run[1] | run[2] | run[3])) run[0] = 1;  // permutation still applies
-        uint32_t cur = 0, first = 4;
-        for (int d = 0; d < 4; ++d) {
-            q->sort_run[d] = run[d];
-            q->sort_src[d] = cur;
-            if (run[d]) {
-                if (first == 4) first = d;
-                cur = (cur == 1u) ? 2u : 1u;
-            }
-        }
-        q->sort_first = first;
-        q->sort_final = cur == 0 ? 1u : cur;
-    }
+    sort_plan(q, n, warp_sums);
 }
 
 __global__ void __launch_bounds__(kSortThreads) k_sort_pass(QueryState* q, const uint32_t* d_n, uint32_t n_host,
@@ -226,11 +201,13 @@ int sort_grid(bcmc_ctx* ctx, uint32_t n_max)
 }
 
 void sort_launch(bcmc_ctx* ctx, QueryState* q, const uint32_t* d_n, uint32_t n_max,
-                 const SortBuffers& bufs, int reverse, cudaStream_t s)
+                 const SortBuffers& bufs, int reverse, cudaStream_t s, int plan_ready)
 {
-    const int hist_grid = (int)min(div_up(n_max ? n_max : 1, 256u * 8u), (uint32_t)ctx->num_sms * 4u);
-    k_sort_hist<<<hist_grid, 256, 0, s>>>(q, d_n, n_max, bufs.in_keys, reverse);
-    count_launches(1);
+    if (!plan_ready) {
+        const int hist_grid = (int)min(div_up(n_max ? n_max : 1, 256u * 8u), (uint32_t)ctx->num_sms * 4u);
+        k_sort_hist<<<hist_grid, 256, 0, s>>>(q, d_n, n_max, bufs.in_keys, reverse);
+        count_launches(1);
+    }
     const int grid = sort_grid(ctx, n_max);
     for (int pass = 0; pass < 4; ++pass)
         k_sort_pass<<<grid, kSortThreads, 0, s>>>(q, d_n, n_max, bufs, reverse, pass);
