@@ -94,8 +94,11 @@ void bcmc_volume_destroy(bcmc_vol* vol);
  * perfTracker (compressed_marching_cubes.js:593-610). */
 typedef struct {
     float computeActiveBlocks; /* active test + compaction + cache lookup        */
-    float cacheUpdate;         /* LRU age/mark/grow/sort/assign                  */
-    float decompression;       /* ZFP decode of newly needed blocks               */
+    float cacheUpdate;         /* LRU age/mark/grow/sort                         */
+    float decompression;       /* slot assignment and the new blocks' data into
+                                * their slots; their ZFP decode runs beside the
+                                * cache update, so only what is left of it after
+                                * the sort is counted here                       */
     float computeVertices;     /* MC count + scan + emit                         */
     float total;
 } bcmc_perf;

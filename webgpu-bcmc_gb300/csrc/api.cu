@@ -379,7 +379,16 @@ struct bcmc_vol {
     uint64_t graph_key[3][4]{};
     bool last_on_host = false;  // the last query's vertices went to host memory only
     uint64_t graph_kernels = 0;
+    // the new blocks' decode runs on a branch of the query graph, beside the
+    // LRU's slot selection, into `stage` (stage_blocks elements of 256 B)
+    float* stage = nullptr;
+    uint32_t stage_blocks = 0;
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
 };
+
+// new blocks a query stages at most (32 MiB); k_assign decodes any beyond
+constexpr uint32_t kStageBlocksMax = 1u << 17;
 
 static void vol_free(bcmc_vol* v)
 {
@@ -394,9 +403,13 @@ static void vol_free(bcmc_vol* v)
     dev_free(ctx, v->vert_offsets, (size_t)v->total * 4);
     dev_free(ctx, v->block_counts, (size_t)v->total * 4);
     dev_free(ctx, v->verts, (size_t)v->vert_capacity * 8);
+    dev_free(ctx, v->stage, (size_t)v->stage_blocks * 256u);
     lru_delete(v->lru);
     for (auto& e : v->ev)
         if (e) cudaEventDestroy(e);
+    if (v->fork_ev) cudaEventDestroy(v->fork_ev);
+    if (v->join_ev) cudaEventDestroy(v->join_ev);
+    if (v->side) cudaStreamDestroy(v->side);
     for (auto& g : v->graph)
         if (g) cudaGraphExecDestroy(g);
     if (v->h_in) cudaFreeHost(v->h_in);
@@ -468,6 +481,11 @@ static bcmc_status vol_create_common(bcmc_ctx* ctx, const void* src, bool src_de
             v->verts_storage = 0;
             for (auto& e : v->ev) BCMC_CUDA(cudaEventCreate(&e));
             BCMC_CUDA(cudaMallocHost(&v->h_in, sizeof(QueryInputs)));
+            v->stage_blocks = (uint32_t)std::min<uint64_t>(total, kStageBlocksMax);
+            v->stage = (float*)dev_alloc(ctx, (size_t)v->stage_blocks * 256u);
+            BCMC_CUDA(cudaStreamCreateWithFlags(&v->side, cudaStreamNonBlocking));
+            BCMC_CUDA(cudaEventCreateWithFlags(&v->fork_ev, cudaEventDisableTiming));
+            BCMC_CUDA(cudaEventCreateWithFlags(&v->join_ev, cudaEventDisableTiming));
             zfp_ranges_launch(ctx, v->words, v->dims, max_bits, v->ranges, s);
             BCMC_CUDA(cudaStreamSynchronize(s));
             v->stats.totalBlocks = v->total;
@@ -580,14 +598,22 @@ static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_s
               v->with_verts, v->vert_offsets, v->block_counts, out, c->st_mc_v, c->st_mc_b};
     SlotArgs sa{v->active, c->slot_age, c->slot_avail, c->slot_item, c->avail_ids, c->avail_keys, c->st_slots, 1u, 1u};
     AssignArgs as{c->new_ids, c->sort_bv, c->sort_cv, c->slot_age, c->slot_avail, c->slot_item,
-                  c->item_slots, v->words, v->max_bits, reinterpret_cast<float*>(c->cache)};
+                  c->item_slots, v->words, v->max_bits, reinterpret_cast<float*>(c->cache), v->stage, v->stage_blocks};
+    DecodeArgs da{c->new_ids, v->words, v->max_bits, v->stage, v->stage_blocks};
     if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[0], s, cudaEventRecordExternal));
     query_begin_launch(c->q, iso, 0, c->capacity, v->vert_capacity, s, from_state ? v->h_in : nullptr);
     active_launch(ctx, c->q, aa, s);
     if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[1], s, cudaEventRecordExternal));
+    // branch: the new blocks' decode into the staging buffer needs only the
+    // active test's new ids, so it overlaps the slot selection below
+    BCMC_CUDA(cudaEventRecord(v->fork_ev, s));
     slots_launch(ctx, c->q, sa, c->capacity, s);
+    BCMC_CUDA(cudaStreamWaitEvent(v->side, v->fork_ev, 0));
+    decode_new_launch(ctx, c->q, da, v->side);
+    BCMC_CUDA(cudaEventRecord(v->join_ev, v->side));
     sort_launch(ctx, c->q, &c->q->num_avail, c->capacity, lru_sort_buffers(c), 1, s, /*plan_ready=*/1);
     if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[2], s, cudaEventRecordExternal));
+    BCMC_CUDA(cudaStreamWaitEvent(s, v->join_ev, 0));
     assign_launch(ctx, c->q, as, v->total, s);
     if (events) BCMC_CUDA(cudaEventRecordWithFlags(v->ev[3], s, cudaEventRecordExternal));
     mc_launch(ctx, c->q, ma, v->total, s);
@@ -784,7 +810,8 @@ bcmc_status bcmc_memory_report(bcmc_vol* v, bcmc_memory* m)
     m->cache = (uint64_t)c->capacity * c->element_size;
     m->cachedItemSlots = (uint64_t)c->aligned_total * 4;
     m->slotData = (uint64_t)c->capacity * 12;
-    m->scratch = (uint64_t)c->capacity * 4 * 6 + c->status_words * 8 + (uint64_t)c->total * 4 + sizeof(QueryState);
+    m->scratch = (uint64_t)c->capacity * 4 * 6 + c->status_words * 8 + (uint64_t)c->total * 4 + sizeof(QueryState) +
+                 (uint64_t)v->stage_blocks * 256u;
     m->deviceTotal = m->compressedData + m->vertexBuffer + m->blockActive + m->blockRanges + m->activeBlockIDs +
                      m->blocksWithVertices + m->blockVertexOffsets + m->cache + m->cachedItemSlots + m->slotData +
                      m->scratch;

@@ -48,6 +48,20 @@ struct AssignArgs {
     const uint64_t* words;    // set: decode each new block into its slot
     uint32_t max_bits;
     float* cache;
+    // set: new blocks [0, stage_blocks) were decoded into stage (one element
+    // per new-block index) by k_decode_new and are copied into their slots
+    const float* stage;
+    uint32_t stage_blocks;
+};
+
+// k_decode_new: the new blocks' ZFP decode, run beside the LRU's slot
+// selection (it needs only the new ids) into a staging buffer.
+struct DecodeArgs {
+    const uint32_t* new_ids;
+    const uint64_t* words;
+    uint32_t max_bits;
+    float* stage;           // stage_blocks * 64 floats
+    uint32_t stage_blocks;
 };
 
 struct McArgs {
@@ -71,6 +85,7 @@ void query_end_launch(const QueryState* q, QueryState* host, cudaStream_t s);
 void active_launch(bcmc_ctx* ctx, QueryState* q, const ActiveArgs& a, cudaStream_t s);
 void slots_launch(bcmc_ctx* ctx, QueryState* q, const SlotArgs& a, uint32_t max_slots, cudaStream_t s);
 void assign_launch(bcmc_ctx* ctx, QueryState* q, const AssignArgs& a, uint32_t max_new, cudaStream_t s);
+void decode_new_launch(bcmc_ctx* ctx, const QueryState* q, const DecodeArgs& a, cudaStream_t s);
 void mc_launch(bcmc_ctx* ctx, QueryState* q, const McArgs& a, uint32_t max_active, cudaStream_t s);
 uint32_t active_tiles(uint32_t total);
 uint32_t slot_tiles(uint32_t slots);

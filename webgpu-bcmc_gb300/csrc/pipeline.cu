@@ -431,8 +431,9 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
 }
 
 // ---------------------------------------------------------------------------
-// k_assign: lru_cache_update.comp:19-37 (+ decode of the new block into its
-// slot when `words` is set).
+// k_assign: lru_cache_update.comp:19-37 (+ the new block's data into its slot
+// when `words` is set: copied from the staging buffer k_decode_new filled,
+// decoded here for new-block indices past it).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_assign(QueryState* q, AssignArgs a)
 {
@@ -453,13 +454,42 @@ __global__ void __launch_bounds__(128) k_assign(QueryState* q, AssignArgs a)
         a.slot_item[slot] = (int32_t)item;
         a.slot_avail[slot] = 0;
         a.item_slots[item] = (int32_t)slot;
-        if (a.words) {
+        if (a.words && i >= a.stage_blocks) {
             float v[64];
             zfp_decode_block<1>(a.words, (uint64_t)item * a.max_bits, a.max_bits, v);
             float4* d4 = reinterpret_cast<float4*>(a.cache + (uint64_t)slot * 64u);
 #pragma unroll
             for (int k = 0; k < 16; ++k) d4[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
         }
+    }
+    if (!a.stage) return;
+    // staged blocks into their slots: 16 threads per block, 16 B each
+    const uint32_t ns = n < a.stage_blocks ? n : a.stage_blocks;
+    const float4* __restrict__ src = reinterpret_cast<const float4*>(a.stage);
+    float4* dst = reinterpret_cast<float4*>(a.cache);
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < ns * 16u; e += gridDim.x * blockDim.x) {
+        const uint32_t i = e >> 4, k = e & 15u;
+        const uint32_t slot = sorted[i];
+        if (slot < size) dst[(uint64_t)slot * 16u + k] = __ldcs(src + (uint64_t)i * 16u + k);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_decode_new: zfp_decompress_block.comp's decode of the query's new blocks,
+// by new-block index into the staging buffer.  It depends on the active test
+// only, so it runs beside k_slots and the sort; k_assign then copies the
+// staged blocks into the slots the sort chose.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_decode_new(const QueryState* q, DecodeArgs a)
+{
+    if (q->num_active == 0 || q->grow_needed) return;
+    const uint32_t n = q->num_new < a.stage_blocks ? q->num_new : a.stage_blocks;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float v[64];
+        zfp_decode_block<1>(a.words, (uint64_t)a.new_ids[i] * a.max_bits, a.max_bits, v);
+        float4* d4 = reinterpret_cast<float4*>(a.stage + (uint64_t)i * 64u);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) d4[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
     }
 }
 
@@ -823,6 +853,15 @@ void slots_launch(bcmc_ctx* ctx, QueryState* q, const SlotArgs& a, uint32_t max_
 void assign_launch(bcmc_ctx* ctx, QueryState* q, const AssignArgs& a, uint32_t max_new, cudaStream_t s)
 {
     k_assign<<<pgrid(ctx, div_up(max_new, 128u), 16), 128, 0, s>>>(q, a);
+    count_launches(1);
+    BCMC_CUDA(cudaGetLastError());
+}
+
+void decode_new_launch(bcmc_ctx* ctx, const QueryState* q, const DecodeArgs& a, cudaStream_t s)
+{
+    // two CTAs per SM: the branch it runs on must leave room for the slot
+    // selection's CTAs, the critical path beside it
+    k_decode_new<<<pgrid(ctx, div_up(a.stage_blocks ? a.stage_blocks : 1u, 128u), 2), 128, 0, s>>>(q, a);
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
 }
