@@ -60,9 +60,20 @@ struct QueryState {
     uint32_t sort_run[4];     // 1 if the digit pass runs
     uint32_t sort_first;      // index of the first pass that runs (4 = none)
     uint32_t sort_final;      // buffer holding the sorted values
+    uint32_t sort_key16;      // 1: the passes sort the 16-bit age keys (age_key16)
+    uint32_t sort_wide;       // set by k_slots when an available slot's age has no 16-bit key
     uint32_t sort_hist[4][256];
+    uint32_t sort_hist16[2][256];  // k_slots: digit histograms of the 16-bit age keys
     uint32_t pad[8];
 };
+
+// The LRU's slot ages (lru_cache.comp, lru_cache_init.comp) are small counts
+// for slots used since the cache was (re)initialised and 100000 plus a count
+// for the others.  While every age is below 2^15 or in [100000, 100000 + 2^15)
+// this map is strictly increasing on them and fits 16 bits, so the sort by age
+// can run two 8-bit digit passes instead of three with the same order and ties.
+__device__ __forceinline__ bool age_has_key16(uint32_t age) { return age < 32768u || age - 100000u < 32768u; }
+__device__ __forceinline__ uint32_t age_key16(uint32_t age) { return age < 32768u ? age : 32768u + (age - 100000u); }
 
 // ---------------------------------------------------------------------------
 // Decoupled look-back status words: [epoch:30 | flag:2][value:32].
@@ -303,13 +314,20 @@ __device__ __forceinline__ uint32_t cta_exclusive_scan(uint32_t v, uint32_t* war
 // fence): a digit pass is skipped when every one of the n keys has the same
 // digit; the histograms become exclusive bucket offsets; the passes that run
 // ping-pong between the two sort buffers, the first reading the input.
-__device__ __forceinline__ void sort_plan(QueryState* q, uint32_t n, uint32_t* warp_sums)
+// `hist` holds the raw histograms of the first `ndig` digits; the digits
+// after them are not sorted on (their passes are skipped).
+__device__ __forceinline__ void sort_plan(QueryState* q, uint32_t n, uint32_t* warp_sums, const uint32_t* hist,
+                                          int ndig)
 {
     uint32_t* gh = &q->sort_hist[0][0];
     uint32_t run[4], hv[4];
 #pragma unroll
-    for (int d = 0; d < 4; ++d) hv[d] = __ldcg(gh + d * 256 + threadIdx.x);  // all four in flight
+    for (int d = 0; d < 4; ++d) hv[d] = d < ndig ? __ldcg(hist + d * 256 + threadIdx.x) : 0u;  // all in flight
     for (int d = 0; d < 4; ++d) {
+        if (d >= ndig) {
+            run[d] = 0;
+            continue;
+        }
         const uint32_t v = hv[d];
         const int full = __syncthreads_or(n > 0 && v == n);
         run[d] = (n > 0 && !full) ? 1u : 0u;

@@ -60,10 +60,11 @@ __global__ void k_query_begin(QueryState* q, float iso, int mc_only, uint32_t ca
             for (int i = 0; i < 4; ++i) q->sort_run[i] = q->sort_src[i] = 0;
             q->sort_first = 4;
             q->sort_final = 1;
+            q->sort_key16 = q->sort_wide = 0;
         }
     }
     if (!mc_only)
-        for (int i = t; i < 1024; i += blockDim.x) (&q->sort_hist[0][0])[i] = 0;
+        for (int i = t; i < 1536; i += blockDim.x) (&q->sort_hist[0][0])[i] = 0;  // and sort_hist16
 }
 
 // Ends a query graph: the query state the host reads (the fields before the
@@ -334,15 +335,16 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
     __shared__ uint8_t s_flags[kSlotTile + kSlotTile / 32];
     __shared__ uint32_t s_warp[kActThreads / 32 + 1];
     __shared__ uint32_t s_tile, s_prefix;
-    __shared__ uint32_t s_hist[4][256];
+    __shared__ uint32_t s_hist[6][256];  // ~age digits 0-3, then the 16-bit keys' digits 0-1
     __shared__ bool s_last;
     if ((a.skip_when_inactive && q->num_active == 0) || q->grow_needed) return;
     const uint32_t old = q->old_cache_size, nsz = q->new_cache_size;
     const bool compact = q->num_new > 0;
     const bool hist = compact && a.plan != 0u;
     const uint32_t lane = threadIdx.x & 31u;
+    uint32_t wide = 0;  // an age without a 16-bit key
     if (hist)
-        for (int i = threadIdx.x; i < 1024; i += kActThreads) (&s_hist[0][0])[i] = 0;
+        for (int i = threadIdx.x; i < 1536; i += kActThreads) (&s_hist[0][0])[i] = 0;
     const uint32_t ntiles = div_up(nsz, kSlotTile);
     const uint32_t epoch = q->epoch;
     for (;;) {
@@ -399,11 +401,12 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
                     a.avail_keys[p] = age;
                     ++p;
                 }
-                if (hist) {  // one shared atomic per distinct digit of ~age and warp
-                    const uint32_t k = ~age;
+                if (hist) {  // one shared atomic per distinct digit and warp
+                    const uint32_t k = ~age, k16 = ~age_key16(age);
+                    if (fl[j] && !age_has_key16(age)) wide = 1;
 #pragma unroll
-                    for (int d = 0; d < 4; ++d) {
-                        const uint32_t digit = fl[j] ? (k >> (8 * d)) & 255u : 256u;
+                    for (int d = 0; d < 6; ++d) {
+                        const uint32_t digit = fl[j] ? ((d < 4 ? k : k16) >> (8 * (d & 3))) & 255u : 256u;
                         const uint32_t peers = __match_any_sync(0xffffffffu, digit);
                         if (fl[j] && lane == (uint32_t)__ffs(peers) - 1u)
                             atomicAdd(&s_hist[d][digit], (uint32_t)__popc(peers));
@@ -416,18 +419,22 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
     if (!hist) return;
     // this CTA's histograms into q->sort_hist; the last CTA to finish makes
     // the sort's pass plan (what k_sort_hist's last CTA does)
-    uint32_t* gh = &q->sort_hist[0][0];
-    for (int i = threadIdx.x; i < 1024; i += kActThreads) {
+    uint32_t* gh = &q->sort_hist[0][0];  // sort_hist16 follows it
+    for (int i = threadIdx.x; i < 1536; i += kActThreads) {
         const uint32_t c = (&s_hist[0][0])[i];
         if (c) atomicAdd(gh + i, c);
     }
+    if (__syncthreads_or(wide) && threadIdx.x == 0) atomicOr(&q->sort_wide, 1u);
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) s_last = atomicAdd(&q->tiles_sort_hist, 1u) == gridDim.x - 1u;
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    sort_plan(q, q->num_avail, s_warp);
+    const bool key16 = *reinterpret_cast<volatile uint32_t*>(&q->sort_wide) == 0u;
+    if (threadIdx.x == 0) q->sort_key16 = key16 ? 1u : 0u;
+    if (key16) sort_plan(q, q->num_avail, s_warp, &q->sort_hist16[0][0], 2);
+    else sort_plan(q, q->num_avail, s_warp, &q->sort_hist[0][0], 4);
 }
 
 // ---------------------------------------------------------------------------

@@ -27,8 +27,9 @@ __global__ void k_prim_begin(QueryState* q)
         for (int i = 0; i < 4; ++i) q->sort_run[i] = q->sort_src[i] = 0;  // the plan of zero keys
         q->sort_first = 4;
         q->sort_final = 1;
+        q->sort_key16 = q->sort_wide = 0;
     }
-    for (int i = t; i < 1024; i += blockDim.x) (&q->sort_hist[0][0])[i] = 0;
+    for (int i = t; i < 1536; i += blockDim.x) (&q->sort_hist[0][0])[i] = 0;  // and sort_hist16
 }
 
 void prim_begin(QueryState* q, cudaStream_t s)

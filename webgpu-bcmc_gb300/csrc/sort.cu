@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(256) k_sort_hist(QueryState* q, const uint32_t
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    sort_plan(q, n, warp_sums);
+    sort_plan(q, n, warp_sums, &q->sort_hist[0][0], 4);
 }
 
 __global__ void __launch_bounds__(kSortThreads) k_sort_pass(QueryState* q, const uint32_t* d_n, uint32_t n_host,
@@ -93,6 +93,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(QueryState* q, const
     uint32_t* __restrict__ kd = src == 1 ? b.c_keys : b.b_keys;
     uint32_t* __restrict__ vd = src == 1 ? b.c_vals : b.b_vals;
     const bool gather = src == 0;
+    const bool key16 = q->sort_key16 != 0u;
     const uint32_t shift = 8u * (uint32_t)pass;
     const uint32_t epoch = q->epoch * 4u + (uint32_t)pass;
     const uint32_t ntiles = div_up(n, kSortTile);
@@ -117,6 +118,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(QueryState* q, const
             if (qi < n) {
                 const uint32_t p = gather ? tie_perm(qi, n, reverse) : qi;
                 uint32_t k = ks[p];
+                if (gather && key16) k = age_key16(k);
                 if (gather && reverse) k = ~k;
                 key[j] = k;
                 val[j] = vs[p];
