@@ -487,8 +487,9 @@ def algorithmic_bytes(stage: str, st: dict, rate: int, total_blocks: int) -> flo
     """Algorithmic DRAM bytes per launch of each stage's kernel."""
     if stage == "computeVertices":  # k_mc: block data + ids/slots + vertices
         return st["numActiveBlocks"] * (256 + 4 + 4) + st["numVertices"] * 8 + st["numBlocksWithVertices"] * 8
-    if stage == "decompression":  # k_assign: compressed bits + decoded block + ids
-        return st["newDecompressed"] * (8 * rate + 256 + 8)
+    if stage == "decompression":  # k_decode_new + k_assign: compressed bits, the decoded
+        # block staged, read back and written into its slot, ids
+        return st["newDecompressed"] * (8 * rate + 3 * 256 + 8)
     if stage == "computeActiveBlocks":  # k_active: ranges, slots, flags
         return total_blocks * (8 + 4 + 4) + st["numActiveBlocks"] * 4
     if stage == "cacheUpdate":  # k_slots + sort: 3 slot arrays rw + sort passes
@@ -621,7 +622,7 @@ def run_gb300(args):
     avg_ms = tot[dominant] / nq
     peak, peak_kind = _peaks()
     achieved = bytes_per_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else 0.0
-    kernel_of = {"computeVertices": "k_mc", "decompression": "k_assign (LRU assign + ZFP decode)",
+    kernel_of = {"computeVertices": "k_mc", "decompression": "k_decode_new + k_assign (ZFP decode beside the cache update, slot assignment and copy)",
                  "computeActiveBlocks": "k_active", "cacheUpdate": "k_slots + radix sort"}
 
     decode = decode_bench(ctx, flush) if not args.no_decode else None

@@ -595,7 +595,7 @@ static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_s
     ActiveArgs aa{reinterpret_cast<const float2*>(v->ranges), nb, grid, nullptr, v->active, c->item_slots,
                   v->total, v->active_ids, c->new_ids, c->st_active_a, c->st_active_n};
     McArgs ma{v->active, v->active_ids, c->item_slots, reinterpret_cast<const float*>(c->cache), nb, grid,
-              v->with_verts, v->vert_offsets, v->block_counts, out, c->st_mc_v, c->st_mc_b};
+              v->with_verts, v->vert_offsets, v->block_counts, out, c->st_mc_v, c->st_mc_b, out != v->verts ? 1u : 0u};
     SlotArgs sa{v->active, c->slot_age, c->slot_avail, c->slot_item, c->avail_ids, c->avail_keys, c->st_slots, 1u, 1u};
     AssignArgs as{c->new_ids, c->sort_bv, c->sort_cv, c->slot_age, c->slot_avail, c->slot_item,
                   c->item_slots, v->words, v->max_bits, reinterpret_cast<float*>(c->cache), v->stage, v->stage_blocks};

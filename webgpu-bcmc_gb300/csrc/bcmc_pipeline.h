@@ -77,6 +77,9 @@ struct McArgs {
     uint2* verts;
     uint64_t* status_v;
     uint64_t* status_b;
+    // 1: verts is page-locked host memory; each warp's vertex stores then
+    // cover one 256 B-aligned window, which such stores need for full speed
+    uint32_t host_verts;
 };
 
 void query_begin_launch(QueryState* q, float iso, int mc_only, uint32_t capacity, uint32_t vert_capacity,

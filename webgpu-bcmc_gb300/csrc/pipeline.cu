@@ -775,7 +775,11 @@ __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
             a.vert_offsets[pb + t] = pv + s_off[64 * t];
         }
         uint2* out = a.verts + pv;
-        for (uint32_t k = t; k < tile_v; k += kMcThreads) {
+        // into host memory, j = k + shift puts each warp's 32 stores in one
+        // 256 B-aligned window: stores over the host link run ~20 % faster
+        // aligned (device memory gains less than the extra round costs)
+        const uint32_t shift = a.host_verts ? (uint32_t)(reinterpret_cast<uintptr_t>(out) >> 3) & 31u : 0u;
+        const auto emit = [&](const uint32_t k) {
             uint32_t cell = 0;
 #pragma unroll
             for (uint32_t step = kMcCells / 2; step; step >>= 1)
@@ -810,6 +814,12 @@ __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
                 qz = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)az, __fmul_rn(tt, (float)((int)bz - (int)az))), (float)z), 0.5f));
             }
             out[k] = make_uint2((qx << 20) | (qy << 10) | qz, s_id[jb]);
+        };
+        if (shift == 0u) {  // the loop of the device path stays free of the shift
+            for (uint32_t k = t; k < tile_v; k += kMcThreads) emit(k);
+        } else {
+            for (uint32_t j = t; j < tile_v + shift; j += kMcThreads)
+                if (j >= shift) emit(j - shift);
         }
         pv += tile_v;
         pb += n_sel;
