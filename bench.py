@@ -480,7 +480,7 @@ def served_bench() -> dict:
 
 # DRAM bytes (read + write) per launch from one ncu capture of this workload's
 # launch list (profiles/ct256_launch_list.md), mean over the 16-isovalue sweep
-NCU_TRAFFIC = {"k_mc": 41.521e6}
+NCU_TRAFFIC = {"k_mc": 42.037e6}
 
 
 def algorithmic_bytes(stage: str, st: dict, rate: int, total_blocks: int) -> float:
