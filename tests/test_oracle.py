@@ -91,6 +91,35 @@ def test_sort_tie_order_closed_form(oracle, reverse):
         assert list(v) == order
 
 
+def _age_key16(ages):
+    """age_key16 of csrc/bcmc_internal.cuh: the LRU age sort's 16-bit key."""
+    a = ages.astype(np.int64)
+    return np.where(a < 32768, a, 32768 + (a - 100000)).astype(np.uint32)
+
+
+def test_age_key16_keeps_the_lru_sort_order(oracle):
+    """On ages below 2^15 or in [100000, 100000 + 2^15) (slots in use count up from
+    0, the others from lru_cache_init.comp's 100000) the 16-bit key is strictly
+    increasing and below 2^16, so the LRU's descending sort by it gives the
+    reference's order and ties exactly."""
+    edge = np.array([0, 1, 2, 32766, 32767, 100000, 100001, 132766, 132767], np.uint32)
+    k16 = _age_key16(edge)
+    assert np.all(np.diff(k16.astype(np.int64)) > 0) and int(k16.max()) < 65536
+    rng = np.random.default_rng(21)
+    for trial in range(24):
+        n = int(rng.integers(1, 5000))
+        if trial % 3 == 0:
+            ages = rng.choice(edge, n).astype(np.uint32)
+        else:
+            small = rng.integers(0, 20, n)
+            big = 100000 + rng.integers(0, 20, n)
+            ages = np.where(rng.random(n) < 0.5, small, big).astype(np.uint32)
+        vals = np.arange(n, dtype=np.uint32)
+        _, v_raw = oracle.sort_by_key(ages, vals, True)
+        _, v_16 = oracle.sort_by_key(_age_key16(ages), vals, True)
+        assert np.array_equal(v_raw, v_16), (trial, n)
+
+
 def test_scan_and_compact(oracle):
     rng = np.random.default_rng(3)
     x = rng.integers(0, 2, size=1000).astype(np.uint32)
