@@ -6,17 +6,23 @@
 // query is a fixed sequence of launches that read every count from the
 // QueryState on the device:
 //   k_query_begin  new look-back epoch, counters cleared
-//   k_active       active test (compute_block_active.comp) for every block,
+//   k_active_ranges / k_active
+//                  active test (compute_block_active.comp) for every block,
 //                  fused with the compaction of active ids, the cache lookup
 //                  (lru_cache_mark_new_items.comp's "needs caching") and the
 //                  compaction of new item ids; the last tile decides the cache
 //                  growth (js/lru_cache.js:510-522)
 //   k_slots        age/mark/grow of every slot (lru_cache_age_slots.comp,
 //                  lru_cache_mark_new_items.comp, lru_cache_init.comp) fused
-//                  with the compaction of available slots and their ages
+//                  with the compaction of available slots and their ages, the
+//                  sort keys' digit histograms and (last CTA) the sort's plan
 //   sort           available slots by age, oldest first (sort.cu)
-//   k_assign       lru_cache_update.comp fused with the ZFP decode of the new
-//                  block into its slot (zfp_decompress_block.comp)
+//   k_decode_new   beside k_slots and the sort (a branch of the query graph):
+//                  the ZFP decode of the new blocks (zfp_decompress_block.comp)
+//                  into a staging buffer
+//   k_assign       lru_cache_update.comp, and the staged blocks copied into
+//                  their slots
+//   k_query_end    the query state the host reads, into its pinned copy
 //   k_mc           marching cubes count + scan + emit in one pass
 //                  (compute_block_has_vertices.comp,
 //                  compute_block_voxel_num_verts.comp,
