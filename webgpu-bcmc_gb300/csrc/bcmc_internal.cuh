@@ -55,7 +55,8 @@ struct QueryState {
     uint32_t tiles_mc;
     uint32_t tiles_sort[4];
     uint32_t tiles_sort_hist;
-    // radix sort plan (written by the histogram kernel)
+    // radix sort plan (sort_plan, run by the last CTA of k_sort_hist or of
+    // k_slots, whichever accumulated the digit histograms)
     uint32_t sort_src[4];     // source buffer (0/1) of each digit pass
     uint32_t sort_run[4];     // 1 if the digit pass runs
     uint32_t sort_first;      // index of the first pass that runs (4 = none)
