@@ -1,4 +1,4 @@
-"""Full-size configurations, checked through properties that do not need the
+"""Full-size workloads, checked through properties that do not need the
 oracle to run the whole workload:
 
 * 512^3 spectral field, rate 2, cache 25 %, a 64-isovalue random walk: the
@@ -30,7 +30,7 @@ def _encode_on_gpu(ctx, field_dev, rate, dims):
     return words, host, host.view(np.uint8)[: nb * 8 * rate].copy()
 
 
-def test_c3_spectral_random_walk(ctx, oracle):
+def test_spectral512_random_walk(ctx, oracle):
     import torch
 
     dims, rate = (512, 512, 512), 2
@@ -70,30 +70,30 @@ def test_c3_spectral_random_walk(ctx, oracle):
             assert np.array_equal(allv[off: off + n], verts), first + i
 
 
-C5_DIMS = (1024, 1024, 1080)
-C5_BLOCKS = 256 * 256 * 270  # 17,694,720
+BIG_DIMS = (1024, 1024, 1080)
+BIG_BLOCKS = 256 * 256 * 270  # 17,694,720
 
 
-def test_c5_block_offsets_past_2_24(ctx, oracle):
+def test_1024x1024x1080_block_offsets_past_2_24(ctx, oracle):
     """Random 32-byte blocks (rate 4): every bit pattern is a valid block."""
     import torch
 
     rate, max_bits = 4, 256
-    assert C5_BLOCKS > (1 << 24)
+    assert BIG_BLOCKS > (1 << 24)
     g = torch.Generator(device="cuda").manual_seed(11)
     # rate 4: 256 bits = 4 words per block, plus the word the reader may fetch past the end
-    nwords = C5_BLOCKS * max_bits // 64 + 2
+    nwords = BIG_BLOCKS * max_bits // 64 + 2
     words = torch.randint(-(1 << 63), (1 << 63) - 1, (nwords,), dtype=torch.int64, device="cuda", generator=g)
-    assert words.numel() * 64 >= C5_BLOCKS * max_bits + 64
+    assert words.numel() * 64 >= BIG_BLOCKS * max_bits + 64
     host = words.cpu().numpy().view(np.uint64)
-    dec = bcmc.zfp_decode_volume(ctx, words, C5_BLOCKS, rate)
-    ranges = bcmc.zfp_block_ranges(ctx, words, C5_DIMS, rate)
+    dec = bcmc.zfp_decode_volume(ctx, words, BIG_BLOCKS, rate)
+    ranges = bcmc.zfp_block_ranges(ctx, words, BIG_DIMS, rate)
     torch.cuda.synchronize()
-    sample = list(range((1 << 24) - 64, (1 << 24) + 64)) + list(range(C5_BLOCKS - 64, C5_BLOCKS)) + \
-        [int(b) for b in np.random.default_rng(4).integers(0, C5_BLOCKS, 128)]
+    sample = list(range((1 << 24) - 64, (1 << 24) + 64)) + list(range(BIG_BLOCKS - 64, BIG_BLOCKS)) + \
+        [int(b) for b in np.random.default_rng(4).integers(0, BIG_BLOCKS, 128)]
     idx = torch.tensor(sample, dtype=torch.int64, device="cuda")
-    got = dec.view(C5_BLOCKS, 64)[idx].cpu().numpy()
-    got_r = ranges.view(C5_BLOCKS, 2)[idx].cpu().numpy()
+    got = dec.view(BIG_BLOCKS, 64)[idx].cpu().numpy()
+    got_r = ranges.view(BIG_BLOCKS, 2)[idx].cpu().numpy()
     for i, b in enumerate(sample):
         want = oracle.decode_block(host, b, max_bits)
         assert np.array_equal(got[i].view(np.uint32), want.view(np.uint32)), b
@@ -110,19 +110,19 @@ def test_c5_block_offsets_past_2_24(ctx, oracle):
             assert not np.array_equal(wrapped.view(np.uint32), want.view(np.uint32)) or not want.any(), b
 
 
-def test_c5_query_plain_equals_engine(ctx):
+def test_1024x1024x1080_query_plain_equals_engine(ctx):
     import torch
 
     rate = 4
-    field = D.ct_uint16_torch(C5_DIMS, 5)
-    _, _, stream = _encode_on_gpu(ctx, field, rate, C5_DIMS)
+    field = D.ct_uint16_torch(BIG_DIMS, 5)
+    _, _, stream = _encode_on_gpu(ctx, field, rate, BIG_DIMS)
     del field
     torch.cuda.empty_cache()
     c = bcmc.Context(ctx.device, initial_cache_fraction=0.1)
     mc = bcmc.CompressedMarchingCubes(c)
-    mc.setCompressedVolume(stream, rate, C5_DIMS)
+    mc.setCompressedVolume(stream, rate, BIG_DIMS)
     eng = bcmc.Engine(ctx)
-    vid = eng.addVolume(stream, rate, C5_DIMS)
+    vid = eng.addVolume(stream, rate, BIG_DIMS)
     for iso in (2500.0, 3600.0):
         n = mc.computeSurface(iso)
         assert n > 0
