@@ -531,6 +531,9 @@ constexpr int kMcCells = 64 * kMcBlocks;  // 4 consecutive cells per thread
 //     and stores are contiguous.
 // A CTA walks back once per launch, not once per tile.  Output order = the
 // reference's: active-block order, cell order, table order.
+// kHost: the vertices go to page-locked host memory (a.host_verts); its own
+// instantiation keeps the device path's emit loop free of the alignment shift.
+template <bool kHost>
 __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
 {
     __shared__ float s_vol[kMcBlocks][128];
@@ -781,10 +784,6 @@ __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
             a.vert_offsets[pb + t] = pv + s_off[64 * t];
         }
         uint2* out = a.verts + pv;
-        // into host memory, j = k + shift puts each warp's 32 stores in one
-        // 256 B-aligned window: stores over the host link run ~20 % faster
-        // aligned (device memory gains less than the extra round costs)
-        const uint32_t shift = a.host_verts ? (uint32_t)(reinterpret_cast<uintptr_t>(out) >> 3) & 31u : 0u;
         const auto emit = [&](const uint32_t k) {
             uint32_t cell = 0;
 #pragma unroll
@@ -821,11 +820,16 @@ __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
             }
             out[k] = make_uint2((qx << 20) | (qy << 10) | qz, s_id[jb]);
         };
-        if (shift == 0u) {  // the loop of the device path stays free of the shift
-            for (uint32_t k = t; k < tile_v; k += kMcThreads) emit(k);
-        } else {
+        if constexpr (kHost) {
+            // into host memory, j = k + shift puts each warp's 32 stores in
+            // one 256 B-aligned window: stores over the host link run ~20 %
+            // faster aligned (device memory gains less than the extra round
+            // costs)
+            const uint32_t shift = (uint32_t)(reinterpret_cast<uintptr_t>(out) >> 3) & 31u;
             for (uint32_t j = t; j < tile_v + shift; j += kMcThreads)
                 if (j >= shift) emit(j - shift);
+        } else {
+            for (uint32_t k = t; k < tile_v; k += kMcThreads) emit(k);
         }
         pv += tile_v;
         pb += n_sel;
@@ -891,7 +895,8 @@ void decode_new_launch(bcmc_ctx* ctx, const QueryState* q, const DecodeArgs& a, 
 
 void mc_launch(bcmc_ctx* ctx, QueryState* q, const McArgs& a, uint32_t max_active, cudaStream_t s)
 {
-    k_mc<<<mc_grid(ctx, max_active), kMcThreads, 0, s>>>(q, a);
+    if (a.host_verts) k_mc<true><<<mc_grid(ctx, max_active), kMcThreads, 0, s>>>(q, a);
+    else k_mc<false><<<mc_grid(ctx, max_active), kMcThreads, 0, s>>>(q, a);
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
 }
