@@ -18,6 +18,11 @@
 // keys are ranked with warp match/popc, each tile publishes its 256 digit
 // counts through decoupled look-back, and keys are scattered via shared memory
 // so that global writes come out in runs.
+//
+// The LRU's age sort skips the histogram kernel: k_slots, which compacts the
+// ages, accumulates the histograms and makes the plan (sort_plan).  When every
+// age has a 16-bit key (age_key16) the plan sorts on that key (sort_key16), so
+// the first pass maps each age through it and two digit passes suffice.
 #include "bcmc_impl.h"
 
 namespace bcmc {
