@@ -138,6 +138,19 @@ def cpu_oracle_time(field, isos, steps: int = 1):
     return len(isos) * steps / dt, oracle.threads(), words
 
 
+def max_over_ranks(value: float, device) -> float:
+    """The slowest rank's figure when a process group is up (every rank calls
+    it); the value itself for a single process."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args):
     """CPU restatement of the reference pipeline, all host threads."""
     rank = int(os.environ.get("RANK", "0"))
@@ -575,11 +588,7 @@ def run_gb300(args):
         e1.synchronize()
         stage_times.append(e0.elapsed_time(e1))
     clk = clocks.stop()
-    ms = float(np.mean(times))
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(float(np.mean(times)), "cuda")
     value = world * len(isos) / (ms / 1000.0)
 
     # e2e: every query's vertices in pinned host memory, through the C ABI:
@@ -599,7 +608,7 @@ def run_gb300(args):
             n_tot = step(**kw)
             times.append(time.perf_counter() - t0)
             d2h = n_tot * 8
-        return world * len(isos) / float(np.mean(times)), d2h
+        return world * len(isos) / max_over_ranks(float(np.mean(times)), "cuda"), d2h
 
     e2e_value, d2h = e2e_pass(to_host=pinned)
     e2e_copy_value, _ = e2e_pass(copy_out=pinned)
