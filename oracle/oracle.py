@@ -340,6 +340,12 @@ class CompressedMarchingCubes:
         p = lib().bcmc_oracle_mc_vertices(self._h)
         return np.ctypeslib.as_array(p, (n, 2)).copy()
 
+    def vertices_view(self, n: int) -> np.ndarray:
+        """The last query's vertices without a copy: valid until the next query."""
+        if n == 0:
+            return np.zeros((0, 2), dtype=np.uint32)
+        return np.ctypeslib.as_array(lib().bcmc_oracle_mc_vertices(self._h), (n, 2))
+
     def ranges(self) -> np.ndarray:
         return np.ctypeslib.as_array(lib().bcmc_oracle_mc_ranges(self._h), (2 * self.total_blocks,)).copy()
 

@@ -13,7 +13,7 @@ copied into the repository: the rewritten sources are written to oracle/_ref/
 The rewrites (no semantic edits to the shader bodies):
   * strip comments, `#version`, `layout(local_size_*) in;`
   * inline `#include "x.comp"` (the C preprocessor keeps include guards)
-  * `layout(...) buffer|uniform Name { members } [inst];` -> namespace-scope
+  * `layout(...) [readonly] buffer|uniform Name { members } [inst];` -> namespace-scope
     variables (runtime-sized arrays become pointers the harness binds)
   * `shared T x[N];` -> namespace-scope array (one workgroup runs at a time)
   * declarations without an initialiser get `{}` (WGSL zero-initialises
@@ -68,6 +68,19 @@ PROGRAMS = {
     "radix_sort_chunk": "radix_sort_chunk.comp",
     "merge_sorted_chunks": "merge_sorted_chunks.comp",
     "reverse_buffer": "reverse_buffer.comp",
+    # LRUCache (js/lru_cache.js): age, mark, extract, init, sort-key copy, assignment
+    "lru_cache_age_slots": "lru_cache_age_slots.comp",
+    "lru_cache_mark_new_items": "lru_cache_mark_new_items.comp",
+    "lru_cache_extract_slot_available": "lru_cache_extract_slot_available.comp",
+    "lru_cache_init": "lru_cache_init.comp",
+    "lru_copy_available_slot_age": "lru_copy_available_slot_age.comp",
+    "lru_cache_update": "lru_cache_update.comp",
+    # ExclusiveScanner (js/exclusive_scan.js): block scan, scan of the block sums, add-back
+    "prefix_sum": "prefix_sum.comp",
+    "block_prefix_sum": "block_prefix_sum.comp",
+    "add_block_sums": "add_block_sums.comp",
+    # StreamCompact (js/stream_compact.js)
+    "stream_compact": "stream_compact.comp",
 }
 # what shaders/embed_shaders.py passes to every shader compile
 DEFINES = ["-DBLOCK_SIZE=512", "-DSORT_CHUNK_SIZE=64"]
@@ -112,7 +125,8 @@ def convert_blocks(s: str) -> str:
                 out.append(f"{decl} {{}};" if "[" in decl else f"{decl} {{}};")
         return "\n".join(out) + "\n"
 
-    return re.sub(r"layout\s*\([^)]*\)\s*(buffer|uniform)\s+(\w+)\s*\{(.*?)\}\s*\w*\s*;", rep, s, flags=re.S)
+    return re.sub(r"layout\s*\([^)]*\)\s*(?:(?:readonly|writeonly|coherent|restrict)\s+)*(buffer|uniform)\s+(\w+)"
+                  r"\s*\{(.*?)\}\s*\w*\s*;", rep, s, flags=re.S)
 
 
 def transform(text: str) -> str:

@@ -34,6 +34,7 @@ struct Fiber {
 ucontext_t g_sched;
 Fiber* g_cur = nullptr;
 void (*g_main)() = nullptr;
+bool g_flat = false;
 
 void fiber_entry()
 {
@@ -46,6 +47,10 @@ void fiber_entry()
 
 void ref_barrier()
 {
+    if (g_flat) {
+        std::fprintf(stderr, "ref_runtime: barrier() in a program dispatched without fibers\n");
+        std::abort();
+    }
     if (!g_cur) return;  // workgroup of one invocation
     swapcontext(&g_cur->ctx, &g_sched);
 }
@@ -96,4 +101,20 @@ void ref_dispatch(void (*main_fn)(), uvec3 groups, uint invocations)
                 }
                 g_cur = nullptr;
             }
+}
+
+void ref_dispatch_flat(void (*main_fn)(), uvec3 groups, uint invocations)
+{
+    g_cur = nullptr;
+    g_flat = true;
+    for (uint z = 0; z < groups.z; ++z)
+        for (uint y = 0; y < groups.y; ++y)
+            for (uint x = 0; x < groups.x; ++x)
+                for (uint i = 0; i < invocations; ++i) {
+                    gl_WorkGroupID = uvec3(x, y, z);
+                    gl_LocalInvocationID = uvec3(i, 0u, 0u);
+                    gl_GlobalInvocationID = uvec3(x * invocations + i, y, z);
+                    main_fn();
+                }
+    g_flat = false;
 }

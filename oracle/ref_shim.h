@@ -383,3 +383,8 @@ void ref_barrier();
 // Runs `invocations` invocations of `main_fn` per workgroup over `groups`
 // workgroups (x-major ids), as fibers that switch at barrier().
 void ref_dispatch(void (*main_fn)(), uvec3 groups, uint invocations);
+
+// The same for programs that call no barrier() and share no workgroup memory:
+// invocations run one after another in id order, without fibers.  A barrier()
+// reached in this mode aborts the process.
+void ref_dispatch_flat(void (*main_fn)(), uvec3 groups, uint invocations);

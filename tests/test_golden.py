@@ -4,6 +4,11 @@
   from the reference's compute shaders compiled as host C++): decode of random
   bit streams at six rates, and full queries (ranges, active flags, active ids,
   blocks with vertices, vertex offsets, packed vertices) on five volumes.
+* Scan and compaction outputs, LRU update sequences (new ids, slot arrays,
+  cachedItemSlots after every update) and query sequences with the LRU cache
+  in the loop, from the reference's scan, compaction, sort and LRU shaders
+  driven the way js/exclusive_scan.js, js/stream_compact.js and
+  js/lru_cache.js drive them.
 * When the reference checkout is present, the same comparison live on further
   seeded cases (oracle/_ref built by oracle/ref_build.py).
 
@@ -14,6 +19,8 @@ import os
 
 import numpy as np
 import pytest
+
+import golden_lru as GL
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 MC_FILES = sorted(glob.glob(os.path.join(GOLDEN, "mc_*.npz")))
@@ -118,3 +125,70 @@ def test_oracle_sort_matches_reference_shaders_live(oracle):
         v = rng.permutation(n).astype(np.uint32)
         for rev in (False, True):
             assert np.array_equal(R.sort_by_key(k, v, rev), oracle.sort_by_key(k, v, rev)[1])
+
+
+# ---- scan, compaction and the LRU cache against the reference's shaders ----
+
+def test_oracle_scan_and_compaction_match_reference_shaders(oracle):
+    for n, v, g, i in GL.scan_cases():
+        aligned = -(-n // 512) * 512
+        buf = np.zeros(aligned, np.uint32)
+        buf[:n] = v
+        scanned, total = oracle.exclusive_scan(buf, n, aligned)
+        GL.check_scan(g, i, n, scanned, total)
+        flags = (v != 0).astype(np.uint32)
+        offs, m = oracle.exclusive_scan(np.concatenate([flags, np.zeros(aligned - n, np.uint32)]), n, aligned)
+        GL.check_compact(g, i, n, oracle.compact(flags, offs, n, m))
+
+
+@pytest.mark.parametrize("seq", range(3))
+def test_oracle_lru_matches_reference_shaders(oracle, seq):
+    total, initial, steps, reset_at, recs = list(GL.lru_sequences())[seq]
+    c = oracle.LRUCache(initial, total)
+    for step, rec in enumerate(recs):
+        if step == reset_at:
+            c.reset()
+        ids = c.update(rec["needed"])
+        assert np.array_equal(ids, rec["new"]), step
+        assert c.cache_size == rec["cache_size"], step
+        if len(ids):
+            assert c.slots_available == rec["display"], step
+        GL.check_lru_state(rec, c.state(), step)
+
+
+def test_oracle_pipeline_lru_matches_reference_shaders(oracle):
+    for name, frac, isos, reset_at, recs in GL.lru_pipeline_cases():
+        g = np.load(os.path.join(GOLDEN, f"mc_{name}.npz"))
+        m = oracle.CompressedMarchingCubes(g["words"], int(g["rate"]), tuple(int(d) for d in g["dims"]),
+                                           initial_cache_fraction=frac)
+        for qi, (iso, rec) in enumerate(zip(isos, recs)):
+            if qi == reset_at:
+                m.cache_reset()
+            n = m.compute_surface(float(iso))
+            nverts, n_active, n_new, n_with = rec["counts"]
+            assert n == nverts, (name, qi)
+            if n_active:
+                s = m.stats()
+                assert (s["numActiveBlocks"], s["newDecompressed"], s["numBlocksWithVertices"]) == \
+                    (n_active, n_new, n_with), (name, qi)
+            assert GL.sha(m.vertices(n).reshape(-1)) == rec["mesh_sha"], (name, qi)
+            GL.check_lru_state(rec, m.lru_state(), (name, qi))
+
+
+def test_oracle_lru_matches_reference_shaders_live(oracle):
+    """A further seeded sequence (small cache, frequent growth) through the
+    reference's LRU, scan, compaction and sort shaders, live."""
+    R = _ref()
+    rng = np.random.default_rng(4242)
+    total = 1200
+    a, b = R.LRUCache(40, total), oracle.LRUCache(40, total)
+    for step in range(16):
+        if step == 12:
+            a.reset()
+            b.reset()
+        needed = (np.convolve(rng.random(total) < rng.uniform(0.002, 0.05), np.ones(6), mode="same") > 0)
+        needed = needed.astype(np.uint32)
+        assert np.array_equal(a.update(needed), b.update(needed)), step
+        sa = a.state()
+        assert sa["cache_size"] == b.cache_size
+        GL.check_lru_state({**sa, "total": total}, b.state(), step)

@@ -1,16 +1,17 @@
 """Full-size workloads, checked through properties that do not need the
 oracle to run the whole workload:
 
-* 512^3 spectral field, rate 2, cache 25 %, a 64-isovalue random walk: the
-  first queries against the oracle (vertices, statistics, LRU state), then
-  every query of the walk through the plain path and the batched engine,
-  which must agree bit for bit.
+* 512^3 spectral field, rate 2, cache 25 %, a 64-isovalue random walk: every
+  query against the oracle (vertices, statistics, LRU slot arrays and
+  cachedItemSlots), then every query of the walk through the batched engine,
+  which must agree with the plain path bit for bit.
 * 1024x1024x1080 at rate 4 (17,694,720 blocks): block bit offsets pass 2^32
   (block 2^24 and beyond), where the reference's u32 offset would wrap; the
   decoder must follow the 64-bit offset -- checked block by block against the
   oracle's decoder on a random stream, with the full-volume decode and the
-  block ranges -- and a query on the volume must agree between the plain path
-  and the engine."""
+  block ranges -- and queries on the CT-like volume of that size must agree
+  between the plain path and the engine, and one of them with the oracle
+  (vertices, statistics and LRU state)."""
 import numpy as np
 import pytest
 
@@ -47,16 +48,15 @@ def test_spectral512_random_walk(ctx, oracle):
         n = mc.computeSurface(iso)
         verts = mc.copyVertices().copy()
         plain.append((n, verts))
-        if qi < 3:
-            n_ref = ref.compute_surface(iso)
-            assert n == n_ref and n > 0, (qi, n, n_ref)
-            assert np.array_equal(verts, ref.vertices(n_ref)), qi
-            st, rs = mc.stats(), ref.stats()
-            for k in ("numActiveBlocks", "newDecompressed", "numBlocksWithVertices", "cacheSize"):
-                assert st[k] == rs[k], (qi, k)
-            g, r = mc.lruCache.state(), ref.lru_state()
-            for k in ("item_slots", "age", "avail", "item"):
-                assert np.array_equal(g[k], r[k]), (qi, k)
+        n_ref = ref.compute_surface(iso)
+        assert n == n_ref and n > 0, (qi, n, n_ref)
+        assert np.array_equal(verts, ref.vertices_view(n_ref)), qi
+        st, rs = mc.stats(), ref.stats()
+        for k in ("numActiveBlocks", "newDecompressed", "numBlocksWithVertices", "cacheSize"):
+            assert st[k] == rs[k], (qi, k)
+        g, r = mc.lruCache.state(), ref.lru_state()
+        for k in ("item_slots", "age", "avail", "item"):
+            assert np.array_equal(g[k], r[k]), (qi, k)
     del ref
     eng = bcmc.Engine(ctx)
     vid = eng.addVolume(stream, rate, dims)
@@ -110,12 +110,12 @@ def test_1024x1024x1080_block_offsets_past_2_24(ctx, oracle):
             assert not np.array_equal(wrapped.view(np.uint32), want.view(np.uint32)) or not want.any(), b
 
 
-def test_1024x1024x1080_query_plain_equals_engine(ctx):
+def test_1024x1024x1080_query_plain_equals_engine_and_oracle(ctx, oracle):
     import torch
 
     rate = 4
     field = D.ct_uint16_torch(BIG_DIMS, 5)
-    _, _, stream = _encode_on_gpu(ctx, field, rate, BIG_DIMS)
+    _, words, stream = _encode_on_gpu(ctx, field, rate, BIG_DIMS)
     del field
     torch.cuda.empty_cache()
     c = bcmc.Context(ctx.device, initial_cache_fraction=0.1)
@@ -123,7 +123,8 @@ def test_1024x1024x1080_query_plain_equals_engine(ctx):
     mc.setCompressedVolume(stream, rate, BIG_DIMS)
     eng = bcmc.Engine(ctx)
     vid = eng.addVolume(stream, rate, BIG_DIMS)
-    for iso in (2500.0, 3600.0):
+    ref = oracle.CompressedMarchingCubes(words, rate, BIG_DIMS, initial_cache_fraction=0.1)
+    for qi, iso in enumerate((2500.0, 3600.0)):
         n = mc.computeSurface(iso)
         assert n > 0
         res = eng.run([(vid, iso)])
@@ -132,3 +133,15 @@ def test_1024x1024x1080_query_plain_equals_engine(ctx):
         off = int(res[0]["vertex_offset"])
         b = eng.vertexBuffer.torch()[off: off + n]
         assert torch.equal(a, b), iso
+        del a, b
+        if qi == 0:  # the oracle runs the first query (some 7 M active blocks)
+            n_ref = ref.compute_surface(iso)
+            assert n == n_ref, (iso, n, n_ref)
+            assert np.array_equal(mc.copyVertices(), ref.vertices_view(n_ref)), iso
+            st, rs = mc.stats(), ref.stats()
+            for k in ("numActiveBlocks", "newDecompressed", "numBlocksWithVertices", "cacheSize"):
+                assert st[k] == rs[k], (iso, k)
+            g, r = mc.lruCache.state(), ref.lru_state()
+            for k in ("item_slots", "age", "avail", "item"):
+                assert np.array_equal(g[k], r[k]), (iso, k)
+            del ref

@@ -100,3 +100,65 @@ def test_sort_matches_reference_shaders(ctx):
             kd, vd = to_dev(k), to_dev(v)
             bcmc.RadixSorter(ctx).sort(kd, vd, len(k), rev)
             assert np.array_equal(to_host(vd, np.uint32), want), (i, rev)
+
+
+# ---- scan, compaction and the LRU cache against the reference's shaders ----
+
+import golden_lru as GL  # noqa: E402
+
+
+def test_scan_and_compaction_match_reference_shaders(ctx):
+    import torch
+
+    from gpu_util import to_host
+
+    pipe = bcmc.ExclusiveScanPipeline(ctx)
+    sc = bcmc.StreamCompact(ctx)
+    for n, v, g, i in GL.scan_cases():
+        s = pipe.prepareInput(v)
+        total = s.scan(n)
+        GL.check_scan(g, i, n, to_host(s.inputBuf, np.uint32), total)
+        flags = (v != 0).astype(np.uint32)
+        fs = pipe.prepareInput(flags)
+        m = fs.scan(n)
+        out = torch.zeros(max(m, 1), dtype=torch.int32, device="cuda")
+        sc.compactActiveIDs(n, to_dev(flags), fs.inputBuf, out)
+        GL.check_compact(g, i, n, to_host(out, np.uint32)[:m])
+
+
+@pytest.mark.parametrize("seq", range(3))
+def test_lru_matches_reference_shaders(ctx, seq):
+    total, initial, steps, reset_at, recs = list(GL.lru_sequences())[seq]
+    c = bcmc.LRUCache(ctx, None, None, initial, 256, total)
+    for step, rec in enumerate(recs):
+        if step == reset_at:
+            c.reset()
+        n, ids = c.update(to_dev(rec["needed"]))
+        assert n == len(rec["new"]), step
+        if n:
+            assert np.array_equal(ids.numpy(), rec["new"]), step
+            assert c.displayNumSlotsAvailable == rec["display"], step
+        assert c.cacheSize == rec["cache_size"], step
+        GL.check_lru_state(rec, c.state(), step)
+
+
+def test_pipeline_lru_matches_reference_shaders(ctx):
+    """computeSurface sequences with the cache in the loop: per query the
+    counts, the mesh and the LRU's slot arrays and cachedItemSlots."""
+    for name, frac, isos, reset_at, recs in GL.lru_pipeline_cases():
+        g = np.load(os.path.join(GOLDEN, f"mc_{name}.npz"))
+        c = bcmc.Context(ctx.device, initial_cache_fraction=frac)
+        mc = bcmc.CompressedMarchingCubes(c)
+        mc.setCompressedVolume(_stream_bytes(g), int(g["rate"]), tuple(int(d) for d in g["dims"]))
+        for qi, (iso, rec) in enumerate(zip(isos, recs)):
+            if qi == reset_at:
+                mc.lruCache.reset()
+            n = mc.computeSurface(float(iso))
+            nverts, n_active, n_new, n_with = rec["counts"]
+            assert n == nverts, (name, qi)
+            if n_active:
+                st = mc.stats()
+                assert (st["numActiveBlocks"], st["newDecompressed"], st["numBlocksWithVertices"]) == \
+                    (n_active, n_new, n_with), (name, qi)
+            assert GL.sha(mc.copyVertices().reshape(-1)) == rec["mesh_sha"], (name, qi)
+            GL.check_lru_state(rec, mc.lruCache.state(), (name, qi))
