@@ -33,8 +33,9 @@ The rewrites (no semantic edits to the shader bodies):
   * every program lives in its own namespace and translation unit
 
 Usage: python oracle/ref_build.py [--reference DIR]
-(default DIR: $BCMC_REFERENCE or /root/reference).  Exits 0 with a message and
-builds nothing when the reference checkout is absent.
+(default DIR: $BCMC_REFERENCE, else a checkout named `reference` beside this
+repository's folder).  Exits 0 with a message and builds nothing when the
+reference checkout is absent.
 """
 from __future__ import annotations
 
@@ -89,7 +90,8 @@ PROGRAM_DEFINES = {"mc_isosurface_vert_fog": ["DRAW_FOG"], "mc_isosurface_frag_f
 
 
 def reference_dir(arg: str | None) -> str:
-    return arg or os.environ.get("BCMC_REFERENCE") or "/root/reference"
+    beside = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+    return arg or os.environ.get("BCMC_REFERENCE") or beside
 
 
 def strip_comments(s: str) -> str:
