@@ -17,6 +17,12 @@ Lines printed (one JSON line on rank 0):
           from a second timed pass with a perf tracker (its stage events
           slow each query down, so the headline pass runs without them)
   cpu_baseline  the CPU oracle (OpenMP, all host cores) on one step
+  decode  full-volume ZFP decode of the 512^3 spectral field at rate 2, GB/s
+  walk    the plain path on that field's 64-isovalue random walk (cache 25 %),
+          with the oracle on the walk's first 8 queries beside it
+  batched / served / render_ms  the batched engine, the continuous-batching
+          server and the render pass, each summarised; their full records
+          (per-rate sweeps, autotune choices) go to gpurun_out/bench_detail.json
 
 `--impl reference` times the CPU restatement of the reference pipeline (the
 reference itself is WebGPU/JavaScript and has no CPU path) on the same config.
@@ -120,7 +126,9 @@ def encode_on_gpu(ctx, field):
     return words, host
 
 
-def cpu_oracle_time(field, isos, steps: int = 1):
+def cpu_oracle_time(field, isos, steps: int = 1, warmup: int = 1):
+    """The oracle (C, OpenMP over all host threads) on `steps` timed steps after
+    `warmup` untimed ones (each: cache reset + the query sequence)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
@@ -128,7 +136,10 @@ def cpu_oracle_time(field, isos, steps: int = 1):
     words = oracle.zfp_encode(field, CONFIG["rate"])
     m = oracle.CompressedMarchingCubes(words, CONFIG["rate"], CONFIG["dims"],
                                        initial_cache_fraction=CONFIG["cache_fraction"])
-    m.compute_surface(float(isos[0]))  # warm caches / threads
+    for _ in range(warmup):
+        m.cache_reset()
+        for iso in isos:
+            m.compute_surface(float(iso))
     t0 = time.perf_counter()
     for _ in range(steps):
         m.cache_reset()
@@ -158,9 +169,7 @@ def run_reference(args):
         return
     field, isos = make_volume()
     steps = max(1, args.steps)
-    for _ in range(args.warmup):
-        pass
-    qps, threads, _ = cpu_oracle_time(field, isos, steps=steps)
+    qps, threads, _ = cpu_oracle_time(field, isos, steps=steps, warmup=args.warmup)
     line = {"impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
             "steps": steps, "warmup": args.warmup, "ms_per_step": 1000.0 * len(isos) / qps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -174,10 +183,14 @@ def run_reference(args):
 
 DECODE = dict(workload="turb512: 512^3 k^-5/3 spectral field, ZFP rate 2, full-volume decode "
                        "(2,097,152 blocks -> 512 MiB float32)", dims=(512, 512, 512), rate=2, seed=3)
+WALK = dict(workload="turb512 walk: 512^3 k^-5/3 spectral field, ZFP rate 2, cache 25% of 2,097,152 blocks, "
+                     "64 isovalues on a seeded +-0.02 random walk from 0, one at a time, cache reset per step",
+            queries=64, seed=3, cache_fraction=0.25, cpu_queries=8)
 
 
-def decode_bench(ctx, flush, reps: int = 10) -> dict:
-    """Full-volume ZFP decode throughput: blocks * (8*rate + 256) B / event time."""
+def turb512_stream(ctx):
+    """The 512^3 spectral field, ZFP-encoded at rate 2 on the GPU: (device
+    words, host stream bytes, block count)."""
     import torch
 
     import bcmc
@@ -186,8 +199,20 @@ def decode_bench(ctx, flush, reps: int = 10) -> dict:
     dims, rate = DECODE["dims"], DECODE["rate"]
     f = torch.from_numpy(D.turbulence(dims, DECODE["seed"])).cuda()
     words = bcmc.zfp_encode(ctx, f, rate)
+    torch.cuda.synchronize()
     del f
     nb = int(np.prod([(d + 3) // 4 for d in dims]))
+    host = words.cpu().numpy().view(np.uint8)[: nb * 8 * rate].copy()
+    return words, host, nb
+
+
+def decode_bench(ctx, flush, words, nb, reps: int = 10) -> dict:
+    """Full-volume ZFP decode throughput: blocks * (8*rate + 256) B / event time."""
+    import torch
+
+    import bcmc
+
+    rate = DECODE["rate"]
     out = torch.empty(nb * 64, dtype=torch.float32, device="cuda")
     L = bcmc._lib.load()
     torch.cuda.synchronize()
@@ -214,10 +239,72 @@ def decode_bench(ctx, flush, reps: int = 10) -> dict:
     algo = nb * (8 * rate + 256)
     peak, peak_kind = _peaks()
     gbs = algo / (ms / 1000.0) / 1e9
-    del out, words
+    del out
     return {"workload": DECODE["workload"], "unit": "GB/s", "value": gbs, "ms": ms, "peak": peak,
             "peak_kind": peak_kind, "frac": gbs / peak, "algorithmic_bytes": algo,
             "kernel": "k_decode_volume", "l2": "flushed (512 MB write) before each rep"}
+
+
+def walk_bench(ctx, flush, host_stream, steps: int, warmup: int, cpu: bool) -> dict:
+    """The plain per-query path on the cache-bound 512^3 walk (js/run_benchmark.js
+    style: a sequence of isovalues after a cache reset): iso-queries/s from CUDA
+    events on the library's stream, per-query host latency, and the oracle on
+    the walk's first queries."""
+    import torch
+
+    import bcmc
+    from bcmc import datasets as D
+
+    dims, rate = DECODE["dims"], DECODE["rate"]
+    isos = [float(np.float32(v)) for v in D.random_walk(WALK["queries"], WALK["seed"])]
+    c = bcmc.Context(ctx.device, initial_cache_fraction=WALK["cache_fraction"])
+    mc = bcmc.CompressedMarchingCubes(c)
+    mc.setCompressedVolume(host_stream, rate, dims)
+    s = torch.cuda.ExternalStream(c.stream)
+
+    def step(lat=None):
+        mc.lruCache.reset()
+        for iso in isos:
+            t0 = time.perf_counter()
+            mc.computeSurface(iso)
+            if lat is not None:
+                lat.append(1000.0 * (time.perf_counter() - t0))
+
+    for _ in range(max(1, warmup)):
+        step()
+    times, lat = [], []
+    for _ in range(max(1, steps)):
+        flush.fill_(3)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        step(lat)
+        e1.record(s)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = float(np.mean(times))
+    out = {"workload": WALK["workload"], "value": len(isos) / (ms / 1000.0), "unit": "queries/s",
+           "ms_per_step": ms, "steps": max(1, steps), "cache_size": mc.stats()["cacheSize"],
+           "p50_ms": float(np.percentile(lat, 50)), "p95_ms": float(np.percentile(lat, 95)),
+           "p99_ms": float(np.percentile(lat, 99))}
+    del mc
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        oracle.build()
+        words = np.frombuffer(host_stream.tobytes() + bytes(16), dtype=np.uint64)
+        m = oracle.CompressedMarchingCubes(words, rate, dims, initial_cache_fraction=WALK["cache_fraction"])
+        k = WALK["cpu_queries"]
+        m.compute_surface(isos[0])  # warm-up (threads, pages)
+        m.cache_reset()
+        t0 = time.perf_counter()
+        for iso in isos[:k]:
+            m.compute_surface(iso)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": k / dt, "unit": "queries/s", "cores": oracle.threads(), "kind": "port",
+                               "sample": f"the walk's first {k} queries from a reset cache, CPU oracle (C, OpenMP)"}
+    return out
 
 
 RENDER = dict(width=1920, height=1080, reps=20)
@@ -491,8 +578,8 @@ def served_bench() -> dict:
                      "evicted_blocks": st["evicted_blocks"]}}
 
 
-# DRAM bytes (read + write) per launch from one ncu capture of this workload's
-# launch list (profiles/ct256_launch_list.md), mean over the 16-isovalue sweep
+# DRAM bytes (read + write) per launch of k_mc on this workload, from one ncu
+# capture (mean over the 16-isovalue sweep): a profile constant, reported as such
 NCU_TRAFFIC = {"k_mc": 42.037e6}
 
 
@@ -508,6 +595,34 @@ def algorithmic_bytes(stage: str, st: dict, rate: int, total_blocks: int) -> flo
     if stage == "cacheUpdate":  # k_slots + sort: 3 slot arrays rw + sort passes
         return st["cacheSize"] * (12 + 12) + st["slotsAvailable"] * 16
     return 0.0
+
+
+# The full per-leg record (per-rate sweeps, autotune choices, stage passes) goes
+# to this file; the printed line keeps each leg's headline figures.
+DETAIL = "gpurun_out/bench_detail.json"
+
+
+def _pick(d, keys):
+    return None if d is None else {k: d[k] for k in keys if k in d}
+
+
+def _batched_summary(b):
+    if b is None:
+        return None
+    return {"queries_per_s": b["batched"]["queries_per_s"], "plain_queries_per_s": b["plain"]["queries_per_s"],
+            "speedup_qps": b["speedup_qps"], "p50_ms": b["batched"]["p50_ms"], "p99_ms": b["batched"]["p99_ms"],
+            "plain_p99_ms": b["plain"]["p99_ms"], "identical_to_plain": b["identical_to_plain"]}
+
+
+def _served_summary(sv):
+    if sv is None:
+        return None
+    ok = [r for r in sv["served"] if r["achieved_qps"] >= 0.95 * r["offered_qps"]]
+    top = max(ok, key=lambda r: r["achieved_qps"]) if ok else None
+    return {"plain_queries_per_s": sv["plain"]["queries_per_s"], "plain_p99_ms": sv["plain"]["p99_ms"],
+            "max_sustained_qps": top["achieved_qps"] if top else None, "p99_ms_at_max": top["p99_ms"] if top else None,
+            "best_ratio_at_equal_p99": sv["best_ratio_at_equal_p99"],
+            "ratios_at_equal_p99": [round(r["ratio"], 3) for r in sv["served_vs_plain_at_equal_p99"]]}
 
 
 def run_gb300(args):
@@ -634,7 +749,14 @@ def run_gb300(args):
     kernel_of = {"computeVertices": "k_mc", "decompression": "k_decode_new + k_assign (ZFP decode beside the cache update, slot assignment and copy)",
                  "computeActiveBlocks": "k_active", "cacheUpdate": "k_slots + radix sort"}
 
-    decode = decode_bench(ctx, flush) if not args.no_decode else None
+    decode = walk = None
+    if not (args.no_decode and args.no_walk):
+        turb_words, turb_host, turb_nb = turb512_stream(ctx)
+        decode = decode_bench(ctx, flush, turb_words, turb_nb) if not args.no_decode else None
+        del turb_words
+        torch.cuda.empty_cache()
+        walk = walk_bench(ctx, flush, turb_host, max(3, args.steps // 10), max(args.warmup, 3),
+                          cpu=(rank == 0 and world == 1 and not args.no_cpu)) if not args.no_walk else None
     batched = batched_bench() if not args.no_batched else None
     served = served_bench() if not args.no_served else None
     render = render_bench(mc, isos) if not args.no_render else None
@@ -646,37 +768,49 @@ def run_gb300(args):
                "sample": "1 step (cache reset + 16 queries) of the same workload, CPU oracle (C, OpenMP)"}
 
     if rank == 0:
+        e2e = {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": 4 * len(isos),
+               "d2h_bytes_per_step": d2h,
+               "what": "bcmc_compute_surface_host per query: vertices stored into pinned host memory "
+                       "by the kernels (host wall time per step)",
+               "compute_then_copy": {"value": e2e_copy_value,
+                                     "what": "bcmc_compute_surface + bcmc_copy_vertices per query"}}
+        roofline = {"bound": "hbm", "kernel": kernel_of[dominant], "achieved": achieved, "peak": peak,
+                    "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                    "traffic": NCU_TRAFFIC.get(kernel_of[dominant]), "avg_launch_ms": avg_ms,
+                    "algorithmic_bytes": bytes_per_launch,
+                    "traffic_source": "a constant from one ncu capture of this kernel on this workload "
+                                      "(dram bytes read+write per launch), not measured in this run"}
         line = {"metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
                 "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded CT-like field, ZFP-encoded on the GPU by the project's encoder)",
                 "config": {"workload": CONFIG["workload"], "l2": "flushed (512 MB write) between steps",
                            "parallelism": f"replicas x{world}"},
-                "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": 4 * len(isos),
-                        "d2h_bytes_per_step": d2h,
-                        "what": "bcmc_compute_surface_host per query: vertices stored into pinned host memory "
-                                "by the kernels (host wall time per step)",
-                        "compute_then_copy": {"value": e2e_copy_value,
-                                              "what": "bcmc_compute_surface + bcmc_copy_vertices per query"}},
-                "roofline": {"bound": "hbm", "kernel": kernel_of[dominant], "achieved": achieved, "peak": peak,
-                             "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                             "traffic": NCU_TRAFFIC.get(kernel_of[dominant]), "avg_launch_ms": avg_ms,
-                             "algorithmic_bytes": bytes_per_launch,
-                             "traffic_source": "profiles/ct256_launch_list.md (ncu dram bytes read+write, "
-                                               "mean over the sweep's launches)"},
+                "e2e": e2e,
+                "roofline": roofline,
                 "stage_ms_per_query": {s: tot[s] / nq for s in stages},
-                "stage_pass_ms_per_step": float(np.mean(stage_times)),
                 "latency_ms": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
-                               "p99": float(np.percentile(lat, 99)), "queries": len(lat),
-                               "what": "host wall time of each computeSurface call (returns the vertex count)"},
-                "decode": decode,
-                "batched": batched,
-                "served": served,
-                "render": render,
+                               "p99": float(np.percentile(lat, 99))},
+                "decode": _pick(decode, ("value", "unit", "frac", "ms", "peak_kind")),
+                "walk": _pick(walk, ("value", "unit", "p50_ms", "p99_ms", "cache_size")),
+                "walk_cpu_baseline": _pick((walk or {}).get("cpu_baseline"), ("value", "unit", "cores", "kind")),
+                "batched": _batched_summary(batched),
+                "served": _served_summary(served),
+                "render_ms": {k: render[k]["ms"] for k in ("plain", "fog")} if render else None,
                 "gpu_launches": int(launches),
                 "clocks": clk,
-                "volume_load_s": load_s,
-                "cpu_baseline": cpu}
+                "cpu_baseline": cpu,
+                "detail_file": DETAIL}
+        detail = dict(line, e2e=e2e, roofline=roofline, decode=decode, walk=walk, batched=batched, served=served,
+                      render=render, stage_pass_ms_per_step=float(np.mean(stage_times)), volume_load_s=load_s,
+                      latency_ms=dict(line["latency_ms"], queries=len(lat),
+                                      what="host wall time of each computeSurface call"))
+        try:
+            os.makedirs(os.path.dirname(os.path.join(ROOT, DETAIL)), exist_ok=True)
+            with open(os.path.join(ROOT, DETAIL), "w") as f:
+                json.dump(detail, f, indent=1)
+        except OSError:
+            line["detail_file"] = None
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -690,6 +824,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-decode", action="store_true", help="skip the full-volume decode leg")
+    ap.add_argument("--no-walk", action="store_true", help="skip the 512^3 random-walk leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-engine leg")
     ap.add_argument("--no-served", action="store_true", help="skip the served (continuous batching) leg")
     ap.add_argument("--no-render", action="store_true", help="skip the render-pass leg")

@@ -76,6 +76,17 @@ bcmc_status bcmc_ctx_synchronize(bcmc_ctx* ctx);
  * No reference counterpart: lets callers account for the GPU work behind a
  * call (e.g. kernels per query). */
 uint64_t bcmc_kernel_launches(void);
+/* Test hook, no reference counterpart (the reference's only guards are alerts,
+ * js/lru_cache.js:315-317, js/exclusive_scan.js:117-119).  With
+ * tile_plus_one = t + 1, tile t of the active test of every later query on
+ * this context, and of its primitive scans (bcmc_scan_exclusive_u32[_async],
+ * bcmc_select_ids), publishes no decoupled look-back status: the tiles after
+ * it wait on a status word that nothing sets until their bounded spin runs
+ * out (about a second), and the call returns BCMC_E_TIMEOUT.  A query that
+ * times out resets its volume's cache (the slot arrays are not trusted after
+ * a wait gave up), so the next query starts from an empty cache.  0 turns the
+ * hook off.  Nothing faults or hangs: the waits are bounded. */
+bcmc_status bcmc_debug_drop_tile(bcmc_ctx* ctx, uint32_t tile_plus_one);
 
 /* ---- CompressedMarchingCubes -------------------------------------------- */
 /* setCompressedVolume(volume, compressionRate, volumeDims, volumeScale)
@@ -212,14 +223,19 @@ bcmc_status bcmc_scan_exclusive_u32_async(bcmc_ctx* ctx, const uint32_t* d_in, u
  * context and without any device allocation, for callers that may not
  * allocate on the call (a runtime that owns all device memory through its own
  * pool, or one that cannot take an allocation's implicit synchronisation) or
- * hold no context.  Scratch is a fixed ~132 KB static array per device, so
- * n > BCMC_SCAN_NOALLOC_MAX_N returns BCMC_E_LIMIT with nothing launched.
- * Runs on the calling thread's current device; `stream` NULL is the legacy
- * default stream (there is no context stream).  The first call on a device
- * does its one-time set-up (looks up the scratch array's device address and
- * the SM count), so make it before any stream capture on that device.  Calls
- * on one device share the scratch: calls that may run concurrently (other
- * streams or threads without ordering) race, and their results are undefined.
+ * hold no context.  Scratch is a fixed static array of 137,480 bytes (about
+ * 134 KiB) per device, so n > BCMC_SCAN_NOALLOC_MAX_N returns BCMC_E_LIMIT
+ * with nothing launched.  Runs in the calling thread's current CUDA context
+ * (the device's primary context when none is current); `stream` NULL is the
+ * legacy default stream (there is no context stream).  The first call in a
+ * context does its one-time set-up there (looks up the scratch array's device
+ * address in that context and the SM count), so make it before any stream
+ * capture in that context; a new context (after a device reset, or one the
+ * caller creates) gets its own set-up.  Calls on one device share the
+ * scratch: calls that may run concurrently (other streams or threads without
+ * ordering) race, and their results are undefined.  A look-back wait that
+ * runs out of spins is not reported here (its prefixes are wrong and the call
+ * still returns BCMC_OK); the context-based scans report BCMC_E_TIMEOUT.
  * Failures: BCMC_E_ARG (null pointers with n > 0), BCMC_E_CUDA (set-up or
  * launch). */
 #define BCMC_SCAN_NOALLOC_MAX_N (1u << 26)

@@ -45,7 +45,7 @@ def test_noalloc_scan_matches_context_scan_two_calls_in_a_row(ctx):
         assert st == 0
     torch.cuda.synchronize()
 
-    # first no-alloc call does the per-device set-up; the rest must not allocate
+    # first no-alloc call does the per-context set-up; the rest must not allocate
     assert L.bcmc_scan_exclusive_u32_noalloc(None, None, 0, C.c_void_p(tot_na.data_ptr()),
                                              C.c_void_p(stream)) == 0
     torch.cuda.synchronize()

@@ -115,6 +115,7 @@ SIGNATURES = {
     "bcmc_ctx_stream": (P, [P]),
     "bcmc_ctx_synchronize": (C.c_int, [P]),
     "bcmc_kernel_launches": (U64, []),
+    "bcmc_debug_drop_tile": (C.c_int, [P, U32]),
     "bcmc_volume_create": (C.c_int, [P, P, C.c_size_t, U32, U32P, C.POINTER(C.c_float), C.POINTER(P)]),
     "bcmc_volume_create_device": (C.c_int, [P, P, C.c_size_t, U32, U32P, C.POINTER(C.c_float), C.POINTER(P)]),
     "bcmc_volume_destroy": (None, [P]),

@@ -560,6 +560,18 @@ void bcmc_ctx_destroy(bcmc_ctx* ctx)
 
 const char* bcmc_last_error(const bcmc_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "no context"; }
 
+bcmc_status bcmc_debug_drop_tile(bcmc_ctx* ctx, uint32_t tile_plus_one)
+{
+    if (!ctx) return BCMC_E_ARG;
+    return guarded(ctx, [&]() -> bcmc_status {
+        ctx->debug_drop_tile = tile_plus_one;
+        BCMC_CUDA(cudaMemcpyAsync(&ctx->d_prim->debug_drop_tile, &ctx->debug_drop_tile, 4, cudaMemcpyHostToDevice,
+                                  ctx->stream));
+        BCMC_CUDA(cudaStreamSynchronize(ctx->stream));
+        return BCMC_OK;
+    });
+}
+
 void* bcmc_ctx_stream(bcmc_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
 bcmc_status bcmc_ctx_synchronize(bcmc_ctx* ctx)
@@ -660,6 +672,8 @@ static void vol_ensure_graph(bcmc_vol* v, int mode, uint2* out = nullptr)
 // One query: into the volume's vertex buffer (host_out null), or straight
 // into a page-locked host buffer of host_cap vertices (host_out = its device
 // address).
+static bcmc_status lru_reset_impl(bcmc_lru* c);
+
 static bcmc_status vol_query(bcmc_vol* v, float iso, bcmc_perf* perf, uint32_t* num_vertices, uint2* host_out,
                              uint64_t host_cap)
 {
@@ -672,11 +686,18 @@ static bcmc_status vol_query(bcmc_vol* v, float iso, bcmc_perf* perf, uint32_t* 
         for (int attempt = 0;; ++attempt) {
             vol_ensure_graph(v, mode, host_out);
             lru_epoch_tick(c, s);
-            *v->h_in = QueryInputs{iso, c->capacity, out_cap, 0u};
+            *v->h_in = QueryInputs{iso, c->capacity, out_cap, 0u, ctx->debug_drop_tile};
             BCMC_CUDA(cudaGraphLaunch(v->graph[mode], s));
             count_launches(v->graph_kernels);
             BCMC_CUDA(cudaStreamSynchronize(s));
-            if (c->h_q->error) return fail(ctx, BCMC_E_TIMEOUT, "device wait timed out (site " + std::to_string(c->h_q->error) + ")");
+            if (c->h_q->error) {
+                // the cache's slot arrays are not trusted after a wait gave up: reset them
+                // over the logical size the query reached
+                const uint32_t site = c->h_q->error;
+                c->cache_size = std::min(std::max(c->cache_size, c->h_q->cache_size), c->capacity);
+                lru_reset_impl(c);
+                return fail(ctx, BCMC_E_TIMEOUT, "device wait timed out (site " + std::to_string(site) + ")");
+            }
             if (c->h_q->grow_needed) {
                 if (attempt > 2) return fail(ctx, BCMC_E_STATE, "cache growth did not converge");
                 lru_grow_capacity(c, c->h_q->grow_needed);

@@ -30,6 +30,8 @@ struct bcmc_ctx {
     // release until the last of them is destroyed
     uint32_t children = 0;
     bool destroy_pending = false;
+    // test hook (bcmc_debug_drop_tile): 0, or the dropped tile + 1
+    uint32_t debug_drop_tile = 0;
 };
 
 namespace bcmc {

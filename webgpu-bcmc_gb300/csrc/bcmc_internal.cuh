@@ -25,6 +25,7 @@ struct QueryInputs {
     uint32_t capacity;
     uint32_t vert_capacity;
     uint32_t mc_only;
+    uint32_t debug_drop_tile;  // test hook (bcmc_debug_drop_tile): 0, or tile + 1
 };
 
 struct QueryState {
@@ -65,8 +66,18 @@ struct QueryState {
     uint32_t sort_wide;       // set by k_slots when an available slot's age has no 16-bit key
     uint32_t sort_hist[4][256];
     uint32_t sort_hist16[2][256];  // k_slots: digit histograms of the 16-bit age keys
-    uint32_t pad[8];
+    // test hook (bcmc_debug_drop_tile): 0, or t + 1 when tile t of the active
+    // test and of the primitive scans must publish no look-back status
+    uint32_t debug_drop_tile;
+    uint32_t pad[7];
 };
+
+// The test hook's check: this tile publishes nothing, so the tiles after it
+// wait on a status word that nobody sets until their bounded spin runs out.
+__device__ __forceinline__ bool lb_dropped(const QueryState* q, uint32_t tile)
+{
+    return q->debug_drop_tile == tile + 1u;
+}
 
 // The LRU's slot ages (lru_cache.comp, lru_cache_init.comp) are small counts
 // for slots used since the cache was (re)initialised and 100000 plus a count

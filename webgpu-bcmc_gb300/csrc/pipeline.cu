@@ -57,6 +57,7 @@ __global__ void k_query_begin(QueryState* q, float iso, int mc_only, uint32_t ca
         q->num_with_verts = 0;
         q->num_verts = 0;
         if (!mc_only) {
+            q->debug_drop_tile = in ? __ldcv(&in->debug_drop_tile) : 0u;
             q->isovalue = iso;
             q->tiles_active = q->tiles_slots = q->tiles_sort_hist = 0;
             for (int i = 0; i < 4; ++i) q->tiles_sort[i] = 0;
@@ -237,10 +238,12 @@ __global__ void __launch_bounds__(kActRThreads, 1) k_active_ranges(QueryState* q
         const uint32_t excl =
             cta_exclusive_scan<kActRThreads>((uint32_t)__popc(act) | ((uint32_t)__popc(need) << 16), s_warp, &tot);
         if (t < 32) {
-            const uint32_t p = warp_lookback(a.status_a, tile, tot & 0xffffu, epoch, &q->error, 30u);
+            const uint32_t p =
+                lb_dropped(q, tile) ? 0u : warp_lookback(a.status_a, tile, tot & 0xffffu, epoch, &q->error, 30u);
             if (t == 0) s_pa = p;
         } else if (t < 64) {
-            const uint32_t p = warp_lookback(a.status_n, tile, tot >> 16, epoch, &q->error, 31u);
+            const uint32_t p =
+                lb_dropped(q, tile) ? 0u : warp_lookback(a.status_n, tile, tot >> 16, epoch, &q->error, 31u);
             if (t == 32) s_pn = p;
         }
         __syncthreads();
@@ -308,10 +311,12 @@ __global__ void __launch_bounds__(kActThreads) k_active(QueryState* q, ActiveArg
         uint32_t tot;
         const uint32_t excl = cta_exclusive_scan<kActThreads>(cnt, s_warp, &tot);
         if (threadIdx.x < 32) {
-            const uint32_t p = warp_lookback(a.status_a, tile, tot & 0xffffu, epoch, &q->error, 30u);
+            const uint32_t p =
+                lb_dropped(q, tile) ? 0u : warp_lookback(a.status_a, tile, tot & 0xffffu, epoch, &q->error, 30u);
             if (threadIdx.x == 0) s_pa = p;
         } else if (threadIdx.x < 64) {
-            const uint32_t p = warp_lookback(a.status_n, tile, tot >> 16, epoch, &q->error, 31u);
+            const uint32_t p =
+                lb_dropped(q, tile) ? 0u : warp_lookback(a.status_n, tile, tot >> 16, epoch, &q->error, 31u);
             if (threadIdx.x == 32) s_pn = p;
         }
         __syncthreads();

@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(QueryState* q, const uint
         uint32_t vals[kScanItems], excl, total;
         tile_scan(in, n, tile, s_buf, s_warp, [](uint32_t v) { return v; }, vals, &excl, &total);
         if (threadIdx.x < 32) {
-            const uint32_t p = warp_lookback(status, tile, total, epoch, &q->error, 1u);
+            const uint32_t p = lb_dropped(q, tile) ? 0u : warp_lookback(status, tile, total, epoch, &q->error, 1u);
             if (threadIdx.x == 0) {
                 s_prefix = p;
                 if (tile == ntiles - 1 && d_total) *d_total = p + total;
@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(kScanThreads) k_select(QueryState* q, const ui
         tile_scan(flags, n, tile, s_buf, s_warp, [](uint32_t v) { return v != 0u ? 1u : 0u; }, vals, &excl,
                   &total);
         if (threadIdx.x < 32) {
-            const uint32_t p = warp_lookback(status, tile, total, epoch, &q->error, 2u);
+            const uint32_t p = lb_dropped(q, tile) ? 0u : warp_lookback(status, tile, total, epoch, &q->error, 2u);
             if (threadIdx.x == 0) {
                 s_prefix = p;
                 if (tile == ntiles - 1 && d_count) *d_count = p + total;
