@@ -355,6 +355,24 @@ BATCH = dict(workload="256 queries over 8 resident volumes (32^3 blobs, 64^3 val
              rate=4, queries=256, seed=4)
 
 
+def _mc_share(mcs, queries) -> dict:
+    """The plain path's marching-cubes share on a query mix: the same queries
+    again with a perf tracker (CUDA-event stage times).  A batched or served
+    path that kept only the MC work per query could reach at most
+    wall time / MC time per query times the plain path's rate."""
+    perf = {}
+    t0 = time.perf_counter()
+    for v, iso in queries:
+        mcs[v].computeSurface(iso, perf)
+    wall = (time.perf_counter() - t0) / len(queries)
+    mc = float(np.sum(perf["computeVertices"])) / len(queries) / 1000.0
+    stages = sum(float(np.sum(perf[k])) for k in ("computeActiveBlocks", "cacheUpdate", "decompression",
+                                                  "computeVertices")) / len(queries) / 1000.0
+    return {"mc_ms_per_query": 1000.0 * mc, "stages_ms_per_query": 1000.0 * stages,
+            "wall_ms_per_query": 1000.0 * wall, "mc_share_of_wall": mc / wall,
+            "max_speedup_if_only_mc_remains": wall / mc if mc > 0 else None}
+
+
 def batched_bench(reps: int = 5) -> dict:
     """The batched engine against the plain per-query path on the same 256
     queries: iso-queries/s, per-query latency, and a bit-exact check of every
@@ -398,6 +416,7 @@ def batched_bench(reps: int = 5) -> dict:
         mcs[v].computeSurface(iso)
         plain_lat.append(1000.0 * (time.perf_counter() - tq))
     plain_s = time.perf_counter() - t0
+    mc_share = _mc_share(mcs, qs)
 
     # batched engine: every volume resident, one pool for all of them
     eng = bcmc.Engine(ctx, pool_slots=total_blocks, max_batch=BATCH["queries"])
@@ -430,16 +449,34 @@ def batched_bench(reps: int = 5) -> dict:
             if not torch.equal(mcs[v].vertexBuffer.torch()[:n], allv[off: off + n]):
                 identical = False
     bm = float(np.median(batch_ms))
+    # per-query latency (arrival -> result) with all the queries arriving at
+    # once, through the continuous-batching server (two batches in flight)
+    srv = bcmc.Server(eng, max_batch=BATCH["queries"])
+    try:
+        srv_lat, srv_s = [], []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            tickets = [srv.submit(v, iso) for v, iso in qs]
+            srv_lat.extend(srv.wait(t)[2] for t in tickets)
+            srv_s.append(time.perf_counter() - t0)
+    finally:
+        srv.close()
     return {"workload": BATCH["workload"], "queries": len(qs), "vertices": nverts,
+            "served_at_once": {"queries_per_s": len(qs) / float(np.median(srv_s)),
+                               "p50_ms": float(np.percentile(srv_lat, 50)),
+                               "p99_ms": float(np.percentile(srv_lat, 99)),
+                               "what": "all queries submitted at once to bcmc_server; latency = arrival to result"},
             "plain": {"queries_per_s": len(qs) / plain_s, "p50_ms": float(np.percentile(plain_lat, 50)),
                       "p99_ms": float(np.percentile(plain_lat, 99))},
             "batched": {"queries_per_s": len(qs) / (bm / 1000.0), "batch_ms": bm,
                         "device_ms": float(np.median(dev_ms)), "p50_ms": bm, "p99_ms": float(np.max(batch_ms)),
                         "gpu_launches_per_batch": launches / reps},
             "autotune": tune,
+            "plain_mc": mc_share,
             "speedup_qps": (len(qs) / (bm / 1000.0)) / (len(qs) / plain_s),
             "identical_to_plain": identical,
-            "latency_note": "a batch's queries all complete when the batch does: per-query latency = batch wall time"}
+            "latency_note": "batched: a batch's queries all complete when the batch does (per-query latency = "
+                            "batch wall time); served_at_once gives per-request latencies"}
 
 
 SERVED = dict(workload="1024x1024x1080 uint16-range value noise (~60% background blocks, 17,694,720 blocks) "
@@ -506,6 +543,7 @@ def served_bench() -> dict:
         mcs[v].computeSurface(iso)
         lat.append(1000.0 * (time.perf_counter() - tq))
     plain_qps = len(plain_q) / (time.perf_counter() - t0)
+    mc_share = _mc_share(mcs, plain_q)
     del mcs
     torch.cuda.empty_cache()
 
@@ -523,7 +561,7 @@ def served_bench() -> dict:
             n = max(50, int(r * SERVED["seconds"]))
             rep = srv.run_load(r, n, list(range(len(vols))), weights, iso_lo, iso_hi, seed=int(r))
             sweeps.append({k: rep[k] for k in ("offered_qps", "achieved_qps", "p50_ms", "p95_ms", "p99_ms",
-                                                "mean_batch", "completed")})
+                                                "mean_batch", "completed", "batches", "overlapped_batches")})
     finally:
         srv.close()
     st = eng.stats()
@@ -570,6 +608,8 @@ def served_bench() -> dict:
     return {"workload": SERVED["workload"],
             "plain": {"queries_per_s": plain_qps, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": p99_plain,
                       "what": "back to back, one query at a time (service times)"},
+            "plain_mc": mc_share,
+            "overlapped_batches": sum(s.get("overlapped_batches", 0) for s in sweeps),
             "plain_open_loop": plain_sweep,
             "served": sweeps,
             "served_vs_plain_at_equal_p99": ratios,
@@ -611,7 +651,9 @@ def _batched_summary(b):
         return None
     return {"queries_per_s": b["batched"]["queries_per_s"], "plain_queries_per_s": b["plain"]["queries_per_s"],
             "speedup_qps": b["speedup_qps"], "p50_ms": b["batched"]["p50_ms"], "p99_ms": b["batched"]["p99_ms"],
-            "plain_p99_ms": b["plain"]["p99_ms"], "identical_to_plain": b["identical_to_plain"]}
+            "plain_p99_ms": b["plain"]["p99_ms"], "identical_to_plain": b["identical_to_plain"],
+            "served_at_once": {k: b["served_at_once"][k] for k in ("queries_per_s", "p50_ms", "p99_ms")},
+            "max_speedup_if_only_mc_remains": b["plain_mc"]["max_speedup_if_only_mc_remains"]}
 
 
 def _served_summary(sv):
@@ -622,7 +664,9 @@ def _served_summary(sv):
     return {"plain_queries_per_s": sv["plain"]["queries_per_s"], "plain_p99_ms": sv["plain"]["p99_ms"],
             "max_sustained_qps": top["achieved_qps"] if top else None, "p99_ms_at_max": top["p99_ms"] if top else None,
             "best_ratio_at_equal_p99": sv["best_ratio_at_equal_p99"],
-            "ratios_at_equal_p99": [round(r["ratio"], 3) for r in sv["served_vs_plain_at_equal_p99"]]}
+            "ratios_at_equal_p99": [round(r["ratio"], 3) for r in sv["served_vs_plain_at_equal_p99"]],
+            "overlapped_batches": sv["overlapped_batches"],
+            "max_speedup_if_only_mc_remains": sv["plain_mc"]["max_speedup_if_only_mc_remains"]}
 
 
 def run_gb300(args):

@@ -366,6 +366,7 @@ typedef struct {
     uint64_t batches, launch_sequences, queries, decoded_blocks, evicted_blocks;
     uint64_t pool_slots, pool_used, vertex_capacity, device_bytes;
     double last_batch_ms;       /* device time of the last batch (CUDA events) */
+    uint64_t overlapped_batches; /* server batches launched while another batch was on the device */
 } bcmc_engine_stats;
 
 bcmc_status bcmc_engine_create(bcmc_ctx* ctx, const bcmc_engine_opts* opts, bcmc_engine** out);
@@ -396,15 +397,24 @@ bcmc_status bcmc_engine_stats_get(bcmc_engine* eng, bcmc_engine_stats* out);
  * the CTAs per SM of the active test and of the MC kernel (coordinate descent
  * from the defaults), and times a decode probe over up to 2^18 blocks of the
  * largest volume for the decode kernel's threads per CTA and CTAs per SM.  The
- * chosen parameters are used (and captured into that bucket's graph) from then
- * on.  The kernels' tile shapes are compile-time constants. */
+ * MC kernel's tile (active blocks per CTA tile: 8, 16 or 32, each a compiled
+ * instance of the kernel) is tuned first, then its CTAs per SM.  The chosen
+ * parameters are used (and captured into that bucket's graph) from then on.
+ * The engine has no sort (its pool hands out free slots instead of the LRU's
+ * age order), so no radix digit width is tuned here. */
 typedef struct {
     uint32_t bucket;
     int32_t act_ctas_per_sm, decode_threads, decode_ctas_per_sm, mc_ctas_per_sm;
     double batch_ms_default, batch_ms_tuned, decode_ms_default, decode_ms_tuned;
+    int32_t mc_blocks_per_tile;
 } bcmc_tune_report;
 bcmc_status bcmc_engine_autotune(bcmc_engine* eng, const bcmc_query* queries, uint32_t n,
                                  bcmc_tune_report* out);
+/* Applies a tune report's launch parameters to its bucket (for instance one
+ * saved from an earlier bcmc_engine_autotune), without timing anything.  The
+ * timing fields are ignored.  BCMC_E_ARG for a bucket that is not a power of
+ * two up to max_batch or a parameter outside the autotuner's choices. */
+bcmc_status bcmc_engine_set_tuning(bcmc_engine* eng, const bcmc_tune_report* cfg);
 
 /* ---- Isosurface server ----------------------------------------------------- */
 /* No counterpart in the reference.  A request loop over an engine: a worker
@@ -448,6 +458,7 @@ typedef struct {
 typedef struct {
     double offered_qps, achieved_qps, p50_ms, p95_ms, p99_ms, mean_ms, max_ms, mean_batch, duration_s;
     uint64_t completed, batches, vertices;
+    uint64_t overlapped_batches; /* batches launched while the previous one was still on the device */
 } bcmc_load_report;
 bcmc_status bcmc_server_run_load(bcmc_server* srv, const bcmc_load_spec* spec, bcmc_load_report* out);
 

@@ -152,7 +152,19 @@ def test_autotune_keeps_results(ctx, volumes):
     rep = eng.autotune(qs)
     assert rep["bucket"] == 16
     assert rep["mc_ctas_per_sm"] in (4, 5, 6) and rep["act_ctas_per_sm"] in (4, 8, 16)
+    assert rep["mc_blocks_per_tile"] in (8, 16, 32)
     assert rep["decode_threads"] in (64, 128, 256) and rep["decode_ctas_per_sm"] in (8, 16, 32)
     assert rep["batch_ms_tuned"] <= rep["batch_ms_default"] + 1e-9
     res = eng.run(qs)
     _check(eng, res, want)
+
+
+@pytest.mark.parametrize("mc_blocks", [8, 16, 32])
+def test_every_mc_tile_keeps_results(ctx, volumes, mc_blocks):
+    """Each compiled MC tile shape the autotuner can pick gives the plain
+    path's meshes (the tile is forced through the autotuner's test hook)."""
+    qs = _queries(volumes, 12, seed=10 + mc_blocks)
+    want = _plain(ctx, volumes, qs)
+    eng = _engine(ctx, volumes)
+    eng.force_config(len(qs), mc_blocks_per_tile=mc_blocks)
+    _check(eng, eng.run(qs), want)

@@ -1,7 +1,9 @@
 """Continuous-batching server (bcmc_server_*): requests submitted together are
 batched, each request's vertices equal the plain path's for its (volume,
-isovalue) -- alone and in the mix -- and the open-loop load generator reports
-consistent throughput and latency figures."""
+isovalue) -- alone and in the mix, also when batches overlap on the device --
+and the open-loop load generator reports consistent throughput and latency
+figures."""
+import time
 import threading
 
 import numpy as np
@@ -105,3 +107,36 @@ def test_open_loop_load_report(ctx, volumes):
     assert 0.0 < rep["p50_ms"] <= rep["p95_ms"] <= rep["p99_ms"] <= rep["max_ms"]
     assert rep["batches"] >= 1 and rep["mean_batch"] >= 1.0
     assert rep["achieved_qps"] > 0.0
+    assert 0 <= rep["overlapped_batches"] < rep["batches"]
+
+
+def test_overlapped_batches_match_plain_path(ctx, volumes):
+    """A steady stream of requests keeps a batch on the device while the next
+    arrives: the next batch is launched at once (its active test, claims and
+    decode overlap the first batch's marching cubes).  Every result equals
+    the plain path's."""
+    reqs = _isos(volumes, 160, seed=8)
+    plain = []
+    mcs = {}
+    for v, iso in reqs:
+        if v not in mcs:
+            mcs[v] = bcmc.CompressedMarchingCubes(ctx)
+            mcs[v].setCompressedVolume(volumes[v]["stream"], volumes[v]["rate"], volumes[v]["dims"])
+        mcs[v].computeSurface(iso)
+        plain.append(mcs[v].copyVertices().copy())
+    eng, srv = _server(ctx, volumes)
+    try:
+        tickets = []
+        for i, (v, iso) in enumerate(reqs):
+            tickets.append(srv.submit(v, iso, max_vertices=len(plain[i]) + 8))
+            if i % 4 == 3:
+                time.sleep(50e-6)
+        for i, t in enumerate(tickets):
+            n, nact, lat, verts = srv.wait(t)
+            assert n == len(plain[i]), i
+            assert np.array_equal(verts, plain[i]), i
+        st = eng.stats()
+        assert st["overlapped_batches"] > 0, st
+        assert st["batches"] < len(reqs)
+    finally:
+        srv.close()

@@ -653,6 +653,26 @@ class Engine:
         check(_lib.load().bcmc_engine_autotune(self._h, qs, n, C.byref(rep)), self.ctx.handle)
         return {k: getattr(rep, k) for k, _ in _lib.bcmc_tune_report._fields_}
 
+    def set_tuning(self, report: dict):
+        """Applies a tune report (as autotune returns it) to its bucket
+        (bcmc_engine_set_tuning)."""
+        rep = _lib.bcmc_tune_report()
+        for k, _ in _lib.bcmc_tune_report._fields_:
+            if k in report:
+                setattr(rep, k, report[k])
+        check(_lib.load().bcmc_engine_set_tuning(self._h, C.byref(rep)), self.ctx.handle)
+
+    def force_config(self, n: int, **params):
+        """The default launch parameters of n queries' bucket with `params`
+        changed (the tune report's field names), applied by set_tuning."""
+        b = 1
+        while b < n:
+            b <<= 1
+        cfg = {"bucket": b, "act_ctas_per_sm": 8, "decode_threads": 128, "decode_ctas_per_sm": 16,
+               "mc_ctas_per_sm": 6, "mc_blocks_per_tile": 16}
+        cfg.update(params)
+        self.set_tuning(cfg)
+
     def run_admit(self, queries):
         """Runs the longest prefix of `queries` that the slot pool and the
         vertex budget admit; returns (results of that prefix, its length)."""

@@ -63,7 +63,7 @@ class bcmc_tune_report(C.Structure):
     _fields_ = [("bucket", C.c_uint32)] + [(n, C.c_int32) for n in ("act_ctas_per_sm", "decode_threads",
                                                                      "decode_ctas_per_sm", "mc_ctas_per_sm")] + \
                [(n, C.c_double) for n in ("batch_ms_default", "batch_ms_tuned", "decode_ms_default",
-                                          "decode_ms_tuned")]
+                                          "decode_ms_tuned")] + [("mc_blocks_per_tile", C.c_int32)]
 
 
 class bcmc_render_params(C.Structure):
@@ -84,7 +84,7 @@ class bcmc_load_spec(C.Structure):
 class bcmc_load_report(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("offered_qps", "achieved_qps", "p50_ms", "p95_ms", "p99_ms", "mean_ms",
                                            "max_ms", "mean_batch", "duration_s")] + \
-               [(n, C.c_uint64) for n in ("completed", "batches", "vertices")]
+               [(n, C.c_uint64) for n in ("completed", "batches", "vertices", "overlapped_batches")]
 
 
 class bcmc_query(C.Structure):
@@ -98,7 +98,8 @@ class bcmc_query_result(C.Structure):
 class bcmc_engine_stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("batches", "launch_sequences", "queries", "decoded_blocks",
                                            "evicted_blocks", "pool_slots", "pool_used", "vertex_capacity",
-                                           "device_bytes")] + [("last_batch_ms", C.c_double)]
+                                           "device_bytes")] + [("last_batch_ms", C.c_double),
+                                                                ("overlapped_batches", C.c_uint64)]
 
 
 P = C.c_void_p
@@ -147,6 +148,7 @@ SIGNATURES = {
     "bcmc_engine_copy_vertices": (C.c_int, [P, U64, U64, P]),
     "bcmc_engine_stats_get": (C.c_int, [P, C.POINTER(bcmc_engine_stats)]),
     "bcmc_engine_autotune": (C.c_int, [P, C.POINTER(bcmc_query), U32, C.POINTER(bcmc_tune_report)]),
+    "bcmc_engine_set_tuning": (C.c_int, [P, C.POINTER(bcmc_tune_report)]),
     "bcmc_server_create": (C.c_int, [P, C.POINTER(bcmc_server_opts), C.POINTER(P)]),
     "bcmc_server_destroy": (None, [P]),
     "bcmc_server_submit": (C.c_int, [P, U32, C.c_float, P, U64, C.POINTER(U64)]),

@@ -41,6 +41,13 @@ namespace bcmc {
 extern std::atomic<uint64_t> g_kernel_launches;
 inline void count_launches(uint64_t n) { g_kernel_launches.fetch_add(n, std::memory_order_relaxed); }
 
+// Dynamic shared memory above the 48 KB a launch gets without opting in.
+template <typename K>
+inline void allow_smem(K kernel, size_t bytes)
+{
+    if (bytes > 48u * 1024u) BCMC_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
+
 // Objects made from a context (volumes, caches, engines) keep it alive:
 // bcmc_ctx_destroy defers the release until the last of them is gone.
 void ctx_child_added(bcmc_ctx* ctx);
@@ -59,6 +66,20 @@ void render_launch(bcmc_ctx* ctx, const uint2* verts, uint64_t n, const uint32_t
 
 // ---- engine.cu (for server.cu) ------------------------------------------------
 int engine_device(bcmc_engine* e);
+// Pipelined batches, for the server: two lanes of batch buffers, so that one
+// batch's phase 1 (active test, claims, decode) runs while the other's phase 2
+// (marching cubes) does.  engine_submit launches queries[0..n) on lane k and
+// returns at once (on_done(arg) runs on a CUDA host thread when the batch's
+// results are on the host); engine_complete takes the results (blocking until
+// they are there), in submission order; engine_copy_lane_vertices copies from
+// that lane's vertex buffer, valid until the lane's next submit.
+bcmc_status engine_submit(bcmc_engine* e, int k, const bcmc_query* queries, uint32_t n, void (*on_done)(void*),
+                          void* arg);
+bcmc_status engine_complete(bcmc_engine* e, int k, bcmc_query_result* out, uint32_t* admitted);
+bcmc_status engine_copy_lane_vertices(bcmc_engine* e, int k, uint64_t first, uint64_t count, void* host);
+// Waits for everything the engine queued, host callbacks included.
+void engine_drain(bcmc_engine* e);
+uint32_t engine_max_batch(bcmc_engine* e);
 uint64_t engine_vertex_budget(bcmc_engine* e);
 bcmc_ctx* engine_ctx(bcmc_engine* e);
 

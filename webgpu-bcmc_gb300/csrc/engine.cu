@@ -40,10 +40,11 @@ namespace {
 
 constexpr int kEngThreads = 256;
 constexpr uint32_t kEngTile = 1024;  // blocks per active tile (4 per thread)
-constexpr int kBmcBlocks = 16;
-constexpr int kBmcThreads = 256;
-constexpr int kBmcCells = 64 * kBmcBlocks;
-constexpr int kBmcPerSm = 6;
+// k_bmc tiles: kBlocks active blocks per tile, 16 threads per block (4 cells
+// each); 1536 threads per SM resident whatever the tile (6 CTAs of 16 blocks)
+constexpr int kBmcThreadsPerSm = 1536;
+constexpr int kBmcPerSm = 6;        // CTAs per SM of the default 16-block tile
+constexpr int kBmcMaxPerSm = 12;    // of the 8-block tile: sizes the MC look-back status words
 constexpr uint32_t kMaxVolumes = 4096;
 
 struct EngVolDev {
@@ -290,15 +291,38 @@ __global__ void __launch_bounds__(kEngThreads) k_bactive(BatchArgs a)
 // ---------------------------------------------------------------------------
 // k_bdecode: claimed blocks into their slots, then publish the slot
 // ---------------------------------------------------------------------------
+// Volumes of a batch differ in rate: the staged words of one CTA are laid out
+// at the largest rate of the resident volumes (`max_rate` u64 words per block).
+
 template <int kThreads>
-__global__ void __launch_bounds__(kThreads) k_bdecode(BatchArgs a)
+__global__ void __launch_bounds__(kThreads) k_bdecode(BatchArgs a, uint32_t max_rate)
 {
+    extern __shared__ __align__(16) uint32_t s_words[];
+    uint32_t* pl = s_words + zfp_stage_words(kThreads, max_rate) + threadIdx.x * kZfpPlaneWords;
+    if (threadIdx.x < 4) s_words[kThreads * 2u * max_rate + threadIdx.x] = 0u;
     const uint32_t n = a.st->num_decode;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t v = a.dec_vol[i], b = a.dec_block[i], slot = a.dec_slot[i];
+    for (uint32_t i0 = blockIdx.x * kThreads; i0 < n; i0 += gridDim.x * kThreads) {
+        const uint32_t i = i0 + threadIdx.x;
+        uint32_t v = 0, b = 0, slot = 0;
+        __syncthreads();
+        if (i < n) {
+            v = a.dec_vol[i];
+            b = a.dec_block[i];
+            slot = a.dec_slot[i];
+            const EngVolDev& V = a.vols[v];
+            // this thread's slot of the staged words, at the CTA's stride
+            uint2* dst = reinterpret_cast<uint2*>(s_words + threadIdx.x * 2u * max_rate);
+            const uint32_t rate = V.max_bits / 64u;
+            for (uint32_t k = 0; k < rate; ++k) {
+                const uint64_t x = __ldg(V.words + (uint64_t)b * rate + k);
+                dst[k] = make_uint2((uint32_t)x, (uint32_t)(x >> 32));
+            }
+        }
+        __syncthreads();
+        if (i >= n) continue;
         const EngVolDev& V = a.vols[v];
         float out[64];
-        zfp_decode_block<1>(V.words, (uint64_t)b * V.max_bits, V.max_bits, out);
+        zfp_decode_staged(s_words + threadIdx.x * 2u * max_rate, V.max_bits, pl, out);
         float4* d4 = reinterpret_cast<float4*>(a.cache + (uint64_t)slot * 64u);
 #pragma unroll
         for (int k = 0; k < 16; ++k) d4[k] = make_float4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
@@ -310,13 +334,20 @@ __global__ void __launch_bounds__(kThreads) k_bdecode(BatchArgs a)
 
 // The autotuner's decode probe: k_bdecode's inner loop into a scratch buffer.
 template <int kThreads>
-__global__ void __launch_bounds__(kThreads) k_decode_probe(const uint64_t* __restrict__ words, uint32_t max_bits,
+__global__ void __launch_bounds__(kThreads) k_decode_probe(const uint64_t* __restrict__ words, uint32_t rate,
                                                            uint32_t n, float* __restrict__ scratch)
 {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    extern __shared__ __align__(16) uint32_t s_words[];
+    uint32_t* pl = s_words + zfp_stage_words(kThreads, rate) + threadIdx.x * kZfpPlaneWords;
+    for (uint32_t i0 = blockIdx.x * kThreads; i0 < n; i0 += gridDim.x * kThreads) {
+        const uint32_t nb = n - i0 < (uint32_t)kThreads ? n - i0 : (uint32_t)kThreads;
+        __syncthreads();
+        zfp_stage_run(words, i0, nb, rate, s_words);
+        __syncthreads();
+        if (threadIdx.x >= nb) continue;
         float out[64];
-        zfp_decode_block<1>(words, (uint64_t)i * max_bits, max_bits, out);
-        float4* d4 = reinterpret_cast<float4*>(scratch + (uint64_t)i * 64u);
+        zfp_decode_staged(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, out);
+        float4* d4 = reinterpret_cast<float4*>(scratch + (uint64_t)(i0 + threadIdx.x) * 64u);
 #pragma unroll
         for (int k = 0; k < 16; ++k) d4[k] = make_float4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
     }
@@ -325,8 +356,11 @@ __global__ void __launch_bounds__(kThreads) k_decode_probe(const uint64_t* __res
 // ---------------------------------------------------------------------------
 // k_bmc: the per-query MC kernel (pipeline.cu, k_mc) over a batch's entries
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBmcThreads, kBmcPerSm) k_bmc(BatchArgs a)
+template <int kBmcBlocks>
+__global__ void __launch_bounds__(16 * kBmcBlocks, kBmcThreadsPerSm / (16 * kBmcBlocks)) k_bmc(BatchArgs a)
 {
+    constexpr int kBmcThreads = 16 * kBmcBlocks;
+    constexpr int kBmcCells = 64 * kBmcBlocks;
     __shared__ float s_vol[kBmcBlocks][128];
     __shared__ uint8_t s_rm[kBmcBlocks][32];  // corner-row masks of each block (count_cells)
     __shared__ uint32_t s_pair[32], s_pair_sw[32];  // 5-bit row mask -> per-cell corner pairs
@@ -358,7 +392,8 @@ __global__ void __launch_bounds__(kBmcThreads, kBmcPerSm) k_bmc(BatchArgs a)
     const uint32_t rank = s_rank;
     const uint32_t range = div_up(div_up(A, G), kBmcBlocks) * kBmcBlocks;
     const uint32_t start = min(A, rank * range), end = min(A, start + range);
-    reinterpret_cast<uint4*>(&s_te[0][0])[t] = reinterpret_cast<const uint4*>(&c_tri.corners[0][0])[t];
+    for (uint32_t i = t; i < 256u; i += kBmcThreads)
+        reinterpret_cast<uint4*>(&s_te[0][0])[i] = reinterpret_cast<const uint4*>(&c_tri.corners[0][0])[i];
     if (t < 16) reinterpret_cast<uint4*>(s_cnt)[t] = reinterpret_cast<const uint4*>(c_tri.count)[t];
     if (t == 0) {
         s_cta_v = 0;
@@ -726,25 +761,16 @@ struct EngConfig {
     int act_per_sm = 8;      // k_bactive CTAs per SM
     int dec_threads = 128;   // k_bdecode threads per CTA (64, 128, 256)
     int dec_per_sm = 16;     // k_bdecode CTAs per SM
-    int mc_per_sm = kBmcPerSm;  // k_bmc CTAs per SM (<= its residency, 6)
+    int mc_per_sm = kBmcPerSm;  // k_bmc CTAs per SM of the 16-block tile (<= its residency, 6); scaled
+                                // by 16 / mc_blocks for the other tiles
+    int mc_blocks = 16;         // k_bmc active blocks per tile (8, 16, 32)
 };
 
-struct bcmc_engine {
-    bcmc_ctx* ctx = nullptr;
-    cudaStream_t stream = nullptr;
-    bcmc_engine_opts opts{};
-    std::vector<EngVolume> vols;
-    EngVolDev* d_vols = nullptr;
-    uint32_t d_vols_cap = 0;
-    // pool
-    uint64_t pool_slots = 0;
-    float* cache = nullptr;
-    uint32_t *free_list = nullptr, *last_use = nullptr, *owner_vol = nullptr, *owner_block = nullptr;
-    EngPool* d_pool = nullptr;
-    EngPool* h_pool = nullptr;
-    unsigned long long* d_evicted = nullptr;
-    // batch buffers
-    uint32_t max_batch = 0;
+// The buffers of one batch in flight.  Two lanes let the server keep two
+// batches on the device at once: the next batch's active test, claims and
+// decode (phase 1) run while the current batch's marching cubes (phase 2) do.
+struct EngLane {
+    bool ready = false;  // buffers allocated
     EngQuery* d_queries = nullptr;
     EngQuery* h_queries = nullptr;  // pinned
     EngResult* d_results = nullptr;
@@ -756,33 +782,71 @@ struct bcmc_engine {
     uint64_t bitmap_words = 0;
     uint32_t *ent_id = nullptr, *ent_q = nullptr, *block_counts = nullptr;
     uint32_t entry_cap = 0;
-    uint32_t *dec_vol = nullptr, *dec_block = nullptr, *dec_slot = nullptr;
-    uint32_t dec_cap = 0;
     uint2* verts = nullptr;
     uint64_t vert_cap = 0, vert_used = 0;
     uint64_t* status = nullptr;
     uint64_t status_words = 0;
     uint64_t status_a_words = 0;
     uint64_t epoch_calls = 0;
-    uint32_t use_epoch = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // one graph per batch-size bucket, rebuilt when buffers move
     struct Graph {
-        cudaGraphExec_t exec = nullptr;
-        uint64_t generation = 0;
-        int cfg_key = -1;  // the launch parameters it was captured with
+        cudaGraphExec_t exec = nullptr;        // the whole sequence on one stream
+        cudaGraphExec_t front = nullptr;       // phase 1 (pipelined runs)
+        cudaGraphExec_t back = nullptr;        // phase 2 (pipelined runs)
+        uint64_t generation = 0, split_generation = 0;
+        int cfg_key = -1, split_cfg_key = -1;  // the launch parameters they were captured with
     };
     std::map<uint32_t, Graph> graphs;
+    uint64_t generation = 1;
+    // pipelined batch in flight on this lane
+    cudaEvent_t ev_front = nullptr;  // its phase 1 finished
+    cudaEvent_t ev_done = nullptr;   // its phase 2 and the state copies finished
+    bool in_flight = false;
+    uint32_t batch_epoch = 0;        // use epoch of its sequence (protected from eviction)
+    uint32_t n = 0, bucket = 0;
+    std::vector<bcmc_query> queries;
+};
+
+struct bcmc_engine {
+    bcmc_ctx* ctx = nullptr;
+    cudaStream_t stream = nullptr;       // every synchronous run; phase 1 of pipelined runs
+    cudaStream_t stream_back = nullptr;  // phase 2 of pipelined runs
+    cudaStream_t stream_copy = nullptr;  // vertex copies of completed pipelined batches
+    bcmc_engine_opts opts{};
+    std::vector<EngVolume> vols;
+    EngVolDev* d_vols = nullptr;
+    uint32_t d_vols_cap = 0;
+    // pool
+    uint64_t pool_slots = 0;
+    float* cache = nullptr;
+    uint32_t *free_list = nullptr, *last_use = nullptr, *owner_vol = nullptr, *owner_block = nullptr;
+    EngPool* d_pool = nullptr;
+    EngPool* h_pool = nullptr;
+    unsigned long long* d_evicted = nullptr;
+    // the decode list of a sequence's claims: written and read in phase 1 only,
+    // which runs one batch at a time, so both lanes share it
+    uint32_t *dec_vol = nullptr, *dec_block = nullptr, *dec_slot = nullptr;
+    uint32_t dec_cap = 0;
+    uint32_t max_batch = 0;
+    uint32_t max_rate = 1;  // largest rate of the resident volumes (k_bdecode's staging stride)
+    uint32_t use_epoch = 0;
+    EngLane lanes[2];
+    EngLane* L = &lanes[0];  // the lane the next sequence runs on, and whose vertices the API returns
     std::map<uint32_t, EngConfig> tuned;  // per bucket
     EngConfig cfg;                        // of the sequence being enqueued
-    uint64_t generation = 1;
     bcmc_engine_stats stats{};
+    uint64_t overlapped = 0;  // pipelined batches launched while another was in flight
 };
 
 namespace {
 
-int eng_grid_mc_max(bcmc_engine* e) { return e->ctx->num_sms * kBmcPerSm; }  // sizes the status words
-int eng_grid_mc(bcmc_engine* e) { return e->ctx->num_sms * std::min(e->cfg.mc_per_sm, kBmcPerSm); }
+int eng_grid_mc_max(bcmc_engine* e) { return e->ctx->num_sms * kBmcMaxPerSm; }  // sizes the status words
+int eng_grid_mc(bcmc_engine* e)
+{
+    const int per_sm = std::min(e->cfg.mc_per_sm, kBmcPerSm) * 16 / e->cfg.mc_blocks;
+    return e->ctx->num_sms * std::max(per_sm, 1);
+}
 int eng_grid_act(bcmc_engine* e) { return e->ctx->num_sms * e->cfg.act_per_sm; }
 int eng_grid_dec(bcmc_engine* e) { return e->ctx->num_sms * e->cfg.dec_per_sm; }
 
@@ -798,27 +862,27 @@ BatchArgs eng_args(bcmc_engine* e)
 {
     BatchArgs a;
     a.vols = e->d_vols;
-    a.queries = e->d_queries;
-    a.results = e->d_results;
-    a.st = e->d_st;
+    a.queries = e->L->d_queries;
+    a.results = e->L->d_results;
+    a.st = e->L->d_st;
     a.pool = e->d_pool;
     a.free_list = e->free_list;
     a.last_use = e->last_use;
     a.owner_vol = e->owner_vol;
     a.owner_block = e->owner_block;
     a.cache = e->cache;
-    a.bitmap = e->bitmap;
-    a.ent_id = e->ent_id;
-    a.ent_q = e->ent_q;
-    a.block_counts = e->block_counts;
-    a.q_nactive = e->q_nactive;
-    a.q_nverts = e->q_nverts;
+    a.bitmap = e->L->bitmap;
+    a.ent_id = e->L->ent_id;
+    a.ent_q = e->L->ent_q;
+    a.block_counts = e->L->block_counts;
+    a.q_nactive = e->L->q_nactive;
+    a.q_nverts = e->L->q_nverts;
     a.dec_vol = e->dec_vol;
     a.dec_block = e->dec_block;
     a.dec_slot = e->dec_slot;
-    a.verts = e->verts;
-    a.status_a = e->status;
-    a.status_v = e->status + e->status_a_words;
+    a.verts = e->L->verts;
+    a.status_a = e->L->status;
+    a.status_v = e->L->status + e->L->status_a_words;
     return a;
 }
 
@@ -826,23 +890,23 @@ void eng_ensure_status(bcmc_engine* e, uint64_t active_tiles)
 {
     const uint64_t need_a = std::max<uint64_t>(active_tiles + 1, 1024);
     const uint64_t need = need_a + (uint64_t)eng_grid_mc_max(e) + 1;
-    if (need_a <= e->status_a_words && need <= e->status_words) return;
+    if (need_a <= e->L->status_a_words && need <= e->L->status_words) return;
     BCMC_CUDA(cudaStreamSynchronize(e->stream));
     const uint64_t words = std::max<uint64_t>(need_a * 2, 4096) + eng_grid_mc_max(e) + 1;
-    eng_realloc(e, e->status, e->status_words, words);
-    BCMC_CUDA(cudaMemsetAsync(e->status, 0, words * 8, e->stream));
-    e->status_words = words;
-    e->status_a_words = words - eng_grid_mc_max(e) - 1;
-    ++e->generation;
+    eng_realloc(e, e->L->status, e->L->status_words, words);
+    BCMC_CUDA(cudaMemsetAsync(e->L->status, 0, words * 8, e->stream));
+    e->L->status_words = words;
+    e->L->status_a_words = words - eng_grid_mc_max(e) - 1;
+    ++e->L->generation;
 }
 
 // Every 2^26 sequences the look-back epoch restarts over cleared status words.
 void eng_epoch_tick(bcmc_engine* e)
 {
-    if (++e->epoch_calls < (1ull << 26)) return;
-    BCMC_CUDA(cudaMemsetAsync(e->status, 0, e->status_words * 8, e->stream));
-    BCMC_CUDA(cudaMemsetAsync(&e->d_st->epoch, 0, 4, e->stream));
-    e->epoch_calls = 0;
+    if (++e->L->epoch_calls < (1ull << 26)) return;
+    BCMC_CUDA(cudaMemsetAsync(e->L->status, 0, e->L->status_words * 8, e->stream));
+    BCMC_CUDA(cudaMemsetAsync(&e->L->d_st->epoch, 0, 4, e->stream));
+    e->L->epoch_calls = 0;
 }
 
 void eng_upload_vols(bcmc_engine* e)
@@ -851,7 +915,7 @@ void eng_upload_vols(bcmc_engine* e)
     if (n > e->d_vols_cap) {
         eng_realloc(e, e->d_vols, e->d_vols_cap, std::max<uint32_t>(n * 2, 8));
         e->d_vols_cap = std::max<uint32_t>(n * 2, 8);
-        ++e->generation;
+        for (EngLane& l : e->lanes) ++l.generation;
     }
     std::vector<EngVolDev> h(n);
     for (uint32_t i = 0; i < n; ++i) {
@@ -887,98 +951,227 @@ void eng_alloc_pool(bcmc_engine* e, uint64_t slots)
     e->h_pool->tail = (uint32_t)slots;
     BCMC_CUDA(cudaMemcpyAsync(e->d_pool, e->h_pool, sizeof(EngPool), cudaMemcpyHostToDevice, e->stream));
     BCMC_CUDA(cudaStreamSynchronize(e->stream));
-    ++e->generation;
+    for (EngLane& l : e->lanes) ++l.generation;
 }
 
 void eng_ensure_batch(bcmc_engine* e, uint64_t bitmap_words, uint32_t entries)
 {
-    if (bitmap_words > e->bitmap_words) {
+    if (bitmap_words > e->L->bitmap_words) {
         BCMC_CUDA(cudaStreamSynchronize(e->stream));
         const uint64_t n = std::max<uint64_t>(bitmap_words + bitmap_words / 2, 1u << 16);
-        eng_realloc(e, e->bitmap, e->bitmap_words, n);
-        e->bitmap_words = n;
-        ++e->generation;
+        eng_realloc(e, e->L->bitmap, e->L->bitmap_words, n);
+        e->L->bitmap_words = n;
+        ++e->L->generation;
     }
-    if (entries > e->entry_cap) {
+    if (entries > e->L->entry_cap) {
         BCMC_CUDA(cudaStreamSynchronize(e->stream));
         const uint64_t n64 = std::min<uint64_t>((uint64_t)entries + entries / 2, 0xffffffffull);
         const uint32_t n = (uint32_t)std::max<uint64_t>(n64, 1u << 16);
-        eng_realloc(e, e->ent_id, e->entry_cap, n);
-        eng_realloc(e, e->ent_q, e->entry_cap, n);
-        eng_realloc(e, e->block_counts, e->entry_cap, n);
-        e->entry_cap = n;
-        ++e->generation;
+        eng_realloc(e, e->L->ent_id, e->L->entry_cap, n);
+        eng_realloc(e, e->L->ent_q, e->L->entry_cap, n);
+        eng_realloc(e, e->L->block_counts, e->L->entry_cap, n);
+        e->L->entry_cap = n;
+        ++e->L->generation;
     }
 }
 
 void eng_ensure_verts(bcmc_engine* e, uint64_t need)
 {
-    if (need <= e->vert_cap) return;
+    if (need <= e->L->vert_cap) return;
     BCMC_CUDA(cudaStreamSynchronize(e->stream));
     uint64_t n = std::max<uint64_t>(need + need / 2, 1u << 20);
     if (e->opts.vertex_budget) n = std::max<uint64_t>(need, std::min<uint64_t>(n, e->opts.vertex_budget));
     // keep the vertices already written by earlier sequences of this run
     uint2* nv = (uint2*)dev_alloc(e->ctx, n * sizeof(uint2));
-    if (e->vert_used)
-        BCMC_CUDA(cudaMemcpyAsync(nv, e->verts, e->vert_used * sizeof(uint2), cudaMemcpyDeviceToDevice, e->stream));
+    if (e->L->vert_used)
+        BCMC_CUDA(cudaMemcpyAsync(nv, e->L->verts, e->L->vert_used * sizeof(uint2), cudaMemcpyDeviceToDevice, e->stream));
     BCMC_CUDA(cudaStreamSynchronize(e->stream));
-    dev_free(e->ctx, e->verts, e->vert_cap * sizeof(uint2));
-    e->verts = nv;
-    e->vert_cap = n;
-    ++e->generation;
+    dev_free(e->ctx, e->L->verts, e->L->vert_cap * sizeof(uint2));
+    e->L->verts = nv;
+    e->L->vert_cap = n;
+    ++e->L->generation;
+}
+
+// Allocates lane k's buffers (lane 0 at creation; lane 1 on the first
+// pipelined run) and makes k the current lane.
+void eng_lane_init(bcmc_engine* e, int k)
+{
+    EngLane& l = e->lanes[k];
+    e->L = &l;
+    if (l.ready) return;
+    bcmc_ctx* ctx = e->ctx;
+    BCMC_CUDA(cudaEventCreate(&l.ev0));
+    BCMC_CUDA(cudaEventCreate(&l.ev1));
+    BCMC_CUDA(cudaEventCreateWithFlags(&l.ev_front, cudaEventDisableTiming));
+    BCMC_CUDA(cudaEventCreateWithFlags(&l.ev_done, cudaEventDisableTiming));
+    BCMC_CUDA(cudaMallocHost(&l.h_queries, e->max_batch * sizeof(EngQuery)));
+    BCMC_CUDA(cudaMallocHost(&l.h_results, e->max_batch * sizeof(EngResult)));
+    BCMC_CUDA(cudaMallocHost(&l.h_st, sizeof(EngState)));
+    memset(l.h_st, 0, sizeof(EngState));
+    l.d_queries = (EngQuery*)dev_alloc(ctx, e->max_batch * sizeof(EngQuery));
+    l.d_results = (EngResult*)dev_alloc(ctx, e->max_batch * sizeof(EngResult));
+    l.d_st = (EngState*)dev_alloc(ctx, sizeof(EngState));
+    BCMC_CUDA(cudaMemsetAsync(l.d_st, 0, sizeof(EngState), e->stream));
+    l.q_nactive = (uint32_t*)dev_alloc(ctx, e->max_batch * 4);
+    l.q_nverts = (uint32_t*)dev_alloc(ctx, e->max_batch * 4);
+    l.ready = true;
+    // with a vertex budget the buffer is sized for it once, up front
+    eng_ensure_verts(e, e->opts.vertex_budget ? e->opts.vertex_budget
+                                              : (e->opts.vertex_capacity ? e->opts.vertex_capacity : (1ull << 24)));
+    eng_ensure_status(e, 1024);
+    eng_ensure_batch(e, 1u << 16, 1u << 16);
+    BCMC_CUDA(cudaStreamSynchronize(e->stream));
+}
+
+void eng_lane_free(bcmc_engine* e, EngLane& l)
+{
+    bcmc_ctx* ctx = e->ctx;
+    for (auto& kv : l.graphs) {
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        if (kv.second.front) cudaGraphExecDestroy(kv.second.front);
+        if (kv.second.back) cudaGraphExecDestroy(kv.second.back);
+    }
+    l.graphs.clear();
+    dev_free(ctx, l.d_queries, e->max_batch * sizeof(EngQuery));
+    dev_free(ctx, l.d_results, e->max_batch * sizeof(EngResult));
+    dev_free(ctx, l.d_st, sizeof(EngState));
+    dev_free(ctx, l.q_nactive, e->max_batch * 4);
+    dev_free(ctx, l.q_nverts, e->max_batch * 4);
+    dev_free(ctx, l.bitmap, l.bitmap_words * 4);
+    dev_free(ctx, l.ent_id, (size_t)l.entry_cap * 4);
+    dev_free(ctx, l.ent_q, (size_t)l.entry_cap * 4);
+    dev_free(ctx, l.block_counts, (size_t)l.entry_cap * 4);
+    dev_free(ctx, l.verts, l.vert_cap * sizeof(uint2));
+    dev_free(ctx, l.status, l.status_words * 8);
+    if (l.h_queries) cudaFreeHost(l.h_queries);
+    if (l.h_results) cudaFreeHost(l.h_results);
+    if (l.h_st) cudaFreeHost(l.h_st);
+    if (l.ev0) cudaEventDestroy(l.ev0);
+    if (l.ev1) cudaEventDestroy(l.ev1);
+    if (l.ev_front) cudaEventDestroy(l.ev_front);
+    if (l.ev_done) cudaEventDestroy(l.ev_done);
+    l = EngLane{};
 }
 
 // The launch sequence of one batch (also what a graph captures).
-void eng_enqueue(bcmc_engine* e, uint32_t bucket)
+// Phase 1 of a batch: inputs in, active test, claims, decode of the claimed
+// blocks into their slots.
+void eng_enqueue_front(bcmc_engine* e, uint32_t bucket, cudaStream_t s)
 {
-    cudaStream_t s = e->stream;
     const BatchArgs a = eng_args(e);
-    BCMC_CUDA(cudaMemcpyAsync(e->d_queries, e->h_queries, bucket * sizeof(EngQuery), cudaMemcpyHostToDevice, s));
-    BCMC_CUDA(cudaMemcpyAsync(e->d_st, e->h_st, offsetof(EngState, epoch), cudaMemcpyHostToDevice, s));
-    BCMC_CUDA(cudaEventRecordWithFlags(e->ev0, s, cudaEventRecordExternal));
-    k_bbegin<<<1, 1024, 0, s>>>(e->d_st, e->q_nverts, e->q_nactive, bucket);
+    BCMC_CUDA(cudaMemcpyAsync(e->L->d_queries, e->L->h_queries, bucket * sizeof(EngQuery), cudaMemcpyHostToDevice, s));
+    BCMC_CUDA(cudaMemcpyAsync(e->L->d_st, e->L->h_st, offsetof(EngState, epoch), cudaMemcpyHostToDevice, s));
+    BCMC_CUDA(cudaEventRecordWithFlags(e->L->ev0, s, cudaEventRecordExternal));
+    k_bbegin<<<1, 1024, 0, s>>>(e->L->d_st, e->L->q_nverts, e->L->q_nactive, bucket);
     k_bactive<<<eng_grid_act(e), kEngThreads, 0, s>>>(a);
-    if (e->cfg.dec_threads == 64) k_bdecode<64><<<eng_grid_dec(e), 64, 0, s>>>(a);
-    else if (e->cfg.dec_threads == 256) k_bdecode<256><<<eng_grid_dec(e), 256, 0, s>>>(a);
-    else k_bdecode<128><<<eng_grid_dec(e), 128, 0, s>>>(a);
+    const uint32_t r = e->max_rate;
+    if (e->cfg.dec_threads == 64) {
+        const size_t smem = zfp_stage_smem(64, r);
+        allow_smem(k_bdecode<64>, smem);
+        k_bdecode<64><<<eng_grid_dec(e), 64, smem, s>>>(a, r);
+    } else if (e->cfg.dec_threads == 256) {
+        const size_t smem = zfp_stage_smem(256, r);
+        allow_smem(k_bdecode<256>, smem);
+        k_bdecode<256><<<eng_grid_dec(e), 256, smem, s>>>(a, r);
+    } else {
+        const size_t smem = zfp_stage_smem(128, r);
+        allow_smem(k_bdecode<128>, smem);
+        k_bdecode<128><<<eng_grid_dec(e), 128, smem, s>>>(a, r);
+    }
     count_launches(3);
-    k_bmc<<<eng_grid_mc(e), kBmcThreads, 0, s>>>(a);
+    BCMC_CUDA(cudaGetLastError());
+}
+
+// Phase 2: marching cubes over the batch's entries, per-query results, state out.
+void eng_enqueue_back(bcmc_engine* e, uint32_t bucket, cudaStream_t s)
+{
+    const BatchArgs a = eng_args(e);
+    if (e->cfg.mc_blocks == 8) k_bmc<8><<<eng_grid_mc(e), 16 * 8, 0, s>>>(a);
+    else if (e->cfg.mc_blocks == 32) k_bmc<32><<<eng_grid_mc(e), 16 * 32, 0, s>>>(a);
+    else k_bmc<16><<<eng_grid_mc(e), 16 * 16, 0, s>>>(a);
     k_bfinish<<<1, kFinThreads, 0, s>>>(a);
     count_launches(2);
     BCMC_CUDA(cudaGetLastError());
-    BCMC_CUDA(cudaEventRecordWithFlags(e->ev1, s, cudaEventRecordExternal));
-    BCMC_CUDA(cudaMemcpyAsync(e->h_st, e->d_st, sizeof(EngState), cudaMemcpyDeviceToHost, s));
-    BCMC_CUDA(cudaMemcpyAsync(e->h_results, e->d_results, bucket * sizeof(EngResult), cudaMemcpyDeviceToHost, s));
+    BCMC_CUDA(cudaEventRecordWithFlags(e->L->ev1, s, cudaEventRecordExternal));
+    BCMC_CUDA(cudaMemcpyAsync(e->L->h_st, e->L->d_st, sizeof(EngState), cudaMemcpyDeviceToHost, s));
+    BCMC_CUDA(cudaMemcpyAsync(e->L->h_results, e->L->d_results, bucket * sizeof(EngResult), cudaMemcpyDeviceToHost, s));
+}
+
+// The launch sequence of one batch on one stream (also what a graph captures).
+void eng_enqueue(bcmc_engine* e, uint32_t bucket)
+{
+    eng_enqueue_front(e, bucket, e->stream);
+    eng_enqueue_back(e, bucket, e->stream);
+}
+
+int eng_cfg_key(const EngConfig& c)
+{
+    const int log_blocks = c.mc_blocks == 8 ? 3 : (c.mc_blocks == 32 ? 5 : 4);
+    return c.act_per_sm | (c.dec_threads << 8) | (c.dec_per_sm << 18) | (c.mc_per_sm << 24) | (log_blocks << 27);
+}
+
+// Captures what `enqueue` issues on stream s into a graph.
+template <typename F>
+cudaGraphExec_t eng_capture(cudaStream_t s, F&& enqueue)
+{
+    cudaGraph_t graph = nullptr;
+    const uint64_t before = g_kernel_launches.load();
+    BCMC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+        enqueue();
+    } catch (...) {
+        cudaStreamEndCapture(s, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        throw;
+    }
+    BCMC_CUDA(cudaStreamEndCapture(s, &graph));
+    g_kernel_launches.store(before);  // captured, not launched
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t err = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    BCMC_CUDA(err);
+    return exec;
 }
 
 void eng_launch(bcmc_engine* e, uint32_t bucket)
 {
     auto it = e->tuned.find(bucket);
     e->cfg = it != e->tuned.end() ? it->second : EngConfig{};
-    auto& g = e->graphs[bucket];
-    const int key = e->cfg.act_per_sm | (e->cfg.dec_threads << 8) | (e->cfg.dec_per_sm << 18) | (e->cfg.mc_per_sm << 26);
-    if (!g.exec || g.generation != e->generation || g.cfg_key != key) {
+    auto& g = e->L->graphs[bucket];
+    const int key = eng_cfg_key(e->cfg);
+    if (!g.exec || g.generation != e->L->generation || g.cfg_key != key) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
         g.exec = nullptr;
-        cudaGraph_t graph = nullptr;
-        const uint64_t before = g_kernel_launches.load();
-        BCMC_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-        try {
-            eng_enqueue(e, bucket);
-        } catch (...) {
-            cudaStreamEndCapture(e->stream, &graph);
-            if (graph) cudaGraphDestroy(graph);
-            throw;
-        }
-        BCMC_CUDA(cudaStreamEndCapture(e->stream, &graph));
-        g_kernel_launches.store(before);  // captured, not launched
-        const cudaError_t err = cudaGraphInstantiate(&g.exec, graph, 0);
-        cudaGraphDestroy(graph);
-        BCMC_CUDA(err);
-        g.generation = e->generation;
+        g.exec = eng_capture(e->stream, [&] { eng_enqueue(e, bucket); });
+        g.generation = e->L->generation;
         g.cfg_key = key;
     }
     BCMC_CUDA(cudaGraphLaunch(g.exec, e->stream));
+    count_launches(5);
+}
+
+// Pipelined launch: phase 1 on the front stream, phase 2 on the back stream
+// after it.  The next batch's phase 1 (front stream) can then run while this
+// batch's phase 2 does.
+void eng_launch_split(bcmc_engine* e, uint32_t bucket)
+{
+    auto it = e->tuned.find(bucket);
+    e->cfg = it != e->tuned.end() ? it->second : EngConfig{};
+    auto& g = e->L->graphs[bucket];
+    const int key = eng_cfg_key(e->cfg);
+    if (!g.front || g.split_generation != e->L->generation || g.split_cfg_key != key) {
+        if (g.front) cudaGraphExecDestroy(g.front);
+        if (g.back) cudaGraphExecDestroy(g.back);
+        g.front = g.back = nullptr;
+        g.front = eng_capture(e->stream, [&] { eng_enqueue_front(e, bucket, e->stream); });
+        g.back = eng_capture(e->stream_back, [&] { eng_enqueue_back(e, bucket, e->stream_back); });
+        g.split_generation = e->L->generation;
+        g.split_cfg_key = key;
+    }
+    BCMC_CUDA(cudaGraphLaunch(g.front, e->stream));
+    BCMC_CUDA(cudaEventRecord(e->L->ev_front, e->stream));
+    BCMC_CUDA(cudaStreamWaitEvent(e->stream_back, e->L->ev_front, 0));
+    BCMC_CUDA(cudaGraphLaunch(g.back, e->stream_back));
     count_launches(5);
 }
 
@@ -998,43 +1191,79 @@ struct AdmitPrefix : std::length_error {
 
 // Runs queries[0..n) (n <= max_batch) as one launch sequence; results go to out.
 // Throws std::length_error when the pool cannot hold the sequence's active blocks.
-void eng_run_sequence(bcmc_engine* e, const bcmc_query* queries, uint32_t n, bcmc_query_result* out)
+struct SeqShape {
+    uint32_t bucket;
+    uint64_t tiles, words;
+};
+
+// The current lane's query table for queries[0..n), padded to the batch-size
+// bucket, and its buffers sized for it.
+SeqShape eng_prepare(bcmc_engine* e, const bcmc_query* queries, uint32_t n)
 {
-    const uint32_t bucket = std::min(bucket_of(n), e->max_batch);
-    uint64_t tiles = 0, words = 0;
-    for (uint32_t i = 0; i < bucket; ++i) {
+    SeqShape sh{std::min(bucket_of(n), e->max_batch), 0, 0};
+    for (uint32_t i = 0; i < sh.bucket; ++i) {
         EngQuery q{};
         if (i < n) {
             if (queries[i].volume >= e->vols.size()) throw std::invalid_argument("unknown volume id");
             const EngVolume& v = e->vols[queries[i].volume];
             q.vol = queries[i].volume;
             q.iso = queries[i].isovalue;
-            q.tile0 = (uint32_t)tiles;
-            q.bit0 = (uint32_t)words;
-            tiles += v.tiles;
-            words += (uint64_t)v.tiles * (kEngTile / 32);
+            q.tile0 = (uint32_t)sh.tiles;
+            q.bit0 = (uint32_t)sh.words;
+            sh.tiles += v.tiles;
+            sh.words += (uint64_t)v.tiles * (kEngTile / 32);
         } else {  // padding queries of the bucket: no tiles
             q.vol = 0;
             q.iso = 0.0f;
-            q.tile0 = (uint32_t)tiles;
-            q.bit0 = (uint32_t)words;
+            q.tile0 = (uint32_t)sh.tiles;
+            q.bit0 = (uint32_t)sh.words;
         }
-        e->h_queries[i] = q;
+        e->L->h_queries[i] = q;
     }
-    if (tiles >= 0xffffffffull || words >= 0xffffffffull) throw std::invalid_argument("batch too large");
-    eng_ensure_status(e, tiles);
-    eng_ensure_batch(e, words, std::max<uint32_t>(e->entry_cap, 1u << 16));
+    if (sh.tiles >= 0xffffffffull || sh.words >= 0xffffffffull) throw std::invalid_argument("batch too large");
+    eng_ensure_status(e, sh.tiles);
+    eng_ensure_batch(e, sh.words, std::max<uint32_t>(e->L->entry_cap, 1u << 16));
+    return sh;
+}
+
+// The current lane's batch inputs for one launch of the sequence.
+void eng_set_inputs(bcmc_engine* e, const SeqShape& sh)
+{
+    EngState& st = *e->L->h_st;
+    st.nq = sh.bucket;
+    st.ntiles = (uint32_t)sh.tiles;
+    st.entry_capacity = e->L->entry_cap;
+    st.use_epoch = e->use_epoch;
+    st.vert_capacity = e->L->vert_cap;
+    st.vert_base = e->L->vert_used;
+}
+
+void eng_take_results(bcmc_engine* e, uint32_t n, bcmc_query_result* out)
+{
+    for (uint32_t i = 0; i < n; ++i) {
+        out[i].vertex_offset = e->L->h_results[i].vstart;
+        out[i].num_vertices = e->L->h_results[i].nverts;
+        out[i].num_active_blocks = e->L->h_results[i].nactive;
+    }
+    e->L->vert_used += e->L->h_st->num_verts;
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, e->L->ev0, e->L->ev1) == cudaSuccess) e->stats.last_batch_ms = ms;
+    e->stats.queries += n;
+}
+
+// Runs queries[0..n) (n <= max_batch) as one launch sequence; results go to out.
+// Throws std::length_error when the pool cannot hold the sequence's active blocks.
+void eng_run_sequence(bcmc_engine* e, const bcmc_query* queries, uint32_t n, bcmc_query_result* out)
+{
+    const SeqShape sh = eng_prepare(e, queries, n);
+    const uint32_t bucket = sh.bucket;
+    const uint64_t words = sh.words;
     ++e->use_epoch;
     for (int attempt = 0;; ++attempt) {
         if (attempt > 8) throw std::runtime_error("batch did not converge");
-        eng_ensure_verts(e, e->vert_used + 1);
-        EngState& st = *e->h_st;
-        st.nq = bucket;
-        st.ntiles = (uint32_t)tiles;
-        st.entry_capacity = e->entry_cap;
-        st.use_epoch = e->use_epoch;
-        st.vert_capacity = e->vert_cap;
-        st.vert_base = e->vert_used;
+        eng_ensure_verts(e, e->L->vert_used + 1);
+        EngState& st = *e->L->h_st;
+        eng_set_inputs(e, sh);
         eng_epoch_tick(e);
         eng_launch(e, bucket);
         BCMC_CUDA(cudaStreamSynchronize(e->stream));
@@ -1065,31 +1294,23 @@ void eng_run_sequence(bcmc_engine* e, const bcmc_query* queries, uint32_t n, bcm
         // vertex admission from the count pass: per-query totals are complete
         // even when the emit pass was refused for lack of room
         const uint64_t limit_seq = std::min<uint64_t>(
-            (1ull << 32) - 1, e->opts.vertex_budget ? e->opts.vertex_budget - std::min(e->opts.vertex_budget, e->vert_used)
+            (1ull << 32) - 1, e->opts.vertex_budget ? e->opts.vertex_budget - std::min(e->opts.vertex_budget, e->L->vert_used)
                                                     : ~0ull);
         if (st.vert_overflow || st.num_verts > limit_seq) {
             uint64_t cum = 0;
             uint32_t fit = 0;
             for (; fit < n; ++fit) {
-                const uint64_t v = e->h_results[fit].nverts;
+                const uint64_t v = e->L->h_results[fit].nverts;
                 if (cum + v > limit_seq) break;
                 cum += v;
             }
             if (fit < n) throw AdmitPrefix(fit);
-            eng_ensure_verts(e, e->vert_used + cum);
+            eng_ensure_verts(e, e->L->vert_used + cum);
             continue;  // the re-run finds every block cached: no decode work repeats
         }
         break;
     }
-    for (uint32_t i = 0; i < n; ++i) {
-        out[i].vertex_offset = e->h_results[i].vstart;
-        out[i].num_vertices = e->h_results[i].nverts;
-        out[i].num_active_blocks = e->h_results[i].nactive;
-    }
-    e->vert_used += e->h_st->num_verts;
-    float ms = 0.0f;
-    if (cudaEventElapsedTime(&ms, e->ev0, e->ev1) == cudaSuccess) e->stats.last_batch_ms = ms;
-    e->stats.queries += n;
+    eng_take_results(e, n, out);
 }
 
 // Admission by slot memory: a batch whose active blocks do not fit the pool
@@ -1110,8 +1331,9 @@ void eng_free(bcmc_engine* e)
 {
     bcmc_ctx* ctx = e->ctx;
     if (e->stream) cudaStreamSynchronize(e->stream);
-    for (auto& kv : e->graphs)
-        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    if (e->stream_back) cudaStreamSynchronize(e->stream_back);
+    if (e->stream_copy) cudaStreamSynchronize(e->stream_copy);
+    for (EngLane& l : e->lanes) eng_lane_free(e, l);
     for (auto& v : e->vols) {
         dev_free(ctx, v.words, v.words_bytes);
         dev_free(ctx, v.ranges, (size_t)v.total * 8);
@@ -1126,27 +1348,13 @@ void eng_free(bcmc_engine* e)
     dev_free(ctx, e->owner_block, e->pool_slots * 4);
     dev_free(ctx, e->d_pool, sizeof(EngPool));
     dev_free(ctx, e->d_evicted, 8);
-    dev_free(ctx, e->d_queries, e->max_batch * sizeof(EngQuery));
-    dev_free(ctx, e->d_results, e->max_batch * sizeof(EngResult));
-    dev_free(ctx, e->d_st, sizeof(EngState));
-    dev_free(ctx, e->q_nactive, e->max_batch * 4);
-    dev_free(ctx, e->q_nverts, e->max_batch * 4);
-    dev_free(ctx, e->bitmap, e->bitmap_words * 4);
-    dev_free(ctx, e->ent_id, (size_t)e->entry_cap * 4);
-    dev_free(ctx, e->ent_q, (size_t)e->entry_cap * 4);
-    dev_free(ctx, e->block_counts, (size_t)e->entry_cap * 4);
     dev_free(ctx, e->dec_vol, (size_t)e->dec_cap * 4);
     dev_free(ctx, e->dec_block, (size_t)e->dec_cap * 4);
     dev_free(ctx, e->dec_slot, (size_t)e->dec_cap * 4);
-    dev_free(ctx, e->verts, e->vert_cap * sizeof(uint2));
-    dev_free(ctx, e->status, e->status_words * 8);
-    if (e->h_queries) cudaFreeHost(e->h_queries);
-    if (e->h_results) cudaFreeHost(e->h_results);
-    if (e->h_st) cudaFreeHost(e->h_st);
     if (e->h_pool) cudaFreeHost(e->h_pool);
-    if (e->ev0) cudaEventDestroy(e->ev0);
-    if (e->ev1) cudaEventDestroy(e->ev1);
     if (e->stream) cudaStreamDestroy(e->stream);
+    if (e->stream_back) cudaStreamDestroy(e->stream_back);
+    if (e->stream_copy) cudaStreamDestroy(e->stream_copy);
     delete e;
     ctx_child_removed(ctx);
 }
@@ -1192,27 +1400,13 @@ extern "C" bcmc_status bcmc_engine_create(bcmc_ctx* ctx, const bcmc_engine_opts*
     const bcmc_status st = eng_guarded(e, [&]() -> bcmc_status {
         BCMC_CUDA(cudaSetDevice(ctx->device));
         BCMC_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
-        BCMC_CUDA(cudaEventCreate(&e->ev0));
-        BCMC_CUDA(cudaEventCreate(&e->ev1));
+        BCMC_CUDA(cudaStreamCreateWithFlags(&e->stream_back, cudaStreamNonBlocking));
+        BCMC_CUDA(cudaStreamCreateWithFlags(&e->stream_copy, cudaStreamNonBlocking));
         e->max_batch = bucket_of(e->opts.max_batch ? std::min<uint32_t>(e->opts.max_batch, 1u << 16) : 1024u);
-        BCMC_CUDA(cudaMallocHost(&e->h_queries, e->max_batch * sizeof(EngQuery)));
-        BCMC_CUDA(cudaMallocHost(&e->h_results, e->max_batch * sizeof(EngResult)));
-        BCMC_CUDA(cudaMallocHost(&e->h_st, sizeof(EngState)));
         BCMC_CUDA(cudaMallocHost(&e->h_pool, sizeof(EngPool)));
-        memset(e->h_st, 0, sizeof(EngState));
-        e->d_queries = (EngQuery*)dev_alloc(ctx, e->max_batch * sizeof(EngQuery));
-        e->d_results = (EngResult*)dev_alloc(ctx, e->max_batch * sizeof(EngResult));
-        e->d_st = (EngState*)dev_alloc(ctx, sizeof(EngState));
-        BCMC_CUDA(cudaMemsetAsync(e->d_st, 0, sizeof(EngState), e->stream));
-        e->q_nactive = (uint32_t*)dev_alloc(ctx, e->max_batch * 4);
-        e->q_nverts = (uint32_t*)dev_alloc(ctx, e->max_batch * 4);
         e->d_pool = (EngPool*)dev_alloc(ctx, sizeof(EngPool));
         e->d_evicted = (unsigned long long*)dev_alloc(ctx, 8);
-        // with a vertex budget the buffer is sized for it once, up front
-        eng_ensure_verts(e, e->opts.vertex_budget ? e->opts.vertex_budget
-                                                  : (e->opts.vertex_capacity ? e->opts.vertex_capacity : (1ull << 24)));
-        eng_ensure_status(e, 1024);
-        eng_ensure_batch(e, 1u << 16, 1u << 16);
+        eng_lane_init(e, 0);
         BCMC_CUDA(cudaStreamSynchronize(e->stream));
         return BCMC_OK;
     });
@@ -1264,6 +1458,10 @@ extern "C" bcmc_status bcmc_engine_add_volume(bcmc_engine* e, const uint8_t* zfp
         BCMC_CUDA(cudaStreamSynchronize(e->stream));
         *volume = (uint32_t)e->vols.size();
         e->vols.push_back(v);
+        if (rate > e->max_rate) {
+            e->max_rate = rate;
+            for (EngLane& l : e->lanes) ++l.generation;  // graphs captured k_bdecode's staging size
+        }
         eng_upload_vols(e);
         return BCMC_OK;
     });
@@ -1280,7 +1478,7 @@ extern "C" bcmc_status bcmc_engine_run(bcmc_engine* e, const bcmc_query* queries
             for (auto& v : e->vols) all += v.total;
             eng_alloc_pool(e, e->opts.pool_slots ? e->opts.pool_slots : all);
         }
-        e->vert_used = 0;
+        e->L->vert_used = 0;
         for (uint32_t i = 0; i < n; i += e->max_batch) {
             const uint32_t m = std::min(e->max_batch, n - i);
             eng_run_chunk(e, queries + i, m, results + i);
@@ -1315,7 +1513,7 @@ double eng_time_sequence(bcmc_engine* e, const bcmc_query* qs, uint32_t n, bcmc_
 {
     double best = 1e30;
     for (int r = 0; r < 3; ++r) {
-        e->vert_used = 0;
+        e->L->vert_used = 0;
         eng_run_sequence(e, qs, n, out);
         best = std::min(best, e->stats.last_batch_ms);
     }
@@ -1326,17 +1524,25 @@ double eng_time_decode(bcmc_engine* e, const EngVolume& v, uint32_t nblk, float*
 {
     float best = 1e30f;
     for (int r = 0; r < 3; ++r) {
-        BCMC_CUDA(cudaEventRecord(e->ev0, e->stream));
+        BCMC_CUDA(cudaEventRecord(e->L->ev0, e->stream));
         const int grid = e->ctx->num_sms * per_sm;
-        if (threads == 64) k_decode_probe<64><<<grid, 64, 0, e->stream>>>(v.words, 64u * v.rate, nblk, scratch);
-        else if (threads == 256) k_decode_probe<256><<<grid, 256, 0, e->stream>>>(v.words, 64u * v.rate, nblk, scratch);
-        else k_decode_probe<128><<<grid, 128, 0, e->stream>>>(v.words, 64u * v.rate, nblk, scratch);
+        const size_t smem = zfp_stage_smem((uint32_t)threads, v.rate);
+        if (threads == 64) {
+            allow_smem(k_decode_probe<64>, smem);
+            k_decode_probe<64><<<grid, 64, smem, e->stream>>>(v.words, v.rate, nblk, scratch);
+        } else if (threads == 256) {
+            allow_smem(k_decode_probe<256>, smem);
+            k_decode_probe<256><<<grid, 256, smem, e->stream>>>(v.words, v.rate, nblk, scratch);
+        } else {
+            allow_smem(k_decode_probe<128>, smem);
+            k_decode_probe<128><<<grid, 128, smem, e->stream>>>(v.words, v.rate, nblk, scratch);
+        }
         count_launches(1);
         BCMC_CUDA(cudaGetLastError());
-        BCMC_CUDA(cudaEventRecord(e->ev1, e->stream));
-        BCMC_CUDA(cudaEventSynchronize(e->ev1));
+        BCMC_CUDA(cudaEventRecord(e->L->ev1, e->stream));
+        BCMC_CUDA(cudaEventSynchronize(e->L->ev1));
         float ms = 0.0f;
-        BCMC_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+        BCMC_CUDA(cudaEventElapsedTime(&ms, e->L->ev0, e->L->ev1));
         best = std::min(best, ms);
     }
     return best;
@@ -1358,14 +1564,21 @@ extern "C" bcmc_status bcmc_engine_autotune(bcmc_engine* e, const bcmc_query* qu
         const uint32_t bucket = std::min(bucket_of(m), e->max_batch);
         std::vector<bcmc_query_result> res(m);
         e->tuned.erase(bucket);
-        e->vert_used = 0;
+        e->L->vert_used = 0;
         eng_run_sequence(e, queries, m, res.data());  // warm-up: decodes, buffer growth, graph
         EngConfig best{};
         e->tuned[bucket] = best;
         double t_best = eng_time_sequence(e, queries, m, res.data());
         out->batch_ms_default = t_best;
         // coordinate descent over the sequence's launch parameters
-        for (int mc : {4, 5, 6}) {
+        for (int mb : {8, 32}) {  // MC tile: active blocks per CTA tile
+            EngConfig c = best;
+            c.mc_blocks = mb;
+            e->tuned[bucket] = c;
+            const double t = eng_time_sequence(e, queries, m, res.data());
+            if (t < t_best) best = c, t_best = t;
+        }
+        for (int mc : {4, 5}) {
             EngConfig c = best;
             c.mc_per_sm = mc;
             e->tuned[bucket] = c;
@@ -1410,9 +1623,29 @@ extern "C" bcmc_status bcmc_engine_autotune(bcmc_engine* e, const bcmc_query* qu
         out->decode_threads = best.dec_threads;
         out->decode_ctas_per_sm = best.dec_per_sm;
         out->mc_ctas_per_sm = best.mc_per_sm;
+        out->mc_blocks_per_tile = best.mc_blocks;
         out->bucket = bucket;
         return BCMC_OK;
     });
+}
+
+extern "C" bcmc_status bcmc_engine_set_tuning(bcmc_engine* e, const bcmc_tune_report* c)
+{
+    if (!e || !c) return BCMC_E_ARG;
+    const uint32_t b = c->bucket;
+    const auto in = [](int v, std::initializer_list<int> ok) { return std::find(ok.begin(), ok.end(), v) != ok.end(); };
+    if (b == 0 || (b & (b - 1)) != 0 || b > e->max_batch || !in(c->act_ctas_per_sm, {4, 8, 16}) ||
+        !in(c->decode_threads, {64, 128, 256}) || !in(c->decode_ctas_per_sm, {8, 16, 32}) ||
+        !in(c->mc_ctas_per_sm, {4, 5, 6}) || !in(c->mc_blocks_per_tile, {8, 16, 32}))
+        return BCMC_E_ARG;
+    EngConfig cfg;
+    cfg.act_per_sm = c->act_ctas_per_sm;
+    cfg.dec_threads = c->decode_threads;
+    cfg.dec_per_sm = c->decode_ctas_per_sm;
+    cfg.mc_per_sm = c->mc_ctas_per_sm;
+    cfg.mc_blocks = c->mc_blocks_per_tile;
+    e->tuned[b] = cfg;
+    return BCMC_OK;
 }
 
 extern "C" bcmc_status bcmc_engine_run_admit(bcmc_engine* e, const bcmc_query* queries, uint32_t n,
@@ -1427,7 +1660,7 @@ extern "C" bcmc_status bcmc_engine_run_admit(bcmc_engine* e, const bcmc_query* q
             for (auto& v : e->vols) all += v.total;
             eng_alloc_pool(e, e->opts.pool_slots ? e->opts.pool_slots : all);
         }
-        e->vert_used = 0;
+        e->L->vert_used = 0;
         uint32_t done = 0;
         while (done < n) {
             const uint32_t m = std::min(e->max_batch, n - done);
@@ -1450,17 +1683,17 @@ extern "C" bcmc_status bcmc_engine_run_admit(bcmc_engine* e, const bcmc_query* q
 extern "C" bcmc_status bcmc_engine_vertices(bcmc_engine* e, const void** d_vertices, uint64_t* count)
 {
     if (!e || !d_vertices || !count) return BCMC_E_ARG;
-    *d_vertices = e->verts;
-    *count = e->vert_used;
+    *d_vertices = e->L->verts;
+    *count = e->L->vert_used;
     return BCMC_OK;
 }
 
 extern "C" bcmc_status bcmc_engine_copy_vertices(bcmc_engine* e, uint64_t first, uint64_t count, void* host)
 {
-    if (!e || (count && !host) || first > e->vert_used || count > e->vert_used - first) return BCMC_E_ARG;
+    if (!e || (count && !host) || first > e->L->vert_used || count > e->L->vert_used - first) return BCMC_E_ARG;
     return eng_guarded(e, [&]() -> bcmc_status {
         if (count)
-            BCMC_CUDA(cudaMemcpyAsync(host, e->verts + first, count * sizeof(uint2), cudaMemcpyDeviceToHost, e->stream));
+            BCMC_CUDA(cudaMemcpyAsync(host, e->L->verts + first, count * sizeof(uint2), cudaMemcpyDeviceToHost, e->stream));
         BCMC_CUDA(cudaStreamSynchronize(e->stream));
         return BCMC_OK;
     });
@@ -1478,7 +1711,8 @@ extern "C" bcmc_status bcmc_engine_stats_get(bcmc_engine* e, bcmc_engine_stats* 
             const uint32_t head = std::min(e->h_pool->head, e->h_pool->tail);
             s.pool_used = e->pool_slots - (e->h_pool->tail - head);
         }
-        s.vertex_capacity = e->vert_cap;
+        s.vertex_capacity = e->L->vert_cap;
+        s.overlapped_batches = e->overlapped;
         s.device_bytes = e->ctx->device_bytes;
         *out = s;
         return BCMC_OK;
@@ -1486,6 +1720,100 @@ extern "C" bcmc_status bcmc_engine_stats_get(bcmc_engine* e, bcmc_engine_stats* 
 }
 
 namespace bcmc {
+namespace {
+void eng_ensure_pool(bcmc_engine* e)
+{
+    if (e->pool_slots) return;
+    uint64_t all = 0;
+    for (auto& v : e->vols) all += v.total;
+    eng_alloc_pool(e, e->opts.pool_slots ? e->opts.pool_slots : all);
+}
+}  // namespace
+
+bcmc_status engine_submit(bcmc_engine* e, int k, const bcmc_query* queries, uint32_t n, void (*on_done)(void*),
+                          void* arg)
+{
+    if (!e || k < 0 || k > 1 || !n || !queries || n > e->max_batch) return BCMC_E_ARG;
+    if (e->vols.empty() || e->lanes[k].in_flight) return BCMC_E_STATE;
+    return eng_guarded(e, [&]() -> bcmc_status {
+        eng_ensure_pool(e);
+        eng_lane_init(e, k);
+        EngLane& me = *e->L;
+        me.vert_used = 0;
+        const SeqShape sh = eng_prepare(e, queries, n);
+        ++e->use_epoch;
+        eng_ensure_verts(e, 1);
+        eng_set_inputs(e, sh);
+        eng_epoch_tick(e);
+        eng_launch_split(e, sh.bucket);
+        BCMC_CUDA(cudaEventRecord(me.ev_done, e->stream_back));
+        if (on_done) BCMC_CUDA(cudaLaunchHostFunc(e->stream_back, on_done, arg));
+        me.in_flight = true;
+        me.n = n;
+        me.bucket = sh.bucket;
+        me.batch_epoch = e->use_epoch;
+        me.queries.assign(queries, queries + n);
+        if (e->lanes[1 - k].in_flight) ++e->overlapped;
+        ++e->stats.launch_sequences;
+        ++e->stats.batches;
+        return BCMC_OK;
+    });
+}
+
+bcmc_status engine_complete(bcmc_engine* e, int k, bcmc_query_result* out, uint32_t* admitted)
+{
+    if (!e || k < 0 || k > 1 || !out || !admitted) return BCMC_E_ARG;
+    EngLane& me = e->lanes[k];
+    if (!me.in_flight) return BCMC_E_STATE;
+    *admitted = 0;
+    me.in_flight = false;
+    return eng_guarded(e, [&]() -> bcmc_status {
+        e->L = &me;
+        BCMC_CUDA(cudaEventSynchronize(me.ev_done));
+        const EngState& st = *me.h_st;
+        e->stats.decoded_blocks += st.num_decode;
+        if (st.error) throw std::runtime_error("device wait timed out in the batched engine");
+        const uint64_t limit = std::min<uint64_t>((1ull << 32) - 1, e->opts.vertex_budget ? e->opts.vertex_budget : ~0ull);
+        if (st.entry_overflow || st.pool_exhausted || st.vert_overflow || st.num_verts > limit) {
+            // buffer growth, eviction or admission: run this batch again on its
+            // own, after both streams have drained (an eviction must not free a
+            // slot the other lane's batch still reads)
+            BCMC_CUDA(cudaStreamSynchronize(e->stream));
+            BCMC_CUDA(cudaStreamSynchronize(e->stream_back));
+            me.vert_used = 0;
+            *admitted = eng_run_prefix(e, me.queries.data(), me.n, out);
+            return BCMC_OK;
+        }
+        eng_take_results(e, me.n, out);
+        *admitted = me.n;
+        return BCMC_OK;
+    });
+}
+
+bcmc_status engine_copy_lane_vertices(bcmc_engine* e, int k, uint64_t first, uint64_t count, void* host)
+{
+    if (!e || k < 0 || k > 1 || (count && !host)) return BCMC_E_ARG;
+    EngLane& l = e->lanes[k];
+    if (first > l.vert_used || count > l.vert_used - first) return BCMC_E_ARG;
+    return eng_guarded(e, [&]() -> bcmc_status {
+        if (count) {
+            BCMC_CUDA(cudaMemcpyAsync(host, l.verts + first, count * sizeof(uint2), cudaMemcpyDeviceToHost,
+                                      e->stream_copy));
+            BCMC_CUDA(cudaStreamSynchronize(e->stream_copy));
+        }
+        return BCMC_OK;
+    });
+}
+
+void engine_drain(bcmc_engine* e)
+{
+    cudaStreamSynchronize(e->stream);
+    cudaStreamSynchronize(e->stream_back);  // also waits for its host callbacks
+    cudaStreamSynchronize(e->stream_copy);
+}
+
+uint32_t engine_max_batch(bcmc_engine* e) { return e->max_batch; }
+
 int engine_device(bcmc_engine* e) { return e->ctx->device; }
 uint64_t engine_vertex_budget(bcmc_engine* e) { return e->opts.vertex_budget; }
 bcmc_ctx* engine_ctx(bcmc_engine* e) { return e->ctx; }

@@ -453,28 +453,47 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
 // when `words` is set: copied from the staging buffer k_decode_new filled,
 // decoded here for new-block indices past it).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_assign(QueryState* q, AssignArgs a)
+constexpr int kAssignThreads = 128;
+
+__global__ void __launch_bounds__(kAssignThreads) k_assign(QueryState* q, AssignArgs a)
 {
     if (q->num_active == 0 || q->grow_needed) return;
     const uint32_t n = q->num_new;
     const uint32_t size = q->new_cache_size;
     const uint32_t* __restrict__ sorted = q->sort_final == 1 ? a.sorted_b : a.sorted_c;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t item = a.new_ids[i];
-        const uint32_t slot = sorted[i];
-        if (slot >= size) {  // cannot happen with a consistent sort; never write out of bounds
-            atomicCAS(&q->error, 0u, 50u);
-            continue;
+    // new blocks decoded here (all of them for the standalone LRU update, those
+    // past the staging buffer on the query path) are staged in shared memory
+    extern __shared__ __align__(16) uint32_t s_words[];
+    const uint32_t rate = a.max_bits / 64u;
+    const uint32_t first_decode = a.stage ? a.stage_blocks : 0u;
+    if (a.words && threadIdx.x < 4) s_words[kAssignThreads * 2u * rate + threadIdx.x] = 0u;
+    for (uint32_t i0 = blockIdx.x * kAssignThreads; i0 < n; i0 += gridDim.x * kAssignThreads) {
+        const uint32_t i = i0 + threadIdx.x;
+        uint32_t item = 0, slot = 0xffffffffu;
+        if (i < n) {
+            item = a.new_ids[i];
+            slot = sorted[i];
+            if (slot >= size) {  // cannot happen with a consistent sort; never write out of bounds
+                atomicCAS(&q->error, 0u, 50u);
+                slot = 0xffffffffu;
+            } else {
+                const int32_t prev = a.slot_item[slot];
+                if (prev != -1) a.item_slots[prev] = -1;
+                a.slot_age[slot] = 0;
+                a.slot_item[slot] = (int32_t)item;
+                a.slot_avail[slot] = 0;
+                a.item_slots[item] = (int32_t)slot;
+            }
         }
-        const int32_t prev = a.slot_item[slot];
-        if (prev != -1) a.item_slots[prev] = -1;
-        a.slot_age[slot] = 0;
-        a.slot_item[slot] = (int32_t)item;
-        a.slot_avail[slot] = 0;
-        a.item_slots[item] = (int32_t)slot;
-        if (a.words && i >= a.stage_blocks) {
+        if (!a.words || i0 + kAssignThreads <= first_decode) continue;  // no decode in this group (uniform)
+        const bool dec = slot != 0xffffffffu && i >= first_decode;
+        __syncthreads();
+        if (dec) zfp_stage_block(a.words, item, rate, s_words);
+        __syncthreads();
+        if (dec) {
             float v[64];
-            zfp_decode_block<1>(a.words, (uint64_t)item * a.max_bits, a.max_bits, v);
+            zfp_decode_staged(s_words + threadIdx.x * 2u * rate, a.max_bits,
+                              s_words + zfp_stage_words(kAssignThreads, rate) + threadIdx.x * kZfpPlaneWords, v);
             float4* d4 = reinterpret_cast<float4*>(a.cache + (uint64_t)slot * 64u);
 #pragma unroll
             for (int k = 0; k < 16; ++k) d4[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
@@ -498,13 +517,24 @@ __global__ void __launch_bounds__(128) k_assign(QueryState* q, AssignArgs a)
 // only, so it runs beside k_slots and the sort; k_assign then copies the
 // staged blocks into the slots the sort chose.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_decode_new(const QueryState* q, DecodeArgs a)
+constexpr int kDecodeNewThreads = 128;
+
+__global__ void __launch_bounds__(kDecodeNewThreads) k_decode_new(const QueryState* q, DecodeArgs a)
 {
     if (q->num_active == 0 || q->grow_needed) return;
     const uint32_t n = q->num_new < a.stage_blocks ? q->num_new : a.stage_blocks;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    extern __shared__ __align__(16) uint32_t s_words[];
+    const uint32_t rate = a.max_bits / 64u;
+    uint32_t* pl = s_words + zfp_stage_words(kDecodeNewThreads, rate) + threadIdx.x * kZfpPlaneWords;
+    if (threadIdx.x < 4) s_words[kDecodeNewThreads * 2u * rate + threadIdx.x] = 0u;
+    for (uint32_t i0 = blockIdx.x * kDecodeNewThreads; i0 < n; i0 += gridDim.x * kDecodeNewThreads) {
+        const uint32_t i = i0 + threadIdx.x;
+        __syncthreads();
+        if (i < n) zfp_stage_block(a.words, a.new_ids[i], rate, s_words);
+        __syncthreads();
+        if (i >= n) continue;
         float v[64];
-        zfp_decode_block<1>(a.words, (uint64_t)a.new_ids[i] * a.max_bits, a.max_bits, v);
+        zfp_decode_staged(s_words + threadIdx.x * 2u * rate, a.max_bits, pl, v);
         float4* d4 = reinterpret_cast<float4*>(a.stage + (uint64_t)i * 64u);
 #pragma unroll
         for (int k = 0; k < 16; ++k) d4[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
@@ -884,7 +914,9 @@ void slots_launch(bcmc_ctx* ctx, QueryState* q, const SlotArgs& a, uint32_t max_
 
 void assign_launch(bcmc_ctx* ctx, QueryState* q, const AssignArgs& a, uint32_t max_new, cudaStream_t s)
 {
-    k_assign<<<pgrid(ctx, div_up(max_new, 128u), 16), 128, 0, s>>>(q, a);
+    const size_t smem = a.words ? zfp_stage_smem(kAssignThreads, a.max_bits / 64u) : 0;
+    allow_smem(k_assign, smem);
+    k_assign<<<pgrid(ctx, div_up(max_new, (uint32_t)kAssignThreads), 16), kAssignThreads, smem, s>>>(q, a);
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
 }
@@ -893,7 +925,10 @@ void decode_new_launch(bcmc_ctx* ctx, const QueryState* q, const DecodeArgs& a, 
 {
     // two CTAs per SM: the branch it runs on must leave room for the slot
     // selection's CTAs, the critical path beside it
-    k_decode_new<<<pgrid(ctx, div_up(a.stage_blocks ? a.stage_blocks : 1u, 128u), 2), 128, 0, s>>>(q, a);
+    const size_t smem = zfp_stage_smem(kDecodeNewThreads, a.max_bits / 64u);
+    allow_smem(k_decode_new, smem);
+    k_decode_new<<<pgrid(ctx, div_up(a.stage_blocks ? a.stage_blocks : 1u, (uint32_t)kDecodeNewThreads), 2),
+                   kDecodeNewThreads, smem, s>>>(q, a);
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
 }

@@ -2,13 +2,19 @@
 // (bcmc_server_* in include/bcmc.h).  Host code only: a worker thread owns the
 // engine; clients submit (volume, isovalue) requests from any thread.
 //
-// Whenever the device is free the worker takes every request that has arrived
-// (up to max_batch, after an optional short wait for company) and runs them as
-// one engine batch; requests arriving meanwhile queue for the next batch.
-// Admission by memory: the engine runs the longest prefix of the batch whose
-// active blocks fit the slot pool and whose vertex count (known after the
-// count pass) fits the vertex budget; the rest goes back to the front of the
-// queue for the next batch.
+// The worker keeps up to two batches on the device.  Whenever a lane of batch
+// buffers is free it takes every request that has arrived (up to max_batch;
+// with nothing in flight, after an optional short wait for company) and
+// launches them as one batch without waiting for it.  So requests that arrive
+// while a batch is on the GPU go out at once in the next one: its active test,
+// cache claims and decode run while the first batch's marching cubes do, and
+// its marching cubes follow on the device.  A batch's completion (a host
+// callback after its results reach the host) wakes the worker, which hands the
+// results to their waiters.  Admission by memory: a batch whose active blocks
+// do not fit the slot pool, or whose vertex count (known after the count
+// pass) does not fit the vertex budget, is run again on its own; the longest
+// prefix that fits is answered and the rest goes back to the front of the
+// queue.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -53,74 +59,132 @@ struct bcmc_server {
     std::unordered_map<uint64_t, Done> done;
     uint64_t next_ticket = 1;
     bool stop = false;
+    bool lane_done[2] = {false, false};  // set by the completion callback
     std::thread worker;
-    uint64_t batches = 0, batched_requests = 0;
+    uint64_t batches = 0, batched_requests = 0, overlapped = 0;
     double avg_verts = 0.0;  // worker only
 };
 
 namespace {
 
+struct LaneDone {
+    bcmc_server* s;
+    int lane;
+};
+
+// Runs on a CUDA host thread once a batch's results are on the host.
+void on_lane_done(void* p)
+{
+    LaneDone* d = static_cast<LaneDone*>(p);
+    {
+        std::lock_guard<std::mutex> lk(d->s->mu);
+        d->s->lane_done[d->lane] = true;
+    }
+    d->s->cv_work.notify_all();
+}
+
+struct InFlight {
+    int lane;
+    std::vector<Request> batch;
+};
+
+// Hands a batch's outcome to its waiters (under the lock).
+void finish_batch(bcmc_server* s, std::vector<Request>& batch, const std::vector<bcmc_query_result>& res,
+                  bcmc_status st)
+{
+    const Clock::time_point t = Clock::now();
+    ++s->batches;
+    s->batched_requests += batch.size();
+    if (st == BCMC_OK)
+        for (size_t i = 0; i < batch.size(); ++i)  // running mean of vertices per request
+            s->avg_verts = s->avg_verts == 0.0 ? (double)res[i].num_vertices + 1.0
+                                               : 0.98 * s->avg_verts + 0.02 * (double)res[i].num_vertices;
+    for (size_t i = 0; i < batch.size(); ++i) {
+        Done d;
+        d.status = st;
+        d.result = st == BCMC_OK ? res[i] : bcmc_query_result{};
+        d.result.vertex_offset = 0;
+        d.latency_ms = std::chrono::duration<double, std::milli>(t - batch[i].arrive).count();
+        s->done[batch[i].ticket] = d;
+    }
+}
+
 void worker_loop(bcmc_server* s)
 {
     cudaSetDevice(bcmc::engine_device(s->eng));
-    std::vector<Request> batch;
+    std::deque<InFlight> inflight;  // oldest first, at most two
+    LaneDone cb[2] = {{s, 0}, {s, 1}};
     std::vector<bcmc_query> qs;
     std::vector<bcmc_query_result> res;
     for (;;) {
+        std::vector<Request> batch;
+        int lane = -1;
         {
             std::unique_lock<std::mutex> lk(s->mu);
-            s->cv_work.wait(lk, [&] { return s->stop || !s->pending.empty(); });
-            if (s->pending.empty()) return;  // stop requested and nothing left
-            if (s->opts.max_wait_us && s->pending.size() < s->opts.max_batch && !s->stop) {
-                s->cv_work.wait_for(lk, std::chrono::microseconds(s->opts.max_wait_us),
-                                    [&] { return s->stop || s->pending.size() >= s->opts.max_batch; });
+            s->cv_work.wait(lk, [&] {
+                const bool can_launch = !s->pending.empty() && inflight.size() < 2;
+                const bool oldest_done = !inflight.empty() && s->lane_done[inflight.front().lane];
+                return can_launch || oldest_done || (s->stop && inflight.empty());
+            });
+            if (s->pending.empty() && inflight.empty()) return;  // stop requested and nothing left
+            if (!s->pending.empty() && inflight.size() < 2) {
+                if (inflight.empty() && s->opts.max_wait_us && s->pending.size() < s->opts.max_batch && !s->stop) {
+                    s->cv_work.wait_for(lk, std::chrono::microseconds(s->opts.max_wait_us),
+                                        [&] { return s->stop || s->pending.size() >= s->opts.max_batch; });
+                }
+                // size the batch so that its expected vertex count stays within the
+                // engine's vertex budget: an over-full batch would pay a count pass
+                // for requests the engine then refuses
+                size_t cap_n = std::min<size_t>(s->opts.max_batch, bcmc::engine_max_batch(s->eng));
+                const uint64_t budget = bcmc::engine_vertex_budget(s->eng);
+                if (budget && s->avg_verts > 0.0)
+                    cap_n = std::max<size_t>(1, std::min<size_t>(cap_n, (size_t)(0.8 * (double)budget / s->avg_verts)));
+                const size_t n = std::min<size_t>(s->pending.size(), cap_n);
+                batch.assign(s->pending.begin(), s->pending.begin() + n);
+                s->pending.erase(s->pending.begin(), s->pending.begin() + n);
+                lane = inflight.empty() ? 0 : 1 - inflight.front().lane;
+                s->lane_done[lane] = false;
+                if (!inflight.empty()) ++s->overlapped;
             }
-            // size the batch so that its expected vertex count stays within the
-            // engine's vertex budget: an over-full batch would pay a count pass
-            // for requests the engine then refuses
-            size_t cap_n = s->opts.max_batch;
-            const uint64_t budget = bcmc::engine_vertex_budget(s->eng);
-            if (budget && s->avg_verts > 0.0)
-                cap_n = std::max<size_t>(1, std::min<size_t>(cap_n, (size_t)(0.8 * (double)budget / s->avg_verts)));
-            const size_t n = std::min<size_t>(s->pending.size(), cap_n);
-            batch.assign(s->pending.begin(), s->pending.begin() + n);
-            s->pending.erase(s->pending.begin(), s->pending.begin() + n);
         }
-        qs.resize(batch.size());
-        res.assign(batch.size(), bcmc_query_result{});
-        for (size_t i = 0; i < batch.size(); ++i) qs[i] = bcmc_query{batch[i].volume, batch[i].iso};
+        if (lane >= 0) {  // launch, do not wait
+            qs.resize(batch.size());
+            for (size_t i = 0; i < batch.size(); ++i) qs[i] = bcmc_query{batch[i].volume, batch[i].iso};
+            const bcmc_status st =
+                bcmc::engine_submit(s->eng, lane, qs.data(), (uint32_t)qs.size(), on_lane_done, &cb[lane]);
+            if (st == BCMC_OK) {
+                inflight.push_back(InFlight{lane, std::move(batch)});
+            } else {
+                std::lock_guard<std::mutex> lk(s->mu);
+                finish_batch(s, batch, res, st);
+                s->cv_done.notify_all();
+            }
+            continue;
+        }
+        // the oldest batch is done: its results to their waiters
+        InFlight f = std::move(inflight.front());
+        inflight.pop_front();
+        res.assign(f.batch.size(), bcmc_query_result{});
         uint32_t admitted = 0;
-        bcmc_status st = bcmc_engine_run_admit(s->eng, qs.data(), (uint32_t)qs.size(), res.data(), &admitted);
-        if (st == BCMC_OK && admitted < batch.size()) {
-            // the rest did not fit this batch's memory: back to the front of the queue
-            std::lock_guard<std::mutex> lk(s->mu);
-            s->pending.insert(s->pending.begin(), batch.begin() + admitted, batch.end());
-            batch.resize(admitted);
+        bcmc_status st = bcmc::engine_complete(s->eng, f.lane, res.data(), &admitted);
+        std::vector<Request> rest;
+        if (st == BCMC_OK && admitted < f.batch.size()) {
+            rest.assign(f.batch.begin() + admitted, f.batch.end());
+            f.batch.resize(admitted);
         }
         if (st == BCMC_OK) {
-            for (size_t i = 0; i < batch.size() && st == BCMC_OK; ++i) {
-                if (!batch[i].host || !res[i].num_vertices) continue;
-                const uint64_t n = std::min<uint64_t>(res[i].num_vertices, batch[i].host_capacity);
-                st = bcmc_engine_copy_vertices(s->eng, res[i].vertex_offset, n, batch[i].host);
+            for (size_t i = 0; i < f.batch.size() && st == BCMC_OK; ++i) {
+                if (!f.batch[i].host || !res[i].num_vertices) continue;
+                const uint64_t n = std::min<uint64_t>(res[i].num_vertices, f.batch[i].host_capacity);
+                st = bcmc::engine_copy_lane_vertices(s->eng, f.lane, res[i].vertex_offset, n, f.batch[i].host);
             }
         }
-        const Clock::time_point t = Clock::now();
         {
             std::lock_guard<std::mutex> lk(s->mu);
-            ++s->batches;
-            s->batched_requests += batch.size();
-            if (st == BCMC_OK)
-                for (size_t i = 0; i < batch.size(); ++i)  // running mean of vertices per request
-                    s->avg_verts = s->avg_verts == 0.0 ? (double)res[i].num_vertices + 1.0
-                                                       : 0.98 * s->avg_verts + 0.02 * (double)res[i].num_vertices;
-            for (size_t i = 0; i < batch.size(); ++i) {
-                Done d;
-                d.status = st;
-                d.result = res[i];
-                d.result.vertex_offset = 0;
-                d.latency_ms = std::chrono::duration<double, std::milli>(t - batch[i].arrive).count();
-                s->done[batch[i].ticket] = d;
-            }
+            // the rest did not fit this batch's memory: back to the front of the queue
+            if (!rest.empty()) s->pending.insert(s->pending.begin(), rest.begin(), rest.end());
+            s->lane_done[f.lane] = false;
+            finish_batch(s, f.batch, res, st);
         }
         s->cv_done.notify_all();
     }
@@ -156,6 +220,7 @@ extern "C" void bcmc_server_destroy(bcmc_server* s)
     }
     s->cv_work.notify_all();
     if (s->worker.joinable()) s->worker.join();
+    bcmc::engine_drain(s->eng);  // the last completion callback has returned
     delete s;
 }
 
@@ -198,10 +263,11 @@ extern "C" bcmc_status bcmc_server_run_load(bcmc_server* s, const bcmc_load_spec
     std::discrete_distribution<uint32_t> pick(w.begin(), w.end());
     std::uniform_real_distribution<float> unit(0.0f, 1.0f);
     std::vector<uint64_t> tickets(spec->requests);
-    uint64_t batches0;
+    uint64_t batches0, overlapped0;
     {
         std::lock_guard<std::mutex> lk(s->mu);
         batches0 = s->batches;
+        overlapped0 = s->overlapped;
     }
     const Clock::time_point t0 = Clock::now();
     double at = 0.0;
@@ -246,6 +312,7 @@ extern "C" bcmc_status bcmc_server_run_load(bcmc_server* s, const bcmc_load_spec
     {
         std::lock_guard<std::mutex> lk(s->mu);
         r.batches = s->batches - batches0;
+        r.overlapped_batches = s->overlapped - overlapped0;
     }
     r.mean_batch = r.batches ? (double)spec->requests / (double)r.batches : 0.0;
     *out = r;

@@ -5,27 +5,45 @@
 
 namespace bcmc {
 
+// Decode kernels: the CTA stages its blocks' compressed words in shared
+// memory (zfp_stage_run / zfp_stage_block), each thread decodes one block
+// from there (zfp_decode_staged).  Loop bounds are uniform across the CTA
+// (the staging is followed by a barrier).
+constexpr int kDecThreads = 128;
+constexpr int kDeposit = 0;  // 8x8 bit-transposed deposit
+
+__device__ __forceinline__ uint32_t* stage_words() { extern __shared__ __align__(16) uint32_t s_dyn[]; return s_dyn; }
+
+__device__ __forceinline__ void store_block(float* __restrict__ dst, const float* v)
+{
+    float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) d4[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+}
+
 // zfp_compute_block_range.comp:19-61: min/max over the voxels of each block
 // that lie inside the volume (partial blocks at the +x/+y/+z faces are
-// clipped), starting from (1e20, -1e20).  One thread per block.
-// Bulk decoders: register bit-plane deposit, one block per thread, 128-thread
-// CTAs (measured fastest of the deposit variants on full-volume decodes).
-constexpr int kBulkDeposit = 1;
-constexpr int kBulkThreads = 128;
-
-__global__ void __launch_bounds__(kBulkThreads) k_block_ranges(const uint64_t* __restrict__ words, uint3 dims, uint3 nb,
-                                                      uint32_t max_bits, uint64_t ranged,
-                                                      float2* __restrict__ ranges)
+// clipped), starting from (1e20, -1e20).
+__global__ void __launch_bounds__(kDecThreads) k_block_ranges(const uint64_t* __restrict__ words, uint3 dims, uint3 nb,
+                                                              uint32_t rate, uint64_t ranged,
+                                                              float2* __restrict__ ranges)
 {
+    uint32_t* s_words = stage_words();
+    uint32_t* pl = s_words + zfp_stage_words(kDecThreads, rate) + threadIdx.x * kZfpPlaneWords;
     const uint64_t nblocks = (uint64_t)nb.x * nb.y * nb.z;
-    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nblocks;
-         b += (uint64_t)gridDim.x * blockDim.x) {
+    for (uint64_t b0 = (uint64_t)blockIdx.x * kDecThreads; b0 < nblocks; b0 += (uint64_t)gridDim.x * kDecThreads) {
+        const uint32_t n = (uint32_t)(nblocks - b0 < (uint64_t)kDecThreads ? nblocks - b0 : (uint64_t)kDecThreads);
+        __syncthreads();
+        zfp_stage_run(words, b0, n, rate, s_words);
+        __syncthreads();
+        if (threadIdx.x >= n) continue;
+        const uint64_t b = b0 + threadIdx.x;
         if (b >= ranged) {  // beyond the reference's block count: the buffer's zero
             ranges[b] = make_float2(0.0f, 0.0f);
             continue;
         }
         float v[64];
-        zfp_decode_block<kBulkDeposit>(words, b * max_bits, max_bits, v);
+        zfp_decode_staged<kDeposit>(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, v);
         const uint32_t bx = (uint32_t)(b % nb.x), by = (uint32_t)((b / nb.x) % nb.y),
                        bz = (uint32_t)(b / ((uint64_t)nb.x * nb.y));
         const uint32_t px = min(dims.x - 4u * bx, 4u), py = min(dims.y - 4u * by, 4u),
@@ -47,38 +65,47 @@ __global__ void __launch_bounds__(kBulkThreads) k_block_ranges(const uint64_t* _
     }
 }
 
-__device__ __forceinline__ void store_block(float* __restrict__ dst, const float* v)
-{
-    float4* d4 = reinterpret_cast<float4*>(dst);
-#pragma unroll
-    for (int i = 0; i < 16; ++i) d4[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
-}
-
 // zfp_decompress_block.comp:29-39: decode ids[i] into its cache slot.
-__global__ void __launch_bounds__(128) k_decode_blocks(const uint64_t* __restrict__ words, uint32_t max_bits,
-                                                       const uint32_t* __restrict__ ids, uint32_t n,
-                                                       const int32_t* __restrict__ item_slots,
-                                                       float* __restrict__ cache)
+__global__ void __launch_bounds__(kDecThreads) k_decode_blocks(const uint64_t* __restrict__ words, uint32_t rate,
+                                                               const uint32_t* __restrict__ ids, uint32_t n,
+                                                               const int32_t* __restrict__ item_slots,
+                                                               float* __restrict__ cache)
 {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t b = ids[i];
-        const int32_t slot = item_slots[b];
+    uint32_t* s_words = stage_words();
+    uint32_t* pl = s_words + zfp_stage_words(kDecThreads, rate) + threadIdx.x * kZfpPlaneWords;
+    if (threadIdx.x < 4) s_words[kDecThreads * 2u * rate + threadIdx.x] = 0u;
+    for (uint32_t i0 = blockIdx.x * kDecThreads; i0 < n; i0 += gridDim.x * kDecThreads) {
+        const uint32_t i = i0 + threadIdx.x;
+        uint32_t b = 0;
+        int32_t slot = -1;
+        __syncthreads();
+        if (i < n) {
+            b = ids[i];
+            slot = item_slots[b];
+            if (slot >= 0) zfp_stage_block(words, b, rate, s_words);
+        }
+        __syncthreads();
         if (slot < 0) continue;  // not cached: nothing to decode into
         float v[64];
-        zfp_decode_block<1>(words, (uint64_t)b * max_bits, max_bits, v);
+        zfp_decode_staged<kDeposit>(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, v);
         store_block(cache + (uint64_t)slot * 64u, v);
     }
 }
 
-__global__ void __launch_bounds__(kBulkThreads) k_decode_volume(const uint64_t* __restrict__ words,
-                                                                uint64_t nblocks, uint32_t max_bits,
-                                                                float* __restrict__ out)
+__global__ void __launch_bounds__(kDecThreads) k_decode_volume(const uint64_t* __restrict__ words, uint64_t nblocks,
+                                                               uint32_t rate, float* __restrict__ out)
 {
-    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nblocks;
-         b += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t* s_words = stage_words();
+    uint32_t* pl = s_words + zfp_stage_words(kDecThreads, rate) + threadIdx.x * kZfpPlaneWords;
+    for (uint64_t b0 = (uint64_t)blockIdx.x * kDecThreads; b0 < nblocks; b0 += (uint64_t)gridDim.x * kDecThreads) {
+        const uint32_t n = (uint32_t)(nblocks - b0 < (uint64_t)kDecThreads ? nblocks - b0 : (uint64_t)kDecThreads);
+        __syncthreads();
+        zfp_stage_run(words, b0, n, rate, s_words);
+        __syncthreads();
+        if (threadIdx.x >= n) continue;
         float v[64];
-        zfp_decode_block<kBulkDeposit>(words, b * max_bits, max_bits, v);
-        store_block(out + b * 64u, v);
+        zfp_decode_staged<kDeposit>(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, v);
+        store_block(out + (b0 + threadIdx.x) * 64u, v);
     }
 }
 
@@ -147,7 +174,10 @@ void zfp_ranges_launch(bcmc_ctx* ctx, const uint64_t* words, const uint32_t dims
     // (compressed_marching_cubes.js:526-529).  BCMC_FLAG_FULL_RANGES ranges all.
     const uint32_t ref_count = (4u * nb.x * 4u * nb.y) / 64u * (4u * nb.z);
     const uint64_t ranged = (ctx->opts.flags & BCMC_FLAG_FULL_RANGES) ? n : (ref_count < n ? ref_count : n);
-    k_block_ranges<<<grid_all(n, kBulkThreads), kBulkThreads, 0, s>>>(words, d, nb, max_bits, ranged,
+    const uint32_t rate = max_bits / 64u;
+    const size_t smem = zfp_stage_smem(kDecThreads, rate);
+    allow_smem(k_block_ranges, smem);
+    k_block_ranges<<<grid_all(n, kDecThreads), kDecThreads, smem, s>>>(words, d, nb, rate, ranged,
                                                                       reinterpret_cast<float2*>(ranges));
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
@@ -157,7 +187,11 @@ void zfp_decode_blocks_launch(bcmc_ctx* ctx, const uint64_t* words, uint32_t max
                               uint32_t n, const int32_t* item_slots, float* cache, cudaStream_t s)
 {
     if (n == 0) return;
-    k_decode_blocks<<<grid_for(ctx, n, 128, 16), 128, 0, s>>>(words, max_bits, ids, n, item_slots, cache);
+    const uint32_t rate = max_bits / 64u;
+    const size_t smem = zfp_stage_smem(kDecThreads, rate);
+    allow_smem(k_decode_blocks, smem);
+    k_decode_blocks<<<grid_for(ctx, n, kDecThreads, 16), kDecThreads, smem, s>>>(words, rate, ids, n, item_slots,
+                                                                                 cache);
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
 }
@@ -166,7 +200,10 @@ void zfp_decode_volume_launch(bcmc_ctx* ctx, const uint64_t* words, uint64_t nbl
                               float* out, cudaStream_t s)
 {
     if (nblocks == 0) return;
-    k_decode_volume<<<grid_all(nblocks, kBulkThreads), kBulkThreads, 0, s>>>(words, nblocks, max_bits, out);
+    const uint32_t rate = max_bits / 64u;
+    const size_t smem = zfp_stage_smem(kDecThreads, rate);
+    allow_smem(k_decode_volume, smem);
+    k_decode_volume<<<grid_all(nblocks, kDecThreads), kDecThreads, smem, s>>>(words, nblocks, rate, out);
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
 }

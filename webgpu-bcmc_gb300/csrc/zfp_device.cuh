@@ -8,9 +8,10 @@
 // 2^(emax-30) (:378-382).  Bit offsets are 64-bit (the reference multiplies
 // block_index*max_bits in 32 bits, :199, which wraps past 2^32 bits).
 //
-// The GB300 decoder works on native 64-bit words: a 64-bit bit buffer instead
-// of the emulated {lo,hi} pair, and the unary run of each group test is
-// consumed with one find-first-set instead of one bit at a time.
+// The GB300 decoder stages each block's words in shared memory and reads them
+// through a 64-bit window of 32-bit funnel shifts; a group test's unary run is
+// consumed with one find-first-set instead of one bit at a time, and the bit
+// planes become coefficients through 8x8 bit transposes (see "Staged decoder").
 #pragma once
 
 #include <stdint.h>
@@ -20,152 +21,6 @@
 namespace bcmc {
 
 constexpr uint32_t kZfpMaxBitsLimit = 64u * 32u;  // rate <= 32 bits/value
-
-struct BitReader {
-    const uint64_t* __restrict__ p;  // next word to fetch
-    uint64_t buf;                    // unread bits, LSB first; bits >= n are 0
-    uint32_t n;                      // valid bits in buf
-
-    __device__ __forceinline__ void init(const uint64_t* words, uint64_t bit_offset)
-    {
-        p = words + (bit_offset >> 6);
-        const uint32_t s = (uint32_t)(bit_offset & 63u);
-        buf = __ldg(p++) >> s;
-        n = 64u - s;
-    }
-    __device__ __forceinline__ void consume(uint32_t c)  // c <= n
-    {
-        buf = c >= 64u ? 0ull : buf >> c;
-        n -= c;
-    }
-    __device__ __forceinline__ uint32_t bit()
-    {
-        if (n == 0) {
-            buf = __ldg(p++);
-            n = 64;
-        }
-        const uint32_t b = (uint32_t)buf & 1u;
-        buf >>= 1;
-        --n;
-        return b;
-    }
-    // next k (<= 64) bits of the stream, LSB first
-    __device__ __forceinline__ uint64_t bits(uint32_t k)
-    {
-        if (k == 0) return 0;
-        uint64_t v;
-        if (k <= n) {
-            v = buf;
-            consume(k);
-        } else {
-            const uint64_t w = __ldg(p++);
-            v = buf | (w << n);  // n < k <= 64, so n <= 63
-            const uint32_t used = k - n;
-            buf = used >= 64u ? 0ull : w >> used;
-            n = 64u - used;
-        }
-        return k >= 64u ? v : (v & ((1ull << k) - 1ull));
-    }
-    // Consume zero bits, at most `limit` of them; if a one comes first it is
-    // consumed too and *hit is set.  Returns the zeros consumed.
-    __device__ __forceinline__ uint32_t skip_zeros(uint32_t limit, bool* hit)
-    {
-        uint32_t z = 0;
-        *hit = false;
-        while (z < limit) {
-            if (n == 0) {
-                buf = __ldg(p++);
-                n = 64;
-            }
-            const uint32_t rem = limit - z;
-            if (buf != 0ull) {
-                const uint32_t tz = (uint32_t)__ffsll((long long)buf) - 1u;
-                if (tz < rem) {
-                    consume(tz + 1u);
-                    z += tz;
-                    *hit = true;
-                    return z;
-                }
-                consume(rem);
-                return z + rem;
-            }
-            if (n >= rem) {
-                consume(rem);
-                return z + rem;
-            }
-            z += n;
-            buf = 0;
-            n = 0;
-        }
-        return z;
-    }
-};
-
-// decode_ints (zfp_decompress.comp:265-294) into u[64] (stream order).
-__device__ __forceinline__ void zfp_decode_ints(BitReader& rd, uint32_t budget, uint32_t* u)
-{
-#pragma unroll
-    for (int i = 0; i < 64; ++i) u[i] = 0;
-    uint32_t bits = budget, n = 0;
-    for (int k = 31; k >= 0 && bits != 0; --k) {
-        const uint32_t m = n < bits ? n : bits;
-        bits -= m;
-        uint64_t x = rd.bits(m);
-        while (n < 64u && bits != 0) {
-            --bits;
-            if (!rd.bit()) break;
-            const uint32_t limit = (63u - (n < 63u ? n : 63u)) < bits ? (63u - (n < 63u ? n : 63u)) : bits;
-            bool hit;
-            const uint32_t z = rd.skip_zeros(limit, &hit);
-            bits -= z + (hit ? 1u : 0u);
-            n += z;
-            x |= 1ull << n;
-            ++n;
-        }
-        const uint32_t bitk = 1u << k;
-        while (x) {
-            const int i = __ffsll((long long)x) - 1;
-            u[i] |= bitk;
-            x &= x - 1ull;
-        }
-    }
-}
-
-// Same decode with the coefficients in registers: each plane is shifted into
-// all 64 accumulators (acc = acc*2 + bit), so the critical path is short --
-// used where a launch decodes few blocks and latency, not throughput, counts.
-__device__ __forceinline__ void zfp_decode_ints_regs(BitReader& rd, uint32_t budget, uint32_t* u)
-{
-#pragma unroll
-    for (int i = 0; i < 64; ++i) u[i] = 0;
-    uint32_t bits = budget, n = 0;
-    int k = 31;
-    for (; k >= 0 && bits != 0; --k) {
-        const uint32_t m = n < bits ? n : bits;
-        bits -= m;
-        uint64_t x = rd.bits(m);
-        while (n < 64u && bits != 0) {
-            --bits;
-            if (!rd.bit()) break;
-            const uint32_t room = 63u - (n < 63u ? n : 63u);
-            bool hit;
-            const uint32_t z = rd.skip_zeros(room < bits ? room : bits, &hit);
-            bits -= z + (hit ? 1u : 0u);
-            n += z;
-            x |= 1ull << n;
-            ++n;
-        }
-        const uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32);
-#pragma unroll
-        for (int i = 0; i < 32; ++i) u[i] = (u[i] << 1) | ((lo >> i) & 1u);
-#pragma unroll
-        for (int i = 0; i < 32; ++i) u[32 + i] = (u[32 + i] << 1) | ((hi >> i) & 1u);
-    }
-    // planes k..0 were not reached: they are zero
-    const uint32_t rest = (uint32_t)(k + 1);
-#pragma unroll
-    for (int i = 0; i < 64; ++i) u[i] = rest >= 32u ? 0u : u[i] << rest;
-}
 
 __device__ __forceinline__ int32_t zfp_uint2int(uint32_t x)
 {
@@ -223,34 +78,258 @@ __device__ __forceinline__ float zfp_inv_weight(int32_t emax)
     return ldexpf(1.0f, e);
 }
 
-// Decode one block starting at `bit_offset` into out[64] (natural order).
-// kDeposit: 0 = per-set-bit deposit into a local array, 1 = register
-// shift-in per plane (faster on GB300 for both bulk and latency-bound decodes).
-template <int kDeposit = 0>
-__device__ __forceinline__ void zfp_decode_block(const uint64_t* __restrict__ words,
-                                                 uint64_t bit_offset, uint32_t max_bits,
-                                                 float* out)
+// ---------------------------------------------------------------------------
+// Staged decoder: the block's compressed words are first copied into shared
+// memory (coalesced loads by the CTA for runs of consecutive blocks, or one
+// block per thread), then parsed there.
+//
+// The parse is one loop over the stream's group-test bits (plus the raw bits
+// of a plane when a plane starts), not a loop over planes with a loop over
+// group tests inside: the lanes of a warp then do not wait for each other at
+// every plane boundary.  A 64-bit window over the words covers any zero run
+// (at most 63 bits), so a group test is one find-first-set.  The parse writes
+// each plane's 64-bit mask to a per-thread scratch in shared memory; the
+// coefficients are then built from 8-plane chunks with 8x8 bit transposes
+// (kDeposit 0) or shifted in plane by plane (kDeposit 1).
+// ---------------------------------------------------------------------------
+
+// Bit window over 32-bit words (LSB first).  The window reads up to two words
+// past the last bit it consumes, so a staged block is followed by at least
+// three readable words.
+struct ZfpWindow {
+    const uint32_t* p;  // next word to load
+    uint32_t w0, w1, w2, sh;
+    __device__ __forceinline__ void init(const uint32_t* w)
+    {
+        w0 = w[0];
+        w1 = w[1];
+        w2 = w[2];
+        p = w + 3;
+        sh = 0;
+    }
+    __device__ __forceinline__ uint32_t lo() const { return __funnelshift_r(w0, w1, sh); }  // bits 0..31
+    __device__ __forceinline__ uint32_t hi() const { return __funnelshift_r(w1, w2, sh); }  // bits 32..63
+    __device__ __forceinline__ void skip(uint32_t c)  // c <= 64
+    {
+        const uint32_t s = sh + c;
+        sh = s & 31u;
+        const uint32_t adv = s >> 5;  // 0, 1 or 2
+        if (adv == 1u) {
+            w0 = w1;
+            w1 = w2;
+            w2 = p[0];
+            p += 1;
+        } else if (adv == 2u) {
+            w0 = w2;
+            w1 = p[0];
+            w2 = p[1];
+            p += 2;
+        }
+    }
+};
+
+__device__ __forceinline__ uint32_t zfp_ctz64(uint32_t lo, uint32_t hi)  // 64 when both are 0
 {
-    BitReader rd;
-    rd.init(words, bit_offset);
-    if (!rd.bit()) {
+    return lo ? (uint32_t)__ffs(lo) - 1u : (hi ? 31u + (uint32_t)__ffs(hi) : 64u);
+}
+
+// decode_ints' bit planes (zfp_decompress.comp:265-294) as masks: plane 31 - r
+// at pl[2r] (coefficients 0..31) and pl[2r + 1] (32..63).  Returns the number
+// of planes decoded.
+__device__ __forceinline__ uint32_t zfp_parse_planes(ZfpWindow& rd, uint32_t budget, uint32_t* pl)
+{
+    uint32_t bits = budget, n = 0, r = 0, xlo = 0, xhi = 0;
+    bool start = true;
+    while (r < 32u && bits != 0u) {
+        bool end = false;
+        if (start) {  // the raw bits of the n coefficients already significant
+            const uint32_t m = n < bits ? n : bits;
+            bits -= m;
+            const uint32_t a = rd.lo(), b = rd.hi();
+            xlo = m >= 32u ? a : (a & ((1u << m) - 1u));
+            xhi = m >= 64u ? b : (m > 32u ? (b & ((1u << (m - 32u)) - 1u)) : 0u);
+            rd.skip(m);
+            start = false;
+            end = (n == 64u || bits == 0u);
+        }
+        if (!end) {  // one group test: a 0 ends the plane, a 1 is followed by the run
+            const uint32_t a = rd.lo(), b = rd.hi();  // of zeros before the next significant one
+            --bits;
+            if (!(a & 1u)) {
+                rd.skip(1);
+                end = true;
+            } else {
+                const uint32_t limit = min(63u - n, bits);
+                const uint32_t tz = zfp_ctz64(__funnelshift_r(a, b, 1), b >> 1);
+                const uint32_t z = tz < limit ? tz : limit;
+                const uint32_t hit = tz < limit ? 1u : 0u;
+                rd.skip(1u + z + hit);
+                bits -= z + hit;
+                n += z;
+                if (n < 32u) xlo |= 1u << n;
+                else xhi |= 1u << (n - 32u);
+                ++n;
+                end = (n == 64u || bits == 0u);
+            }
+        }
+        if (end) {
+            pl[2 * r] = xlo;
+            pl[2 * r + 1] = xhi;
+            ++r;
+            start = true;
+        }
+    }
+    return r;
+}
+
+// 8x8 bit transpose of the 64-bit matrix (hi:lo), row = byte, column = bit
+// (three delta swaps)
+__device__ __forceinline__ void zfp_transpose8(uint32_t& lo, uint32_t& hi)
+{
+    uint32_t t;
+    t = (lo ^ (lo >> 7)) & 0x00AA00AAu;
+    lo ^= t ^ (t << 7);
+    t = (hi ^ (hi >> 7)) & 0x00AA00AAu;
+    hi ^= t ^ (t << 7);
+    t = (lo ^ (lo >> 14)) & 0x0000CCCCu;
+    lo ^= t ^ (t << 14);
+    t = (hi ^ (hi >> 14)) & 0x0000CCCCu;
+    hi ^= t ^ (t << 14);
+    t = (lo ^ __funnelshift_r(lo, hi, 28)) & 0xF0F0F0F0u;
+    lo ^= t;
+    hi ^= t >> 4;
+}
+
+// Coefficients (stream order) from the plane masks: each 8-plane chunk is cut
+// into eight 8x8 bit matrices (byte g of planes 8c..8c+7), transposed, and
+// each result byte is coefficient 8g + i's bits of those planes.
+__device__ __forceinline__ void zfp_planes_transposed(const uint32_t* pl, uint32_t planes, uint32_t* u)
+{
+#pragma unroll
+    for (int i = 0; i < 64; ++i) u[i] = 0;
+    for (uint32_t c = 0; c * 8u < planes; ++c) {
+        uint32_t w[16];  // planes 8c .. 8c+7: lo, hi
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint4 v = reinterpret_cast<const uint4*>(pl + 16u * c)[q];
+            w[4 * q] = v.x;
+            w[4 * q + 1] = v.y;
+            w[4 * q + 2] = v.z;
+            w[4 * q + 3] = v.w;
+        }
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+            if (8u * c + (uint32_t)r >= planes) w[2 * r] = w[2 * r + 1] = 0u;
+        const uint32_t rs = 8u * c;  // bit j of a result byte is plane 24 - 8c + j: (byte << 24) >> 8c
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+            const int h = g >> 2;
+            const uint32_t sb = (uint32_t)(g & 3);
+            const uint32_t sel = sb | ((sb + 4u) << 4);
+            // matrix byte j = byte g of plane 7 - j (lo word: planes 7..4, hi word: planes 3..0)
+            const uint32_t a = __byte_perm(w[14 + h], w[12 + h], sel);
+            const uint32_t b = __byte_perm(w[10 + h], w[8 + h], sel);
+            const uint32_t d = __byte_perm(w[6 + h], w[4 + h], sel);
+            const uint32_t e = __byte_perm(w[2 + h], w[0 + h], sel);
+            uint32_t lo = __byte_perm(a, b, 0x5410u), hi = __byte_perm(d, e, 0x5410u);
+            zfp_transpose8(lo, hi);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                u[8 * g + i] |= __byte_perm(lo, 0u, 0x0444u | ((uint32_t)i << 12)) >> rs;
+                u[8 * g + 4 + i] |= __byte_perm(hi, 0u, 0x0444u | ((uint32_t)i << 12)) >> rs;
+            }
+        }
+    }
+}
+
+// The same by shifting each plane into the 64 accumulators.
+__device__ __forceinline__ void zfp_planes_shifted(const uint32_t* pl, uint32_t planes, uint32_t* u)
+{
+#pragma unroll
+    for (int i = 0; i < 64; ++i) u[i] = 0;
+    for (uint32_t r = 0; r < planes; ++r) {
+        const uint32_t lo = pl[2 * r], hi = pl[2 * r + 1];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) u[i] = (u[i] << 1) | ((lo >> i) & 1u);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) u[32 + i] = (u[32 + i] << 1) | ((hi >> i) & 1u);
+    }
+    const uint32_t rest = 32u - planes;
+#pragma unroll
+    for (int i = 0; i < 64; ++i) u[i] = rest >= 32u ? 0u : u[i] << rest;
+}
+
+// Words of a staged block: 2 * rate 32-bit words (64 * rate bits).  `pl` is
+// the thread's plane scratch in shared memory: 64 words, 16-byte aligned.
+template <int kDeposit = 0>
+__device__ __forceinline__ void zfp_decode_staged(const uint32_t* w, uint32_t max_bits, uint32_t* pl, float* out)
+{
+    ZfpWindow rd;
+    rd.init(w);
+    const uint32_t h = rd.lo();
+    if (!(h & 1u)) {
 #pragma unroll
         for (int i = 0; i < 64; ++i) out[i] = 0.0f;
         return;
     }
-    const int32_t emax = (int32_t)((uint32_t)rd.bits(8) - 127u);
+    const int32_t emax = (int32_t)((h >> 1) & 255u) - 127;
+    rd.skip(9);
     uint32_t u[64];
-    if (kDeposit == 1) zfp_decode_ints_regs(rd, max_bits - 9u, u);
-    else zfp_decode_ints(rd, max_bits - 9u, u);
+    const uint32_t planes = zfp_parse_planes(rd, max_bits - 9u, pl);
+    if (kDeposit == 0) zfp_planes_transposed(pl, planes, u);
+    else zfp_planes_shifted(pl, planes, u);
     int32_t v[64];
     uint32_t un[64];
     BCMC_ZFP_GATHER(un, u)
 #pragma unroll
     for (int i = 0; i < 64; ++i) v[i] = zfp_uint2int(un[i]);
     zfp_inverse_transform(v);
-    const float w = zfp_inv_weight(emax);
+    const float wt = zfp_inv_weight(emax);
 #pragma unroll
-    for (int i = 0; i < 64; ++i) out[i] = __fmul_rn(w, __int2float_rn(v[i]));
+    for (int i = 0; i < 64; ++i) out[i] = __fmul_rn(wt, __int2float_rn(v[i]));
+}
+
+// Shared memory of a staged decode CTA of `threads` threads at `rate`: the
+// staged words (2 * rate per block, 4 words of padding) and 68 words of plane
+// scratch per thread (64 used; 68 keeps the threads' 16-byte rows apart).
+constexpr uint32_t kZfpPlaneWords = 68;
+__host__ __device__ __forceinline__ uint32_t zfp_stage_words(uint32_t threads, uint32_t rate)
+{
+    return threads * 2u * rate + 4u;
+}
+__host__ __device__ __forceinline__ size_t zfp_stage_smem(uint32_t threads, uint32_t rate)
+{
+    return ((size_t)zfp_stage_words(threads, rate) + (size_t)threads * kZfpPlaneWords) * 4u;
+}
+
+// Copies the words of blocks b0 .. b0+nb-1 (consecutive) to s_words with
+// coalesced 8-byte loads, and zeroes the 4 padding words.  All the CTA's
+// threads call it; the caller synchronises before reading.
+__device__ __forceinline__ void zfp_stage_run(const uint64_t* __restrict__ words, uint64_t b0, uint32_t nb,
+                                              uint32_t rate, uint32_t* s_words)
+{
+    const uint64_t* src = words + b0 * rate;
+    uint2* dst = reinterpret_cast<uint2*>(s_words);
+    const uint32_t n = nb * rate;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint64_t x = __ldg(src + i);
+        dst[i] = make_uint2((uint32_t)x, (uint32_t)(x >> 32));
+    }
+    if (threadIdx.x < 4) s_words[2u * n + threadIdx.x] = 0u;
+}
+
+// Copies the words of block b to this thread's slot of s_words (2 * rate
+// words at threadIdx.x * 2 * rate).  The 4 padding words after the last slot
+// are zeroed by thread 0; the caller synchronises before any thread reads.
+__device__ __forceinline__ void zfp_stage_block(const uint64_t* __restrict__ words, uint64_t b, uint32_t rate,
+                                                uint32_t* s_words)
+{
+    const uint64_t* src = words + b * rate;
+    uint2* dst = reinterpret_cast<uint2*>(s_words + threadIdx.x * 2u * rate);
+    for (uint32_t i = 0; i < rate; ++i) {
+        const uint64_t x = __ldg(src + i);
+        dst[i] = make_uint2((uint32_t)x, (uint32_t)(x >> 32));
+    }
 }
 
 // ---------------------------------------------------------------------------
