@@ -461,39 +461,30 @@ __global__ void __launch_bounds__(kAssignThreads) k_assign(QueryState* q, Assign
     const uint32_t n = q->num_new;
     const uint32_t size = q->new_cache_size;
     const uint32_t* __restrict__ sorted = q->sort_final == 1 ? a.sorted_b : a.sorted_c;
-    // new blocks decoded here (all of them for the standalone LRU update, those
-    // past the staging buffer on the query path) are staged in shared memory
-    extern __shared__ __align__(16) uint32_t s_words[];
-    const uint32_t rate = a.max_bits / 64u;
     const uint32_t first_decode = a.stage ? a.stage_blocks : 0u;
-    if (a.words && threadIdx.x < 4) s_words[kAssignThreads * 2u * rate + threadIdx.x] = 0u;
-    for (uint32_t i0 = blockIdx.x * kAssignThreads; i0 < n; i0 += gridDim.x * kAssignThreads) {
-        const uint32_t i = i0 + threadIdx.x;
-        uint32_t item = 0, slot = 0xffffffffu;
-        if (i < n) {
-            item = a.new_ids[i];
-            slot = sorted[i];
-            if (slot >= size) {  // cannot happen with a consistent sort; never write out of bounds
-                atomicCAS(&q->error, 0u, 50u);
-                slot = 0xffffffffu;
-            } else {
-                const int32_t prev = a.slot_item[slot];
-                if (prev != -1) a.item_slots[prev] = -1;
-                a.slot_age[slot] = 0;
-                a.slot_item[slot] = (int32_t)item;
-                a.slot_avail[slot] = 0;
-                a.item_slots[item] = (int32_t)slot;
-            }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t item = a.new_ids[i];
+        const uint32_t slot = sorted[i];
+        if (slot >= size) {  // cannot happen with a consistent sort; never write out of bounds
+            atomicCAS(&q->error, 0u, 50u);
+            continue;
         }
-        if (!a.words || i0 + kAssignThreads <= first_decode) continue;  // no decode in this group (uniform)
-        const bool dec = slot != 0xffffffffu && i >= first_decode;
-        __syncthreads();
-        if (dec) zfp_stage_block(a.words, item, rate, s_words);
-        __syncthreads();
-        if (dec) {
+        const int32_t prev = a.slot_item[slot];
+        if (prev != -1) a.item_slots[prev] = -1;
+        a.slot_age[slot] = 0;
+        a.slot_item[slot] = (int32_t)item;
+        a.slot_avail[slot] = 0;
+        a.item_slots[item] = (int32_t)slot;
+        if (a.words && i >= first_decode) {
+            // decoded here: every new block of the standalone LRU update, the ones
+            // past the staging buffer on the query path.  Rare enough on the query
+            // path that the words are read in place and the plane scratch is
+            // thread-local, which keeps this kernel free of shared memory for its
+            // assignment and copy work.
+            __align__(16) uint32_t pl[64];
             float v[64];
-            zfp_decode_staged(s_words + threadIdx.x * 2u * rate, a.max_bits,
-                              s_words + zfp_stage_words(kAssignThreads, rate) + threadIdx.x * kZfpPlaneWords, v);
+            zfp_decode_staged(reinterpret_cast<const uint32_t*>(a.words + (uint64_t)item * (a.max_bits / 64u)),
+                              a.max_bits, pl, v);
             float4* d4 = reinterpret_cast<float4*>(a.cache + (uint64_t)slot * 64u);
 #pragma unroll
             for (int k = 0; k < 16; ++k) d4[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
@@ -914,9 +905,7 @@ void slots_launch(bcmc_ctx* ctx, QueryState* q, const SlotArgs& a, uint32_t max_
 
 void assign_launch(bcmc_ctx* ctx, QueryState* q, const AssignArgs& a, uint32_t max_new, cudaStream_t s)
 {
-    const size_t smem = a.words ? zfp_stage_smem(kAssignThreads, a.max_bits / 64u) : 0;
-    allow_smem(k_assign, smem);
-    k_assign<<<pgrid(ctx, div_up(max_new, (uint32_t)kAssignThreads), 16), kAssignThreads, smem, s>>>(q, a);
+    k_assign<<<pgrid(ctx, div_up(max_new, (uint32_t)kAssignThreads), 16), kAssignThreads, 0, s>>>(q, a);
     count_launches(1);
     BCMC_CUDA(cudaGetLastError());
 }

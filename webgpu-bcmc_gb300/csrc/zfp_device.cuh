@@ -83,101 +83,108 @@ __device__ __forceinline__ float zfp_inv_weight(int32_t emax)
 // memory (coalesced loads by the CTA for runs of consecutive blocks, or one
 // block per thread), then parsed there.
 //
-// The parse is one loop over the stream's group-test bits (plus the raw bits
-// of a plane when a plane starts), not a loop over planes with a loop over
-// group tests inside: the lanes of a warp then do not wait for each other at
-// every plane boundary.  A 64-bit window over the words covers any zero run
-// (at most 63 bits), so a group test is one find-first-set.  The parse writes
-// each plane's 64-bit mask to a per-thread scratch in shared memory; the
-// coefficients are then built from 8-plane chunks with 8x8 bit transposes
-// (kDeposit 0) or shifted in plane by plane (kDeposit 1).
+// The parse reads the words through a 32-bit window (a funnel shift of two
+// words), consumes a group test's zero run with one find-first-set, and
+// writes each plane's 64-bit mask to a per-thread scratch in shared memory;
+// the coefficients are then built from 8-plane chunks with 8x8 bit transposes
+// (kDeposit 0) or shifted in plane by plane (kDeposit 1).  (A parse flattened
+// into one loop over group-test bits, so that lanes do not wait for each other
+// at plane boundaries, measured slower: 285 against 214 us for the parse of
+// the 512^3 spectral field at rate 2.)
 // ---------------------------------------------------------------------------
 
-// Bit window over 32-bit words (LSB first).  The window reads up to two words
-// past the last bit it consumes, so a staged block is followed by at least
-// three readable words.
+// Bit window over 32-bit words (LSB first): the 32 bits at the current
+// position are one funnel shift of the two words around it.  The window reads
+// one word past the last bit it consumes, so a block is followed by at least
+// one readable word (staged blocks get padding).
 struct ZfpWindow {
     const uint32_t* p;  // next word to load
-    uint32_t w0, w1, w2, sh;
+    uint32_t lo, hi, sh;
     __device__ __forceinline__ void init(const uint32_t* w)
     {
-        w0 = w[0];
-        w1 = w[1];
-        w2 = w[2];
-        p = w + 3;
+        lo = w[0];
+        hi = w[1];
+        p = w + 2;
         sh = 0;
     }
-    __device__ __forceinline__ uint32_t lo() const { return __funnelshift_r(w0, w1, sh); }  // bits 0..31
-    __device__ __forceinline__ uint32_t hi() const { return __funnelshift_r(w1, w2, sh); }  // bits 32..63
-    __device__ __forceinline__ void skip(uint32_t c)  // c <= 64
+    __device__ __forceinline__ uint32_t peek() const { return __funnelshift_r(lo, hi, sh); }
+    __device__ __forceinline__ void skip(uint32_t c)  // c <= 32
     {
-        const uint32_t s = sh + c;
-        sh = s & 31u;
-        const uint32_t adv = s >> 5;  // 0, 1 or 2
-        if (adv == 1u) {
-            w0 = w1;
-            w1 = w2;
-            w2 = p[0];
-            p += 1;
-        } else if (adv == 2u) {
-            w0 = w2;
-            w1 = p[0];
-            w2 = p[1];
-            p += 2;
+        sh += c;
+        if (sh >= 32u) {
+            sh -= 32u;
+            lo = hi;
+            hi = *p++;
         }
     }
 };
 
-__device__ __forceinline__ uint32_t zfp_ctz64(uint32_t lo, uint32_t hi)  // 64 when both are 0
-{
-    return lo ? (uint32_t)__ffs(lo) - 1u : (hi ? 31u + (uint32_t)__ffs(hi) : 64u);
-}
+__device__ __forceinline__ uint32_t zfp_mask32(uint32_t m) { return m >= 32u ? 0xffffffffu : (1u << m) - 1u; }
 
 // decode_ints' bit planes (zfp_decompress.comp:265-294) as masks: plane 31 - r
 // at pl[2r] (coefficients 0..31) and pl[2r + 1] (32..63).  Returns the number
-// of planes decoded.
+// of planes decoded.  Per plane: the raw bits of the n coefficients already
+// significant, then group tests, each a 1 followed by the run of zeros before
+// the next significant coefficient (one find-first-set in the common case) or
+// a 0 that ends the plane.
 __device__ __forceinline__ uint32_t zfp_parse_planes(ZfpWindow& rd, uint32_t budget, uint32_t* pl)
 {
-    uint32_t bits = budget, n = 0, r = 0, xlo = 0, xhi = 0;
-    bool start = true;
-    while (r < 32u && bits != 0u) {
-        bool end = false;
-        if (start) {  // the raw bits of the n coefficients already significant
-            const uint32_t m = n < bits ? n : bits;
-            bits -= m;
-            const uint32_t a = rd.lo(), b = rd.hi();
-            xlo = m >= 32u ? a : (a & ((1u << m) - 1u));
-            xhi = m >= 64u ? b : (m > 32u ? (b & ((1u << (m - 32u)) - 1u)) : 0u);
+    uint32_t bits = budget, n = 0, r = 0;
+    for (; r < 32u && bits != 0; ++r) {
+        const uint32_t m = n < bits ? n : bits;
+        bits -= m;
+        uint32_t xlo, xhi = 0;
+        if (m <= 32u) {
+            xlo = rd.peek() & zfp_mask32(m);
             rd.skip(m);
-            start = false;
-            end = (n == 64u || bits == 0u);
+        } else {
+            xlo = rd.peek();
+            rd.skip(32);
+            xhi = rd.peek() & zfp_mask32(m - 32u);
+            rd.skip(m - 32u);
         }
-        if (!end) {  // one group test: a 0 ends the plane, a 1 is followed by the run
-            const uint32_t a = rd.lo(), b = rd.hi();  // of zeros before the next significant one
+        while (n < 64u && bits != 0) {
+            const uint32_t W = rd.peek();
             --bits;
-            if (!(a & 1u)) {
+            if (!(W & 1u)) {
                 rd.skip(1);
-                end = true;
-            } else {
-                const uint32_t limit = min(63u - n, bits);
-                const uint32_t tz = zfp_ctz64(__funnelshift_r(a, b, 1), b >> 1);
-                const uint32_t z = tz < limit ? tz : limit;
-                const uint32_t hit = tz < limit ? 1u : 0u;
-                rd.skip(1u + z + hit);
-                bits -= z + hit;
-                n += z;
-                if (n < 32u) xlo |= 1u << n;
-                else xhi |= 1u << (n - 32u);
-                ++n;
-                end = (n == 64u || bits == 0u);
+                break;
             }
+            const uint32_t limit = min(63u - n, bits);
+            const uint32_t Z = W >> 1;
+            const uint32_t tz = (uint32_t)__ffs(Z) - 1u;  // 0xffffffff when Z == 0
+            uint32_t z;
+            if (Z != 0u && tz < limit) {  // the next one is within this window
+                rd.skip(tz + 2u);
+                bits -= tz + 1u;
+                z = tz;
+            } else {  // a longer run, or one that reaches the limit
+                rd.skip(1);
+                z = 0;
+                bool hit = false;
+                while (z < limit) {
+                    const uint32_t V = rd.peek();
+                    const uint32_t rem = limit - z;
+                    const uint32_t t = (uint32_t)__ffs(V) - 1u;
+                    if (V != 0u && t < rem) {
+                        rd.skip(t + 1u);
+                        z += t;
+                        hit = true;
+                        break;
+                    }
+                    const uint32_t step = rem < 32u ? rem : 32u;
+                    rd.skip(step);
+                    z += step;
+                }
+                bits -= z + (hit ? 1u : 0u);
+            }
+            n += z;
+            if (n < 32u) xlo |= 1u << n;
+            else xhi |= 1u << (n - 32u);
+            ++n;
         }
-        if (end) {
-            pl[2 * r] = xlo;
-            pl[2 * r + 1] = xhi;
-            ++r;
-            start = true;
-        }
+        pl[2 * r] = xlo;
+        pl[2 * r + 1] = xhi;
     }
     return r;
 }
@@ -259,14 +266,16 @@ __device__ __forceinline__ void zfp_planes_shifted(const uint32_t* pl, uint32_t 
     for (int i = 0; i < 64; ++i) u[i] = rest >= 32u ? 0u : u[i] << rest;
 }
 
-// Words of a staged block: 2 * rate 32-bit words (64 * rate bits).  `pl` is
-// the thread's plane scratch in shared memory: 64 words, 16-byte aligned.
+// One block from its words `w` (2 * rate 32-bit words, 64 * rate bits; staged
+// in shared memory, or in place in global memory), readable for one word past
+// the block.  `pl` is the thread's plane scratch: 64 words, 16-byte aligned
+// (in shared memory, or a thread-local array).
 template <int kDeposit = 0>
 __device__ __forceinline__ void zfp_decode_staged(const uint32_t* w, uint32_t max_bits, uint32_t* pl, float* out)
 {
     ZfpWindow rd;
     rd.init(w);
-    const uint32_t h = rd.lo();
+    const uint32_t h = rd.peek();
     if (!(h & 1u)) {
 #pragma unroll
         for (int i = 0; i < 64; ++i) out[i] = 0.0f;
