@@ -516,7 +516,9 @@ __global__ void __launch_bounds__(kDecodeNewThreads) k_decode_new(const QuerySta
     const uint32_t n = q->num_new < a.stage_blocks ? q->num_new : a.stage_blocks;
     extern __shared__ __align__(16) uint32_t s_words[];
     const uint32_t rate = a.max_bits / 64u;
-    uint32_t* pl = s_words + zfp_stage_words(kDecodeNewThreads, rate) + threadIdx.x * kZfpPlaneWords;
+    uint32_t* pl = zfp_stage_planes(s_words, kDecodeNewThreads, rate);
+    uint32_t* gt = zfp_stage_gt(s_words, kDecodeNewThreads, rate);
+    zfp_gt_fill(gt);
     if (threadIdx.x < 4) s_words[kDecodeNewThreads * 2u * rate + threadIdx.x] = 0u;
     for (uint32_t i0 = blockIdx.x * kDecodeNewThreads; i0 < n; i0 += gridDim.x * kDecodeNewThreads) {
         const uint32_t i = i0 + threadIdx.x;
@@ -525,7 +527,7 @@ __global__ void __launch_bounds__(kDecodeNewThreads) k_decode_new(const QuerySta
         __syncthreads();
         if (i >= n) continue;
         float v[64];
-        zfp_decode_staged(s_words + threadIdx.x * 2u * rate, a.max_bits, pl, v);
+        zfp_decode_staged(s_words + threadIdx.x * 2u * rate, a.max_bits, pl, v, gt);
         float4* d4 = reinterpret_cast<float4*>(a.stage + (uint64_t)i * 64u);
 #pragma unroll
         for (int k = 0; k < 16; ++k) d4[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);

@@ -29,7 +29,9 @@ __global__ void __launch_bounds__(kDecThreads) k_block_ranges(const uint64_t* __
                                                               float2* __restrict__ ranges)
 {
     uint32_t* s_words = stage_words();
-    uint32_t* pl = s_words + zfp_stage_words(kDecThreads, rate) + threadIdx.x * kZfpPlaneWords;
+    uint32_t* pl = zfp_stage_planes(s_words, kDecThreads, rate);
+    uint32_t* gt = zfp_stage_gt(s_words, kDecThreads, rate);
+    zfp_gt_fill(gt);
     const uint64_t nblocks = (uint64_t)nb.x * nb.y * nb.z;
     for (uint64_t b0 = (uint64_t)blockIdx.x * kDecThreads; b0 < nblocks; b0 += (uint64_t)gridDim.x * kDecThreads) {
         const uint32_t n = (uint32_t)(nblocks - b0 < (uint64_t)kDecThreads ? nblocks - b0 : (uint64_t)kDecThreads);
@@ -43,7 +45,7 @@ __global__ void __launch_bounds__(kDecThreads) k_block_ranges(const uint64_t* __
             continue;
         }
         float v[64];
-        zfp_decode_staged<kDeposit>(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, v);
+        zfp_decode_staged<kDeposit>(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, v, gt);
         const uint32_t bx = (uint32_t)(b % nb.x), by = (uint32_t)((b / nb.x) % nb.y),
                        bz = (uint32_t)(b / ((uint64_t)nb.x * nb.y));
         const uint32_t px = min(dims.x - 4u * bx, 4u), py = min(dims.y - 4u * by, 4u),
@@ -72,7 +74,9 @@ __global__ void __launch_bounds__(kDecThreads) k_decode_blocks(const uint64_t* _
                                                                float* __restrict__ cache)
 {
     uint32_t* s_words = stage_words();
-    uint32_t* pl = s_words + zfp_stage_words(kDecThreads, rate) + threadIdx.x * kZfpPlaneWords;
+    uint32_t* pl = zfp_stage_planes(s_words, kDecThreads, rate);
+    uint32_t* gt = zfp_stage_gt(s_words, kDecThreads, rate);
+    zfp_gt_fill(gt);
     if (threadIdx.x < 4) s_words[kDecThreads * 2u * rate + threadIdx.x] = 0u;
     for (uint32_t i0 = blockIdx.x * kDecThreads; i0 < n; i0 += gridDim.x * kDecThreads) {
         const uint32_t i = i0 + threadIdx.x;
@@ -87,7 +91,7 @@ __global__ void __launch_bounds__(kDecThreads) k_decode_blocks(const uint64_t* _
         __syncthreads();
         if (slot < 0) continue;  // not cached: nothing to decode into
         float v[64];
-        zfp_decode_staged<kDeposit>(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, v);
+        zfp_decode_staged<kDeposit>(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, v, gt);
         store_block(cache + (uint64_t)slot * 64u, v);
     }
 }
@@ -96,7 +100,9 @@ __global__ void __launch_bounds__(kDecThreads) k_decode_volume(const uint64_t* _
                                                                uint32_t rate, float* __restrict__ out)
 {
     uint32_t* s_words = stage_words();
-    uint32_t* pl = s_words + zfp_stage_words(kDecThreads, rate) + threadIdx.x * kZfpPlaneWords;
+    uint32_t* pl = zfp_stage_planes(s_words, kDecThreads, rate);
+    uint32_t* gt = zfp_stage_gt(s_words, kDecThreads, rate);
+    zfp_gt_fill(gt);
     for (uint64_t b0 = (uint64_t)blockIdx.x * kDecThreads; b0 < nblocks; b0 += (uint64_t)gridDim.x * kDecThreads) {
         const uint32_t n = (uint32_t)(nblocks - b0 < (uint64_t)kDecThreads ? nblocks - b0 : (uint64_t)kDecThreads);
         __syncthreads();
@@ -104,7 +110,7 @@ __global__ void __launch_bounds__(kDecThreads) k_decode_volume(const uint64_t* _
         __syncthreads();
         if (threadIdx.x >= n) continue;
         float v[64];
-        zfp_decode_staged<kDeposit>(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, v);
+        zfp_decode_staged<kDeposit>(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, v, gt);
         store_block(out + (b0 + threadIdx.x) * 64u, v);
     }
 }

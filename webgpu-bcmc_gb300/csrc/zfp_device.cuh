@@ -9,9 +9,10 @@
 // block_index*max_bits in 32 bits, :199, which wraps past 2^32 bits).
 //
 // The GB300 decoder stages each block's words in shared memory and reads them
-// through a 64-bit window of 32-bit funnel shifts; a group test's unary run is
-// consumed with one find-first-set instead of one bit at a time, and the bit
-// planes become coefficients through 8x8 bit transposes (see "Staged decoder").
+// through a 64-bit window of 32-bit funnel shifts; the group tests are taken 8
+// bits per step through a 512-entry state table in shared memory (or a unary
+// run per find-first-set where there is no shared memory), and the bit planes
+// become coefficients through 8x8 bit transposes (see "Staged decoder").
 #pragma once
 
 #include <stdint.h>
@@ -84,13 +85,16 @@ __device__ __forceinline__ float zfp_inv_weight(int32_t emax)
 // block per thread), then parsed there.
 //
 // The parse reads the words through a 32-bit window (a funnel shift of two
-// words), consumes a group test's zero run with one find-first-set, and
-// writes each plane's 64-bit mask to a per-thread scratch in shared memory;
-// the coefficients are then built from 8-plane chunks with 8x8 bit transposes
-// (kDeposit 0) or shifted in plane by plane (kDeposit 1).  (A parse flattened
-// into one loop over group-test bits, so that lanes do not wait for each other
-// at plane boundaries, measured slower: 285 against 214 us for the parse of
-// the 512^3 spectral field at rate 2.)
+// words), takes each plane's raw bits at once and its group tests 8 bits per
+// table step (zfp_parse_planes_gt) or one unary run per find-first-set
+// (zfp_parse_planes), and writes each plane's 64-bit mask to a per-thread
+// scratch; the coefficients are then built from 8-plane chunks with 8x8 bit
+// transposes (kDeposit 0) or shifted in plane by plane (kDeposit 1).  On the
+// 512^3 spectral field at rate 2 (8 planes, 11 group tests and 72 group-test
+// bits per block on average) the table parse takes 268 us against 303 us for
+// the find-first-set parse; a parse flattened into one loop of uniform steps
+// (raw chunk, table step or single bit, branch-free or not), so that lanes do
+// not wait for each other at plane boundaries, measured 296-299 us.
 // ---------------------------------------------------------------------------
 
 // Bit window over 32-bit words (LSB first): the 32 bits at the current
@@ -189,6 +193,118 @@ __device__ __forceinline__ uint32_t zfp_parse_planes(ZfpWindow& rd, uint32_t bud
     return r;
 }
 
+// Group-test step table.  A plane's group tests read as a two-state machine
+// over its bits: in state 0 the next bit is a group test (0 ends the plane,
+// 1 enters state 1); in state 1 each bit is the next coefficient's (1: it
+// becomes significant, back to state 0).  Entry (state << 8 | b) is what the
+// 8 bits b do from `state`, as long as neither the bit budget nor coefficient
+// 63 (whose run decode_ints does not read) falls among them:
+//   bits 0-3  bits consumed (1..8; fewer when the plane ends)
+//   bits 4-7  coefficients passed (0..8)
+//   bits 8-15 which of those became significant (bit i: the i-th passed)
+//   bit 16    the plane ended
+//   bit 17    the state after the last bit consumed
+__host__ __device__ __forceinline__ uint32_t zfp_gt_entry(uint32_t idx)
+{
+    uint32_t s = (idx >> 8) & 1u, dn = 0, mask = 0, c = 0, end = 0;
+    while (c < 8u) {
+        const uint32_t b = (idx >> c) & 1u;
+        ++c;
+        if (s == 0u) {
+            if (!b) {
+                end = 1;
+                break;
+            }
+            s = 1;
+        } else {
+            if (b) {
+                mask |= 1u << dn;
+                s = 0;
+            }
+            ++dn;
+        }
+    }
+    return c | (dn << 4) | (mask << 8) | (end << 16) | (s << 17);
+}
+
+constexpr uint32_t kZfpGtWords = 512;
+
+// The CTA's threads fill the table; the caller synchronises before use.
+__device__ __forceinline__ void zfp_gt_fill(uint32_t* gt)
+{
+    for (uint32_t i = threadIdx.x; i < kZfpGtWords; i += blockDim.x) gt[i] = zfp_gt_entry(i);
+}
+
+// zfp_parse_planes with the group tests taken 8 bits per table step: a step
+// is taken when it consumes no more bits than the budget has left and passes
+// coefficients below 63 only (each of its reads then happens in decode_ints
+// too); otherwise, and for the plane's remaining bits, one bit at a time with
+// decode_ints' limits (at coefficient 63 or an empty budget a run ends
+// without a read and marks the coefficient).
+__device__ __forceinline__ uint32_t zfp_parse_planes_gt(ZfpWindow& rd, uint32_t budget, uint32_t* pl,
+                                                        const uint32_t* gt)
+{
+    uint32_t bits = budget, n = 0, r = 0;
+    for (; r < 32u && bits != 0; ++r) {
+        const uint32_t m = n < bits ? n : bits;
+        bits -= m;
+        uint64_t x;
+        if (m <= 32u) {
+            x = rd.peek() & zfp_mask32(m);
+            rd.skip(m);
+        } else {
+            x = rd.peek();
+            rd.skip(32);
+            x |= (uint64_t)(rd.peek() & zfp_mask32(m - 32u)) << 32;
+            rd.skip(m - 32u);
+        }
+        uint32_t s = 0;
+        bool ended = false;
+        for (;;) {
+            const uint32_t e = gt[(s << 8) | (rd.peek() & 255u)];
+            const uint32_t c = e & 15u, dn = (e >> 4) & 15u;
+            if (c > bits || n + dn > 63u) break;
+            rd.skip(c);
+            bits -= c;
+            x |= (uint64_t)((e >> 8) & 255u) << n;
+            n += dn;
+            s = (e >> 17) & 1u;
+            if (e & 0x10000u) {
+                ended = true;
+                break;
+            }
+        }
+        if (!ended) {
+            for (;;) {
+                if (s == 0u) {
+                    if (n >= 64u || bits == 0u) break;
+                    --bits;
+                    const uint32_t b = rd.peek() & 1u;
+                    rd.skip(1);
+                    if (!b) break;
+                    s = 1;
+                } else {
+                    if (n < 63u && bits != 0u) {
+                        --bits;
+                        const uint32_t b = rd.peek() & 1u;
+                        rd.skip(1);
+                        if (!b) {
+                            ++n;
+                            continue;
+                        }
+                    }
+                    x |= 1ull << n;
+                    ++n;
+                    s = 0;
+                }
+            }
+        }
+        pl[2 * r] = (uint32_t)x;
+        pl[2 * r + 1] = (uint32_t)(x >> 32);
+    }
+    return r;
+}
+
 // 8x8 bit transpose of the 64-bit matrix (hi:lo), row = byte, column = bit
 // (three delta swaps)
 __device__ __forceinline__ void zfp_transpose8(uint32_t& lo, uint32_t& hi)
@@ -269,9 +385,12 @@ __device__ __forceinline__ void zfp_planes_shifted(const uint32_t* pl, uint32_t 
 // One block from its words `w` (2 * rate 32-bit words, 64 * rate bits; staged
 // in shared memory, or in place in global memory), readable for one word past
 // the block.  `pl` is the thread's plane scratch: 64 words, 16-byte aligned
-// (in shared memory, or a thread-local array).
+// (in shared memory, or a thread-local array).  `gt`: the CTA's group-test
+// step table (zfp_gt_fill), or null for the find-first-set parse (decoders
+// without shared memory).
 template <int kDeposit = 0>
-__device__ __forceinline__ void zfp_decode_staged(const uint32_t* w, uint32_t max_bits, uint32_t* pl, float* out)
+__device__ __forceinline__ void zfp_decode_staged(const uint32_t* w, uint32_t max_bits, uint32_t* pl, float* out,
+                                                  const uint32_t* gt = nullptr)
 {
     ZfpWindow rd;
     rd.init(w);
@@ -284,7 +403,7 @@ __device__ __forceinline__ void zfp_decode_staged(const uint32_t* w, uint32_t ma
     const int32_t emax = (int32_t)((h >> 1) & 255u) - 127;
     rd.skip(9);
     uint32_t u[64];
-    const uint32_t planes = zfp_parse_planes(rd, max_bits - 9u, pl);
+    const uint32_t planes = gt ? zfp_parse_planes_gt(rd, max_bits - 9u, pl, gt) : zfp_parse_planes(rd, max_bits - 9u, pl);
     if (kDeposit == 0) zfp_planes_transposed(pl, planes, u);
     else zfp_planes_shifted(pl, planes, u);
     int32_t v[64];
@@ -299,8 +418,9 @@ __device__ __forceinline__ void zfp_decode_staged(const uint32_t* w, uint32_t ma
 }
 
 // Shared memory of a staged decode CTA of `threads` threads at `rate`: the
-// staged words (2 * rate per block, 4 words of padding) and 68 words of plane
-// scratch per thread (64 used; 68 keeps the threads' 16-byte rows apart).
+// staged words (2 * rate per block, 4 words of padding), 68 words of plane
+// scratch per thread (64 used; 68 keeps the threads' 16-byte rows apart) and
+// the group-test step table.
 constexpr uint32_t kZfpPlaneWords = 68;
 __host__ __device__ __forceinline__ uint32_t zfp_stage_words(uint32_t threads, uint32_t rate)
 {
@@ -308,7 +428,15 @@ __host__ __device__ __forceinline__ uint32_t zfp_stage_words(uint32_t threads, u
 }
 __host__ __device__ __forceinline__ size_t zfp_stage_smem(uint32_t threads, uint32_t rate)
 {
-    return ((size_t)zfp_stage_words(threads, rate) + (size_t)threads * kZfpPlaneWords) * 4u;
+    return ((size_t)zfp_stage_words(threads, rate) + (size_t)threads * kZfpPlaneWords + kZfpGtWords) * 4u;
+}
+__device__ __forceinline__ uint32_t* zfp_stage_planes(uint32_t* s_words, uint32_t threads, uint32_t rate)
+{
+    return s_words + zfp_stage_words(threads, rate) + threadIdx.x * kZfpPlaneWords;
+}
+__device__ __forceinline__ uint32_t* zfp_stage_gt(uint32_t* s_words, uint32_t threads, uint32_t rate)
+{
+    return s_words + zfp_stage_words(threads, rate) + threads * kZfpPlaneWords;
 }
 
 // Copies the words of blocks b0 .. b0+nb-1 (consecutive) to s_words with
