@@ -69,7 +69,10 @@ struct QueryState {
     // test hook (bcmc_debug_drop_tile): 0, or t + 1 when tile t of the active
     // test and of the primitive scans must publish no look-back status
     uint32_t debug_drop_tile;
-    uint32_t pad[7];
+    // k_mc's grid barrier (CTAs arrived) and its emit tiles' counter
+    uint32_t mc_arrived;
+    uint32_t tiles_emit;
+    uint32_t pad[5];
 };
 
 // The test hook's check: this tile publishes nothing, so the tiles after it

@@ -73,7 +73,7 @@ struct McArgs {
     BlockGrid grid;
     uint32_t* with_verts;
     uint32_t* vert_offsets;
-    uint32_t* block_counts;  // vertices of each active block (count pass -> emit pass)
+    uint32_t* block_counts;  // vertices of each active block (count pass -> list entries)
     uint2* verts;
     uint64_t* status_v;
     uint64_t* status_b;

@@ -23,10 +23,12 @@
 //   k_assign       lru_cache_update.comp, and the staged blocks copied into
 //                  their slots
 //   k_query_end    the query state the host reads, into its pinned copy
-//   k_mc           marching cubes count + scan + emit in one pass
+//   k_mc           marching cubes count + scan + emit in one cooperative launch
 //                  (compute_block_has_vertices.comp,
 //                  compute_block_voxel_num_verts.comp,
 //                  compute_block_vertices.comp)
+#include <algorithm>
+
 #include "active_test.cuh"
 #include "bcmc_pipeline.h"
 #include "mc_common.cuh"
@@ -51,7 +53,7 @@ __global__ void k_query_begin(QueryState* q, float iso, int mc_only, uint32_t ca
         q->epoch += 1;
         q->capacity = capacity;
         q->vert_capacity = vert_capacity;
-        q->tiles_mc = 0;
+        q->tiles_mc = q->mc_arrived = q->tiles_emit = 0;
         q->error = 0;
         q->vert_overflow = 0;
         q->num_with_verts = 0;
@@ -540,29 +542,32 @@ __global__ void __launch_bounds__(kDecodeNewThreads) k_decode_new(const QuerySta
 constexpr int kMcBlocks = 16;
 constexpr int kMcThreads = 256;
 constexpr int kMcCells = 64 * kMcBlocks;  // 4 consecutive cells per thread
+constexpr int kMcPerSm = 6;               // resident CTAs per SM (the grid: one launch, all resident)
 
-// Marching cubes over the active blocks.  Each CTA owns one contiguous range of
-// active blocks and makes two passes over it:
+// Marching cubes over the active blocks, one cooperative launch (every CTA
+// resident).  Each CTA owns one contiguous range of active blocks:
 //   count pass: per 16-block tile, one parallel round of loads fetches the
 //     active flags and cache slots of every block's 7 +x/+y/+z neighbours and
 //     its own slot, a second round fills each block's 5^3 grid in shared
 //     memory (16 B loads of 4 voxels per thread, ghost voxels alongside); a
 //     thread tests its 4 corner rows once and derives the cases and vertex
-//     counts of its 4 cells; block totals are kept for the emit pass;
+//     counts of its 4 cells; block totals are kept;
 //   one warp-cooperative decoupled look-back per CTA turns the CTA totals into
 //     its global vertex offset and its offset in the blocks-with-vertices list;
-//   emit pass: tiles of the next 16 blocks that have vertices (blocks without
-//     are skipped by a warp ballot over the counts), reloaded (from L2); a CTA
-//     scan gives each cell's offset and the vertices are spread over the CTA
-//     -- thread k takes vertex k of the tile, finds its cell by binary search,
-//     its edge in the precomputed corner-pair table -- so lanes stay converged
-//     and stores are contiguous.
-// A CTA walks back once per launch, not once per tile.  Output order = the
-// reference's: active-block order, cell order, table order.
+//   the range's entries of that list and their vertex offsets (a CTA scan over
+//     the block totals), then a grid barrier;
+//   emit: tiles of 16 consecutive list entries, claimed from a counter by
+//     whichever CTA is free -- vertex counts differ between ranges by up to
+//     7x, so the emit work is balanced across the grid, not per range --
+//     reloaded (from L2); a CTA scan gives each cell's offset and the vertices
+//     are spread over the CTA -- thread k takes vertex k of the tile, finds its
+//     cell by binary search, its edge in the precomputed corner-pair table --
+//     so lanes stay converged and stores are contiguous.
+// Output order = the reference's: active-block order, cell order, table order.
 // kHost: the vertices go to page-locked host memory (a.host_verts); its own
 // instantiation keeps the device path's emit loop free of the alignment shift.
 template <bool kHost>
-__global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
+__global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McArgs a)
 {
     __shared__ float s_vol[kMcBlocks][128];
     __shared__ uint8_t s_rm[kMcBlocks][32];  // corner-row masks of each block (count_cells)
@@ -572,11 +577,10 @@ __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
     __shared__ __align__(16) uint8_t s_case[kMcCells];
     __shared__ uint32_t s_off[kMcCells + 1];
     __shared__ uint32_t s_id[kMcBlocks];
-    __shared__ uint32_t s_idx[kMcBlocks];
     __shared__ uint32_t s_slot[kMcBlocks][8];
     __shared__ uint32_t s_act[kMcBlocks];
     __shared__ uint32_t s_warp[kMcThreads / 32 + 1];
-    __shared__ uint32_t s_n, s_pv, s_pb, s_cta_v, s_cta_b, s_rank, s_cursor;
+    __shared__ uint32_t s_stop, s_with, s_pv, s_pb, s_cta_v, s_cta_b, s_rank;
     __shared__ uint32_t s_gdesc[64];  // ghost_desc of each ghost voxel
     __shared__ uint8_t s_nb_off[8];
 
@@ -598,7 +602,6 @@ __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
     if (t < 16) reinterpret_cast<uint4*>(s_cnt)[t] = reinterpret_cast<const uint4*>(c_tri.count)[t];
     if (t == 0) {
         s_cta_v = s_cta_b = 0;
-        s_cursor = start;
     }
     if (t < 61) s_gdesc[t] = ghost_desc(c_ghost[t]);
     if (t < 32) {
@@ -614,7 +617,6 @@ __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
     }
     if (t < 7) s_nb_off[t] = c_nb_off[t];
     const uint32_t j = t >> 4, u = t & 15u, ry = u & 3u, rz = u >> 2;
-    const uint32_t lane = t & 31u;
 
     auto load_tile = [&]() -> uint32_t {
         if (t < kMcBlocks * 8) {
@@ -720,97 +722,9 @@ __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
         return sum;
     };
 
-    // ---- count pass
-    for (uint32_t base = start; base < end; base += kMcBlocks) {
-        __syncthreads();
-        if (t < kMcBlocks) {
-            const uint32_t idx = base + t;
-            s_id[t] = idx < end ? __ldg(a.active_ids + idx) : 0xffffffffu;
-        }
-        __syncthreads();
-        const uint32_t dims = load_tile();
-        uint32_t nv[4], cs4;
-        uint32_t bsum = count_cells(dims, nv, cs4);
-#pragma unroll
-        for (int o = 8; o; o >>= 1) bsum += __shfl_xor_sync(0xffffffffu, bsum, o);
-        if (u == 0 && s_id[j] != 0xffffffffu) {
-            a.block_counts[base + j] = bsum;
-            if (bsum) {
-                atomicAdd(&s_cta_v, bsum);
-                atomicAdd(&s_cta_b, 1u);
-            }
-        }
-    }
-    __syncthreads();
-    if (t < 64) {
-        if (t < 32) {
-            const uint32_t p = warp_lookback(a.status_v, rank, s_cta_v, epoch, &q->error, 40u);
-            if (t == 0) {
-                s_pv = p;
-                if (rank == G - 1) q->num_verts = p + s_cta_v;
-            }
-        } else {
-            const uint32_t p = warp_lookback(a.status_b, rank, s_cta_b, epoch, &q->error, 41u);
-            if (t == 32) {
-                s_pb = p;
-                if (rank == G - 1) q->num_with_verts = p + s_cta_b;
-            }
-        }
-    }
-    __syncthreads();
-    uint32_t pv = s_pv, pb = s_pb;
-    if ((uint64_t)pv + s_cta_v > cap) {
-        if (t == 0) atomicOr(&q->vert_overflow, 1u);
-        return;
-    }
-    // ---- emit pass over tiles of the next 16 blocks that have vertices
-    for (;;) {
-        __syncthreads();
-        if (t < 32) {
-            uint32_t cur = s_cursor, filled = 0;
-            while (filled < kMcBlocks && cur < end) {
-                const uint32_t i = cur + lane;
-                const uint32_t c = i < end ? a.block_counts[i] : 0u;
-                const uint32_t m = __ballot_sync(0xffffffffu, c != 0u);
-                const uint32_t nz = __popc(m), take = min(nz, kMcBlocks - filled);
-                const uint32_t r = __popc(m & ((1u << lane) - 1u));
-                if (c != 0u && r < take) s_idx[filled + r] = i;
-                if (take < nz) {
-                    uint32_t mm = m;
-                    for (uint32_t k = 0; k < take; ++k) mm &= mm - 1u;
-                    cur += (uint32_t)__ffs(mm) - 1u;
-                } else {
-                    cur += 32u;
-                }
-                filled += take;
-            }
-            __syncwarp();
-            if (lane < kMcBlocks) s_id[lane] = lane < filled ? __ldg(a.active_ids + s_idx[lane]) : 0xffffffffu;
-            if (lane == 0) {
-                s_n = filled;
-                s_cursor = min(cur, end);
-            }
-        }
-        __syncthreads();
-        const uint32_t n_sel = s_n;
-        if (n_sel == 0) break;
-        const uint32_t dims = load_tile();
-        uint32_t nv[4], cs4;
-        const uint32_t mysum = count_cells(dims, nv, cs4);
-        uint32_t tile_v;
-        uint32_t run = cta_exclusive_scan<kMcThreads>(mysum, s_warp, &tile_v);
-        *reinterpret_cast<uint32_t*>(&s_case[4u * t]) = cs4;
-#pragma unroll
-        for (uint32_t x = 0; x < 4; ++x) {
-            s_off[4u * t + x] = run;
-            run += nv[x];
-        }
-        if (t == 0) s_off[kMcCells] = tile_v;
-        __syncthreads();
-        if (t < n_sel) {
-            a.with_verts[pb + t] = s_idx[t];
-            a.vert_offsets[pb + t] = pv + s_off[64 * t];
-        }
+    // the vertices of the tile in shared memory (s_vol, s_case, s_off, s_id),
+    // vertex k of the tile to out[k], out = a.verts + pv
+    auto emit_tile = [&](const uint32_t pv, const uint32_t tile_v) {
         uint2* out = a.verts + pv;
         const auto emit = [&](const uint32_t k) {
             uint32_t cell = 0;
@@ -859,8 +773,110 @@ __global__ void __launch_bounds__(kMcThreads, 6) k_mc(QueryState* q, McArgs a)
         } else {
             for (uint32_t k = t; k < tile_v; k += kMcThreads) emit(k);
         }
-        pv += tile_v;
-        pb += n_sel;
+    };
+
+    // ---- count pass
+    for (uint32_t base = start; base < end; base += kMcBlocks) {
+        __syncthreads();
+        if (t < kMcBlocks) {
+            const uint32_t idx = base + t;
+            s_id[t] = idx < end ? __ldg(a.active_ids + idx) : 0xffffffffu;
+        }
+        __syncthreads();
+        const uint32_t dims = load_tile();
+        uint32_t nv[4], cs4;
+        uint32_t bsum = count_cells(dims, nv, cs4);
+#pragma unroll
+        for (int o = 8; o; o >>= 1) bsum += __shfl_xor_sync(0xffffffffu, bsum, o);
+        if (u == 0 && s_id[j] != 0xffffffffu) {
+            a.block_counts[base + j] = bsum;
+            if (bsum) {
+                atomicAdd(&s_cta_v, bsum);
+                atomicAdd(&s_cta_b, 1u);
+            }
+        }
+    }
+    __syncthreads();
+    if (t < 64) {
+        if (t < 32) {
+            const uint32_t p = warp_lookback(a.status_v, rank, s_cta_v, epoch, &q->error, 40u);
+            if (t == 0) {
+                s_pv = p;
+                if (rank == G - 1) q->num_verts = p + s_cta_v;
+            }
+        } else {
+            const uint32_t p = warp_lookback(a.status_b, rank, s_cta_b, epoch, &q->error, 41u);
+            if (t == 32) {
+                s_pb = p;
+                if (rank == G - 1) q->num_with_verts = p + s_cta_b;
+            }
+        }
+    }
+    __syncthreads();
+    uint32_t pv = s_pv, pb = s_pb;
+    const bool fits = (uint64_t)pv + s_cta_v <= cap;
+    if (!fits && t == 0) atomicOr(&q->vert_overflow, 1u);
+    // the range's blocks with vertices: their list entries and vertex offsets
+    if (fits)
+        for (uint32_t b0 = start; b0 < end; b0 += kMcThreads) {
+            const uint32_t i = b0 + t;
+            const uint32_t c = i < end ? a.block_counts[i] : 0u;  // <= 64 cells x 15 vertices
+            uint32_t tot;
+            const uint32_t ex = cta_exclusive_scan<kMcThreads>(c | (c ? 1u << 18 : 0u), s_warp, &tot);
+            if (c) {
+                const uint32_t r = pb + (ex >> 18);
+                a.with_verts[r] = i;
+                a.vert_offsets[r] = pv + (ex & 0x3ffffu);
+            }
+            pv += tot & 0x3ffffu;
+            pb += tot >> 18;
+        }
+    // grid barrier (the launch is cooperative: every CTA is resident)
+    __syncthreads();
+    if (t == 0) {
+        __threadfence();
+        atomicAdd(&q->mc_arrived, 1u);
+        uint32_t spins = 0;
+        while (*reinterpret_cast<volatile uint32_t*>(&q->mc_arrived) < G) {
+            if (++spins > kSpinLimit) {
+                atomicCAS(&q->error, 0u, 42u);
+                break;
+            }
+            if (spins > 8) __nanosleep(100);
+        }
+        __threadfence();
+        s_stop = *reinterpret_cast<volatile uint32_t*>(&q->error) | *reinterpret_cast<volatile uint32_t*>(&q->vert_overflow);
+        s_with = *reinterpret_cast<volatile uint32_t*>(&q->num_with_verts);
+    }
+    __syncthreads();
+    if (s_stop) return;
+    // emit: tiles of 16 consecutive list entries, claimed by whichever CTA is free
+    const uint32_t W = s_with, ntiles = div_up(W, kMcBlocks);
+    for (;;) {
+        __syncthreads();
+        if (t == 0) s_rank = atomicAdd(&q->tiles_emit, 1u);
+        __syncthreads();
+        const uint32_t tile = s_rank;
+        if (tile >= ntiles) break;
+        const uint32_t first = tile * kMcBlocks;
+        if (t < kMcBlocks)
+            s_id[t] = first + t < W ? __ldg(a.active_ids + __ldcg(a.with_verts + first + t)) : 0xffffffffu;
+        if (t == 0) s_pv = __ldcg(a.vert_offsets + first);
+        __syncthreads();
+        const uint32_t dims = load_tile();
+        uint32_t nv[4], cs4;
+        const uint32_t mysum = count_cells(dims, nv, cs4);
+        uint32_t tile_v;
+        uint32_t run = cta_exclusive_scan<kMcThreads>(mysum, s_warp, &tile_v);
+        *reinterpret_cast<uint32_t*>(&s_case[4u * t]) = cs4;
+#pragma unroll
+        for (uint32_t x = 0; x < 4; ++x) {
+            s_off[4u * t + x] = run;
+            run += nv[x];
+        }
+        if (t == 0) s_off[kMcCells] = tile_v;
+        __syncthreads();
+        emit_tile(s_pv, tile_v);
     }
 }
 
@@ -924,20 +940,43 @@ void decode_new_launch(bcmc_ctx* ctx, const QueryState* q, const DecodeArgs& a, 
     BCMC_CUDA(cudaGetLastError());
 }
 
+// CTAs of k_mc resident per SM: the bound of its cooperative grid
+static uint32_t mc_per_sm()
+{
+    static const uint32_t n = [] {
+        int a = 0, b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_mc<false>, kMcThreads, 0) != cudaSuccess) a = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_mc<true>, kMcThreads, 0) != cudaSuccess) b = 1;
+        const int m = std::min(std::min(a, b), kMcPerSm);
+        return (uint32_t)(m > 0 ? m : 1);
+    }();
+    return n;
+}
+
 void mc_launch(bcmc_ctx* ctx, QueryState* q, const McArgs& a, uint32_t max_active, cudaStream_t s)
 {
-    if (a.host_verts) k_mc<true><<<mc_grid(ctx, max_active), kMcThreads, 0, s>>>(q, a);
-    else k_mc<false><<<mc_grid(ctx, max_active), kMcThreads, 0, s>>>(q, a);
+    // cooperative: the kernel's grid barrier needs every CTA resident
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(mc_grid(ctx, max_active));
+    cfg.blockDim = dim3(kMcThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeCooperative;
+    attr.val.cooperative = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    if (a.host_verts) BCMC_CUDA(cudaLaunchKernelEx(&cfg, k_mc<true>, q, a));
+    else BCMC_CUDA(cudaLaunchKernelEx(&cfg, k_mc<false>, q, a));
     count_launches(1);
-    BCMC_CUDA(cudaGetLastError());
 }
 
 uint32_t active_tiles(uint32_t total) { return div_up(total, kActiveTile); }
 uint32_t slot_tiles(uint32_t slots) { return div_up(slots, kSlotTile); }
-// one CTA per range of active blocks: 5 resident CTAs per SM at most
+// one CTA per range of active blocks, every CTA resident
 uint32_t mc_grid(bcmc_ctx* ctx, uint32_t max_active)
 {
-    const uint32_t r = (uint32_t)ctx->num_sms * 6u, tiles = div_up(max_active ? max_active : 1, kMcBlocks);
+    const uint32_t r = (uint32_t)ctx->num_sms * mc_per_sm(), tiles = div_up(max_active ? max_active : 1, kMcBlocks);
     return tiles < r ? tiles : r;
 }
 
