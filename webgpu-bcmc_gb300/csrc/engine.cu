@@ -14,7 +14,9 @@
 //              slot from the pool's free list
 //   k_bdecode  ZFP decode of every claimed block into its slot
 //   k_bmc      marching cubes over all entries: the per-query kernel's
-//              range-per-CTA count pass, one look-back per CTA, emit pass;
+//              range-per-CTA count pass, one look-back per CTA, the list of
+//              entries with vertices, a grid barrier (cooperative launch) and
+//              emit tiles claimed by whichever CTA is free;
 //              per-block isovalue, volume and neighbour flags come from the
 //              entry's query; every query's vertices come out contiguous and
 //              in the plain path's order
@@ -79,7 +81,8 @@ struct EngState {
     // device-side
     uint32_t epoch, tiles_active, tiles_mc, num_entries;
     uint32_t num_decode, pool_exhausted, entry_overflow, vert_overflow;
-    uint32_t error, pad0;
+    uint32_t error, mc_arrived;  // mc_arrived: k_bmc's grid barrier
+    uint32_t tiles_emit, with_verts;  // k_bmc's emit tiles claimed, entries with vertices
     unsigned long long num_verts;  // this sequence's vertices (64-bit, from the per-query totals)
 };
 
@@ -106,6 +109,8 @@ struct BatchArgs {
     uint32_t* ent_id;
     uint32_t* ent_q;
     uint32_t* block_counts;
+    uint32_t* wv_list;  // entries with vertices, in entry order (k_bmc)
+    uint32_t* wv_off;   // their vertex offsets (32-bit, from vert_base)
     uint32_t* q_nactive;
     uint32_t* q_nverts;
     uint32_t* dec_vol;
@@ -114,6 +119,7 @@ struct BatchArgs {
     uint2* verts;
     uint64_t* status_a;  // look-back over active tiles
     uint64_t* status_v;  // look-back over MC CTAs (vertices)
+    uint64_t* status_b;  // look-back over MC CTAs (entries with vertices)
 };
 
 // ---------------------------------------------------------------------------
@@ -165,7 +171,7 @@ __global__ void k_bbegin(EngState* st, uint32_t* q_nverts, uint32_t* q_nactive, 
 {
     if (threadIdx.x == 0) {
         st->epoch += 1;
-        st->tiles_active = st->tiles_mc = 0;
+        st->tiles_active = st->tiles_mc = st->mc_arrived = st->tiles_emit = st->with_verts = 0;
         st->num_entries = st->num_decode = 0;
         st->pool_exhausted = st->entry_overflow = st->vert_overflow = 0;
         st->error = 0;
@@ -375,11 +381,10 @@ __global__ void __launch_bounds__(16 * kBmcBlocks, kBmcThreadsPerSm / (16 * kBmc
     __shared__ uint32_t s_id[kBmcBlocks];
     __shared__ uint32_t s_qi[kBmcBlocks];
     __shared__ float s_iso[kBmcBlocks];
-    __shared__ uint32_t s_idx[kBmcBlocks];
     __shared__ uint32_t s_slot[kBmcBlocks][8];
     __shared__ uint32_t s_act[kBmcBlocks];
     __shared__ uint32_t s_warp[kBmcThreads / 32 + 1];
-    __shared__ uint32_t s_n, s_pv, s_cta_v, s_rank, s_cursor;
+    __shared__ uint32_t s_stop, s_with, s_pv, s_pb, s_cta_v, s_cta_b, s_rank;
     __shared__ uint32_t s_gdesc[64];  // ghost_desc of each ghost voxel
     __shared__ uint8_t s_nb_off[8];
 
@@ -399,10 +404,7 @@ __global__ void __launch_bounds__(16 * kBmcBlocks, kBmcThreadsPerSm / (16 * kBmc
     for (uint32_t i = t; i < 256u; i += kBmcThreads)
         reinterpret_cast<uint4*>(&s_te[0][0])[i] = reinterpret_cast<const uint4*>(&c_tri.corners[0][0])[i];
     if (t < 16) reinterpret_cast<uint4*>(s_cnt)[t] = reinterpret_cast<const uint4*>(c_tri.count)[t];
-    if (t == 0) {
-        s_cta_v = 0;
-        s_cursor = start;
-    }
+    if (t == 0) s_cta_v = s_cta_b = 0;
     if (t < 61) s_gdesc[t] = ghost_desc(c_ghost[t]);
     if (t < 32) {
         uint32_t w = 0, ws = 0;
@@ -417,7 +419,6 @@ __global__ void __launch_bounds__(16 * kBmcBlocks, kBmcThreadsPerSm / (16 * kBmc
     }
     if (t < 7) s_nb_off[t] = c_nb_off[t];
     const uint32_t j = t >> 4, u = t & 15u, ry = u & 3u, rz = u >> 2;
-    const uint32_t lane = t & 31u;
 
     auto load_tile = [&]() -> uint32_t {
         if (t < kBmcBlocks * 8) {
@@ -552,63 +553,86 @@ __global__ void __launch_bounds__(16 * kBmcBlocks, kBmcThreadsPerSm / (16 * kBmc
             a.block_counts[base + j] = bsum;
             if (bsum) {
                 atomicAdd(&s_cta_v, bsum);
+                atomicAdd(&s_cta_b, 1u);
                 atomicAdd(a.q_nverts + s_qi[j], bsum);
             }
         }
     }
     __syncthreads();
-    if (t < 32) {
-        const uint32_t p = warp_lookback(a.status_v, rank, s_cta_v, epoch, &st->error, 61u);
-        if (t == 0) s_pv = p;
+    if (t < 64) {
+        if (t < 32) {
+            const uint32_t p = warp_lookback(a.status_v, rank, s_cta_v, epoch, &st->error, 61u);
+            if (t == 0) s_pv = p;
+        } else {
+            const uint32_t p = warp_lookback(a.status_b, rank, s_cta_b, epoch, &st->error, 64u);
+            if (t == 32) {
+                s_pb = p;
+                if (rank == G - 1) st->with_verts = p + s_cta_b;
+            }
+        }
     }
     __syncthreads();
     // 32-bit prefix: a sequence over 2^32 vertices wraps here; k_bfinish
     // detects it from the 64-bit per-query totals and the host splits
-    uint64_t pv = vbase + s_pv;
-    if (pv + s_cta_v > cap) {
-        if (t == 0) atomicOr(&st->vert_overflow, 1u);
-        return;
+    uint32_t pv = s_pv, pb = s_pb;
+    const bool fits = vbase + pv + s_cta_v <= cap;
+    if (!fits && t == 0) atomicOr(&st->vert_overflow, 1u);
+    // the range's entries with vertices: list positions and vertex offsets
+    if (fits)
+        for (uint32_t b0 = start; b0 < end; b0 += kBmcThreads) {
+            const uint32_t i = b0 + t;
+            const uint32_t c = i < end ? a.block_counts[i] : 0u;  // <= 64 cells x 15 vertices
+            uint32_t tot;
+            const uint32_t ex = cta_exclusive_scan<kBmcThreads>(c | (c ? 1u << 18 : 0u), s_warp, &tot);
+            if (c) {
+                const uint32_t r = pb + (ex >> 18);
+                a.wv_list[r] = i;
+                a.wv_off[r] = pv + (ex & 0x3ffffu);
+            }
+            pv += tot & 0x3ffffu;
+            pb += tot >> 18;
+        }
+    // grid barrier (the launch is cooperative: every CTA is resident)
+    __syncthreads();
+    if (t == 0) {
+        __threadfence();
+        atomicAdd(&st->mc_arrived, 1u);
+        uint32_t spins = 0;
+        while (*reinterpret_cast<volatile uint32_t*>(&st->mc_arrived) < G) {
+            if (++spins > kSpinLimit) {
+                atomicCAS(&st->error, 0u, 65u);
+                break;
+            }
+            if (spins > 8) __nanosleep(100);
+        }
+        __threadfence();
+        s_stop = *reinterpret_cast<volatile uint32_t*>(&st->error) | *reinterpret_cast<volatile uint32_t*>(&st->vert_overflow);
+        s_with = *reinterpret_cast<volatile uint32_t*>(&st->with_verts);
     }
-    // ---- emit pass over tiles of the next 16 blocks that have vertices
+    __syncthreads();
+    if (s_stop) return;
+    // emit: tiles of kBmcBlocks consecutive list entries, claimed by whichever CTA is free
+    const uint32_t W = s_with, ntiles = div_up(W, (uint32_t)kBmcBlocks);
     for (;;) {
         __syncthreads();
-        if (t < 32) {
-            uint32_t cur = s_cursor, filled = 0;
-            while (filled < kBmcBlocks && cur < end) {
-                const uint32_t i = cur + lane;
-                const uint32_t c = i < end ? a.block_counts[i] : 0u;
-                const uint32_t m = __ballot_sync(0xffffffffu, c != 0u);
-                const uint32_t nz = __popc(m), take = min(nz, kBmcBlocks - filled);
-                const uint32_t r = __popc(m & ((1u << lane) - 1u));
-                if (c != 0u && r < take) s_idx[filled + r] = i;
-                if (take < nz) {
-                    uint32_t mm = m;
-                    for (uint32_t k = 0; k < take; ++k) mm &= mm - 1u;
-                    cur += (uint32_t)__ffs(mm) - 1u;
-                } else {
-                    cur += 32u;
-                }
-                filled += take;
-            }
-            __syncwarp();
-            if (lane < kBmcBlocks) {
-                uint32_t id = 0xffffffffu, qi = 0;
-                if (lane < filled) {
-                    id = __ldg(a.ent_id + s_idx[lane]);
-                    qi = __ldg(a.ent_q + s_idx[lane]);
-                }
-                s_id[lane] = id;
-                s_qi[lane] = qi;
-                s_iso[lane] = __ldg(&a.queries[qi].iso);
-            }
-            if (lane == 0) {
-                s_n = filled;
-                s_cursor = min(cur, end);
-            }
-        }
+        if (t == 0) s_rank = atomicAdd(&st->tiles_emit, 1u);
         __syncthreads();
-        const uint32_t n_sel = s_n;
-        if (n_sel == 0) break;
+        const uint32_t tile = s_rank;
+        if (tile >= ntiles) break;
+        const uint32_t first = tile * kBmcBlocks;
+        if (t < kBmcBlocks) {
+            uint32_t id = 0xffffffffu, qi = 0;
+            if (first + t < W) {
+                const uint32_t e = __ldcg(a.wv_list + first + t);
+                id = __ldg(a.ent_id + e);
+                qi = __ldg(a.ent_q + e);
+            }
+            s_id[t] = id;
+            s_qi[t] = qi;
+            s_iso[t] = __ldg(&a.queries[qi].iso);
+        }
+        if (t == 0) s_pv = __ldcg(a.wv_off + first);
+        __syncthreads();
         const uint32_t dims = load_tile();
         uint32_t nv[4], cs4;
         const uint32_t mysum = count_cells(dims, nv, cs4);
@@ -622,7 +646,7 @@ __global__ void __launch_bounds__(16 * kBmcBlocks, kBmcThreadsPerSm / (16 * kBmc
         }
         if (t == 0) s_off[kBmcCells] = tile_v;
         __syncthreads();
-        uint2* out = a.verts + pv;
+        uint2* out = a.verts + vbase + s_pv;
         for (uint32_t k = t; k < tile_v; k += kBmcThreads) {
             uint32_t cell = 0;
 #pragma unroll
@@ -660,7 +684,6 @@ __global__ void __launch_bounds__(16 * kBmcBlocks, kBmcThreadsPerSm / (16 * kBmc
             }
             out[k] = make_uint2((qx << 20) | (qy << 10) | qz, s_id[jb]);
         }
-        pv += tile_v;
     }
 }
 
@@ -784,7 +807,7 @@ struct EngLane {
     uint32_t *q_nactive = nullptr, *q_nverts = nullptr;
     uint32_t* bitmap = nullptr;
     uint64_t bitmap_words = 0;
-    uint32_t *ent_id = nullptr, *ent_q = nullptr, *block_counts = nullptr;
+    uint32_t *ent_id = nullptr, *ent_q = nullptr, *block_counts = nullptr, *wv_list = nullptr, *wv_off = nullptr;
     uint32_t entry_cap = 0;
     uint2* verts = nullptr;
     uint64_t vert_cap = 0, vert_used = 0;
@@ -846,9 +869,22 @@ struct bcmc_engine {
 namespace {
 
 int eng_grid_mc_max(bcmc_engine* e) { return e->ctx->num_sms * kBmcMaxPerSm; }  // sizes the status words
+// k_bmc<kB> CTAs resident per SM: the bound of its cooperative grid
+template <int kB>
+int bmc_resident()
+{
+    static const int n = [] {
+        int r = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_bmc<kB>, 16 * kB, 0) != cudaSuccess || r < 1) r = 1;
+        return r;
+    }();
+    return n;
+}
 int eng_grid_mc(bcmc_engine* e)
 {
-    const int per_sm = std::min(e->cfg.mc_per_sm, kBmcPerSm) * 16 / e->cfg.mc_blocks;
+    const int kb = e->cfg.mc_blocks;
+    const int resident = kb == 8 ? bmc_resident<8>() : (kb == 32 ? bmc_resident<32>() : bmc_resident<16>());
+    const int per_sm = std::min(std::min(e->cfg.mc_per_sm, kBmcPerSm) * 16 / kb, resident);
     return e->ctx->num_sms * std::max(per_sm, 1);
 }
 int eng_grid_act(bcmc_engine* e) { return e->ctx->num_sms * e->cfg.act_per_sm; }
@@ -879,6 +915,8 @@ BatchArgs eng_args(bcmc_engine* e)
     a.ent_id = e->L->ent_id;
     a.ent_q = e->L->ent_q;
     a.block_counts = e->L->block_counts;
+    a.wv_list = e->L->wv_list;
+    a.wv_off = e->L->wv_off;
     a.q_nactive = e->L->q_nactive;
     a.q_nverts = e->L->q_nverts;
     a.dec_vol = e->dec_vol;
@@ -887,20 +925,22 @@ BatchArgs eng_args(bcmc_engine* e)
     a.verts = e->L->verts;
     a.status_a = e->L->status;
     a.status_v = e->L->status + e->L->status_a_words;
+    a.status_b = a.status_v + eng_grid_mc_max(e) + 1;
     return a;
 }
 
 void eng_ensure_status(bcmc_engine* e, uint64_t active_tiles)
 {
     const uint64_t need_a = std::max<uint64_t>(active_tiles + 1, 1024);
-    const uint64_t need = need_a + (uint64_t)eng_grid_mc_max(e) + 1;
+    const uint64_t mc_words = 2 * ((uint64_t)eng_grid_mc_max(e) + 1);  // status_v, status_b
+    const uint64_t need = need_a + mc_words;
     if (need_a <= e->L->status_a_words && need <= e->L->status_words) return;
     BCMC_CUDA(cudaStreamSynchronize(e->stream));
-    const uint64_t words = std::max<uint64_t>(need_a * 2, 4096) + eng_grid_mc_max(e) + 1;
+    const uint64_t words = std::max<uint64_t>(need_a * 2, 4096) + mc_words;
     eng_realloc(e, e->L->status, e->L->status_words, words);
     BCMC_CUDA(cudaMemsetAsync(e->L->status, 0, words * 8, e->stream));
     e->L->status_words = words;
-    e->L->status_a_words = words - eng_grid_mc_max(e) - 1;
+    e->L->status_a_words = words - mc_words;
     ++e->L->generation;
 }
 
@@ -974,6 +1014,8 @@ void eng_ensure_batch(bcmc_engine* e, uint64_t bitmap_words, uint32_t entries)
         eng_realloc(e, e->L->ent_id, e->L->entry_cap, n);
         eng_realloc(e, e->L->ent_q, e->L->entry_cap, n);
         eng_realloc(e, e->L->block_counts, e->L->entry_cap, n);
+        eng_realloc(e, e->L->wv_list, e->L->entry_cap, n);
+        eng_realloc(e, e->L->wv_off, e->L->entry_cap, n);
         e->L->entry_cap = n;
         ++e->L->generation;
     }
@@ -1045,6 +1087,8 @@ void eng_lane_free(bcmc_engine* e, EngLane& l)
     dev_free(ctx, l.ent_id, (size_t)l.entry_cap * 4);
     dev_free(ctx, l.ent_q, (size_t)l.entry_cap * 4);
     dev_free(ctx, l.block_counts, (size_t)l.entry_cap * 4);
+    dev_free(ctx, l.wv_list, (size_t)l.entry_cap * 4);
+    dev_free(ctx, l.wv_off, (size_t)l.entry_cap * 4);
     dev_free(ctx, l.verts, l.vert_cap * sizeof(uint2));
     dev_free(ctx, l.status, l.status_words * 8);
     if (l.h_queries) cudaFreeHost(l.h_queries);
@@ -1090,9 +1134,20 @@ void eng_enqueue_front(bcmc_engine* e, uint32_t bucket, cudaStream_t s)
 void eng_enqueue_back(bcmc_engine* e, uint32_t bucket, cudaStream_t s)
 {
     const BatchArgs a = eng_args(e);
-    if (e->cfg.mc_blocks == 8) k_bmc<8><<<eng_grid_mc(e), 16 * 8, 0, s>>>(a);
-    else if (e->cfg.mc_blocks == 32) k_bmc<32><<<eng_grid_mc(e), 16 * 32, 0, s>>>(a);
-    else k_bmc<16><<<eng_grid_mc(e), 16 * 16, 0, s>>>(a);
+    // cooperative: k_bmc's grid barrier needs every CTA resident
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(eng_grid_mc(e));
+    cfg.blockDim = dim3(16 * e->cfg.mc_blocks);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeCooperative;
+    attr.val.cooperative = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    if (e->cfg.mc_blocks == 8) BCMC_CUDA(cudaLaunchKernelEx(&cfg, k_bmc<8>, a));
+    else if (e->cfg.mc_blocks == 32) BCMC_CUDA(cudaLaunchKernelEx(&cfg, k_bmc<32>, a));
+    else BCMC_CUDA(cudaLaunchKernelEx(&cfg, k_bmc<16>, a));
     k_bfinish<<<1, kFinThreads, 0, s>>>(a);
     count_launches(2);
     BCMC_CUDA(cudaGetLastError());
