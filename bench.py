@@ -12,7 +12,9 @@ Lines printed (one JSON line on rank 0):
           library's stream (L2 flushed with a 512 MB write between steps);
           computeSurface is called without a perf tracker, as by default
   e2e     the same through the C ABI with every query's vertices delivered
-          into pinned host memory (bcmc_compute_surface_host)
+          into pinned host memory (bcmc_compute_surfaces_host: the sweep in
+          one call, each query's vertices copied out while the next computes;
+          per query with bcmc_compute_surface_host alongside)
   roofline  the dominant kernel's algorithmic bytes / its CUDA-event time,
           from a second timed pass with a perf tracker (its stage events
           slow each query down, so the headline pass runs without them)
@@ -694,8 +696,10 @@ def run_gb300(args):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
     L = bcmc._lib.load()
 
-    def step(perf=None, copy_out=None, lat=None, to_host=None):
+    def step(perf=None, copy_out=None, lat=None, to_host=None, seq_host=None):
         mc.lruCache.reset()
+        if seq_host is not None:  # the whole sweep in one call, transfers overlapping the next query
+            return sum(mc.computeSurfacesToHost(isos, seq_host))
         n_tot = 0
         for iso in isos:
             t_q = time.perf_counter()
@@ -751,10 +755,14 @@ def run_gb300(args):
     value = world * len(isos) / (ms / 1000.0)
 
     # e2e: every query's vertices in pinned host memory, through the C ABI:
-    # bcmc_compute_surface_host (the kernels store the vertices into the host
-    # buffer), and for comparison bcmc_compute_surface + bcmc_copy_vertices
+    # bcmc_compute_surfaces_host (the sweep in one call: each query's vertices
+    # are copied out while the next query computes); for comparison
+    # bcmc_compute_surface_host per query (the kernels store the vertices into
+    # the host buffer) and bcmc_compute_surface + bcmc_copy_vertices
     vmax = 1 << 24
     pinned = torch.empty((vmax, 2), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    sweep_verts = step()
+    pinned_seq = torch.empty((sweep_verts + 1024, 2), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
 
     def e2e_pass(**kw):
         times, d2h = [], 0
@@ -769,7 +777,8 @@ def run_gb300(args):
             d2h = n_tot * 8
         return world * len(isos) / max_over_ranks(float(np.mean(times)), "cuda"), d2h
 
-    e2e_value, d2h = e2e_pass(to_host=pinned)
+    e2e_value, d2h = e2e_pass(seq_host=pinned_seq)
+    e2e_query_value, _ = e2e_pass(to_host=pinned)
     e2e_copy_value, _ = e2e_pass(copy_out=pinned)
 
     # roofline of the dominant stage (CUDA-event stage times of the stage pass)
@@ -814,8 +823,11 @@ def run_gb300(args):
     if rank == 0:
         e2e = {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": 4 * len(isos),
                "d2h_bytes_per_step": d2h,
-               "what": "bcmc_compute_surface_host per query: vertices stored into pinned host memory "
-                       "by the kernels (host wall time per step)",
+               "what": "bcmc_compute_surfaces_host, the 16 isovalues in one call: each query's vertices "
+                       "copied into pinned host memory while the next query computes (host wall time per step)",
+               "per_query": {"value": e2e_query_value,
+                             "what": "bcmc_compute_surface_host per query: vertices stored into pinned host "
+                                     "memory by the kernels"},
                "compute_then_copy": {"value": e2e_copy_value,
                                      "what": "bcmc_compute_surface + bcmc_copy_vertices per query"}}
         roofline = {"bound": "hbm", "kernel": kernel_of[dominant], "achieved": achieved, "peak": peak,

@@ -135,6 +135,21 @@ bcmc_status bcmc_compute_surface(bcmc_vol* vol, float isovalue, bcmc_perf* perf,
 bcmc_status bcmc_compute_surface_host(bcmc_vol* vol, float isovalue, void* host_vertices, uint64_t capacity,
                                       uint32_t* num_vertices);
 
+/* n queries run in order on the volume (the cache state advances exactly as
+ * n bcmc_compute_surface calls would), their vertices delivered back to back
+ * into one page-locked, 8-byte aligned host buffer of `capacity` vertices:
+ * query i's num_vertices[i] vertices start at vertex sum(num_vertices[0..i-1]).
+ * Each query computes into one of two device vertex buffers while the
+ * previous query's vertices are copied out of the other, so a sweep runs at
+ * the rate of the slower of computation and transfer.  Returns once every
+ * transfer has completed.  When query i does not fit in what is left of the
+ * buffer: BCMC_E_LIMIT, num_vertices[i] = its count, later queries are not run
+ * (their counts are 0) and the cache state has advanced through query i.
+ * Afterwards bcmc_vertices gives query n-1's vertices on the device.
+ * No counterpart in the reference, whose vertices stay in a GPU buffer. */
+bcmc_status bcmc_compute_surfaces_host(bcmc_vol* vol, const float* isovalues, uint32_t n, void* host_vertices,
+                                       uint64_t capacity, uint32_t* num_vertices);
+
 /* The vertex buffer (this.vertexBuffer, :781-784): numVertices entries of
  * 8 bytes, {uint32 packed 10:10:10 position within the block, uint32 block id}
  * (compute_block_vertices.comp:164).  The pointer stays valid until the next

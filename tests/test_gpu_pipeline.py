@@ -143,3 +143,54 @@ def test_surface_straight_to_host(ctx, oracle):
     with pytest.raises(bcmc.BcmcError):
         b.computeSurfaceToHost(0.5, np.zeros((n, 2), np.uint32))  # pageable
     assert b.computeSurface(0.5) == n and np.array_equal(b.copyVertices(), a.copyVertices())
+
+
+def test_surface_sequence_to_host(ctx, oracle):
+    """computeSurfacesToHost: the same vertices, counts and cache state as one
+    computeSurface per isovalue, the queries back to back in one buffer, with
+    queries that grow the vertex buffers mid-sequence; a buffer that runs out
+    of room stops the sequence at that query (its count reported, the cache
+    advanced through it); the device buffer afterwards holds the last query."""
+    import torch
+
+    dims = (64, 64, 64)
+    f = D.blobs(dims, 2)
+    w = oracle.zfp_encode(f, 8)
+    stream = w.view(np.uint8)[: 4096 * 64].copy()
+    isos = [0.9, 0.5, 0.3, 5.0, 0.2, 0.5, 0.7, 0.25, 0.6]
+
+    def fresh():
+        m = bcmc.CompressedMarchingCubes(bcmc.Context(ctx.device, initial_cache_fraction=0.2))
+        m.setCompressedVolume(stream, 8, dims)
+        return m
+
+    a, b = fresh(), fresh()
+    want, counts = [], []
+    for iso in isos:
+        counts.append(a.computeSurface(iso))
+        want.append(a.copyVertices().copy())
+    pinned = torch.empty((sum(counts) + 7, 2), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    got = b.computeSurfacesToHost(isos, pinned)
+    assert got == counts
+    off = 0
+    for n, v in zip(counts, want):
+        assert np.array_equal(pinned[off:off + n], v)
+        off += n
+    assert a.stats() == b.stats()
+    assert np.array_equal(a.lruCache.state()["item_slots"], b.lruCache.state()["item_slots"])
+    assert np.array_equal(b.copyVertices(), want[-1])
+    # the next plain query on either buffer
+    assert b.computeSurface(0.45) == a.computeSurface(0.45)
+    assert np.array_equal(b.copyVertices(), a.copyVertices())
+    # too small: stops at the first query that does not fit
+    c, d = fresh(), fresh()
+    room = counts[0] + counts[1] + counts[2] // 2
+    with pytest.raises(bcmc.BcmcError):
+        c.computeSurfacesToHost(isos, pinned[:room])
+    for iso in isos[:3]:
+        d.computeSurface(iso)
+    assert c.stats() == d.stats()
+    assert np.array_equal(c.lruCache.state()["item_slots"], d.lruCache.state()["item_slots"])
+    with pytest.raises(bcmc.BcmcError):
+        c.computeSurfacesToHost(isos, np.zeros((16, 2), np.uint32))  # pageable
+    assert c.computeSurfacesToHost([], pinned) == []

@@ -289,6 +289,21 @@ class CompressedMarchingCubes:
                                                     out.nbytes // 8, C.byref(n)), self.ctx.handle)
         return int(n.value)
 
+    def computeSurfacesToHost(self, isovalues, out: np.ndarray) -> list:
+        """computeSurface for each isovalue in order, the vertices of all the
+        queries back to back in `out` (a page-locked array of shape
+        (capacity, 2) uint32); query i+1 computes while query i's vertices are
+        copied out.  Returns the vertex count of each query; raises BcmcError
+        (BCMC_E_LIMIT) when `out` runs out of room."""
+        if out.dtype.itemsize * out.size < 8 or out.ctypes.data % 8:
+            raise ValueError("out must be an 8-byte aligned array of packed vertices")
+        isos = np.ascontiguousarray(np.asarray(isovalues, dtype=np.float32))
+        counts = (C.c_uint32 * max(len(isos), 1))()
+        check(_lib.load().bcmc_compute_surfaces_host(self._vol, isos.ctypes.data_as(C.POINTER(C.c_float)),
+                                                     len(isos), out.ctypes.data_as(C.c_void_p), out.nbytes // 8,
+                                                     counts), self.ctx.handle)
+        return [int(counts[i]) for i in range(len(isos))]
+
     def stats(self) -> dict:
         s = _lib.bcmc_stats()
         check(_lib.load().bcmc_stats_get(self._vol, C.byref(s)), self.ctx.handle)

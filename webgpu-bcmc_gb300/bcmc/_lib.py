@@ -122,6 +122,7 @@ SIGNATURES = {
     "bcmc_volume_destroy": (None, [P]),
     "bcmc_compute_surface": (C.c_int, [P, C.c_float, C.POINTER(bcmc_perf), U32P]),
     "bcmc_compute_surface_host": (C.c_int, [P, C.c_float, P, U64, C.POINTER(U32)]),
+    "bcmc_compute_surfaces_host": (C.c_int, [P, C.POINTER(C.c_float), U32, P, U64, C.POINTER(U32)]),
     "bcmc_vertices": (C.c_int, [P, C.POINTER(P), C.POINTER(U64)]),
     "bcmc_copy_vertices": (C.c_int, [P, P, U64]),
     "bcmc_stats_get": (C.c_int, [P, C.POINTER(bcmc_stats)]),

@@ -7,6 +7,7 @@
 // cache size follows the reference's rule on the device) and of the vertex
 // buffer, each followed by a re-run of the affected launches.
 #include <algorithm>
+#include <utility>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -351,6 +352,9 @@ static void lru_read_state(bcmc_lru* c, cudaStream_t s)
 // ---------------------------------------------------------------------------
 // volume
 // ---------------------------------------------------------------------------
+// device vertex buffers a query sequence into host memory cycles through
+constexpr int kVertRing = 4;
+
 struct bcmc_vol {
     bcmc_ctx* ctx = nullptr;
     uint32_t dims[3]{}, nb[3]{}, total = 0, rate = 0, max_bits = 0;
@@ -367,6 +371,15 @@ struct bcmc_vol {
     uint2* verts = nullptr;
     uint32_t vert_capacity = 0;
     uint32_t verts_storage = 0;  // the reference's numVerticesStorage
+    // a ring of device vertex buffers for query sequences into host memory
+    // (bcmc_compute_surfaces_host): a query computes into one while the
+    // vertices of the queries before it are copied out of the others.
+    // `verts` is ring[cur]; the other entries hold the rest of the ring.
+    uint2* ring[kVertRing]{};
+    uint32_t ring_cap[kVertRing]{};
+    int cur = 0;
+    cudaStream_t copy = nullptr;
+    cudaEvent_t copy_ev[kVertRing]{};
     bcmc_lru* lru = nullptr;
     bcmc_stats stats{};
     cudaEvent_t ev[5]{};
@@ -374,9 +387,10 @@ struct bcmc_vol {
     // copied back to pinned memory; re-captured when a buffer is regrown
     QueryInputs* h_in = nullptr;  // pinned
     // [0]: without the stage-timing events, [1]: with them (a perf tracker),
-    // [2]: vertices written straight into a page-locked host buffer
-    cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
-    uint64_t graph_key[3][4]{};
+    // [2]: vertices written straight into a page-locked host buffer, [2 + r]:
+    // as [0] while ring buffer r (r >= 1) is the current vertex buffer
+    cudaGraphExec_t graph[2 + kVertRing]{};
+    uint64_t graph_key[2 + kVertRing][4]{};
     bool last_on_host = false;  // the last query's vertices went to host memory only
     uint64_t graph_kernels = 0;
     // the new blocks' decode runs on a branch of the query graph, beside the
@@ -402,7 +416,10 @@ static void vol_free(bcmc_vol* v)
     dev_free(ctx, v->with_verts, (size_t)v->total * 4);
     dev_free(ctx, v->vert_offsets, (size_t)v->total * 4);
     dev_free(ctx, v->block_counts, (size_t)v->total * 4);
+    if (v->copy) cudaStreamSynchronize(v->copy);
     dev_free(ctx, v->verts, (size_t)v->vert_capacity * 8);
+    for (int r = 0; r < kVertRing; ++r)
+        if (r != v->cur) dev_free(ctx, v->ring[r], (size_t)v->ring_cap[r] * 8);
     dev_free(ctx, v->stage, (size_t)v->stage_blocks * 256u);
     lru_delete(v->lru);
     for (auto& e : v->ev)
@@ -410,6 +427,9 @@ static void vol_free(bcmc_vol* v)
     if (v->fork_ev) cudaEventDestroy(v->fork_ev);
     if (v->join_ev) cudaEventDestroy(v->join_ev);
     if (v->side) cudaStreamDestroy(v->side);
+    for (auto& e : v->copy_ev)
+        if (e) cudaEventDestroy(e);
+    if (v->copy) cudaStreamDestroy(v->copy);
     for (auto& g : v->graph)
         if (g) cudaGraphExecDestroy(g);
     if (v->h_in) cudaFreeHost(v->h_in);
@@ -425,6 +445,7 @@ static void vol_grow_verts(bcmc_vol* v, uint32_t needed)
     if (st < needed) st = needed;
     if (st > 0xffffffffull) st = 0xffffffffull;
     BCMC_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (v->copy) BCMC_CUDA(cudaStreamSynchronize(v->copy));  // a transfer may still read it
     dev_free(ctx, v->verts, (size_t)v->vert_capacity * 8);
     v->verts = nullptr;
     v->vert_capacity = 0;
@@ -636,14 +657,17 @@ static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_s
 // Captures the query into a CUDA graph if the buffers it refers to changed.
 // mode 0/1: the volume's vertex buffer without/with stage events; mode 2: the
 // vertices go to `out` (the device address of a page-locked host buffer).
+static int graph_slot(const bcmc_vol* v, int mode) { return mode == 0 && v->cur != 0 ? 2 + v->cur : mode; }
+
 static void vol_ensure_graph(bcmc_vol* v, int mode, uint2* out = nullptr)
 {
     bcmc_lru* c = v->lru;
     if (mode != 2) out = v->verts;
     const uint64_t key[4] = {c->capacity, mode == 2 ? 0u : v->vert_capacity, (uint64_t)(uintptr_t)out,
                              (uint64_t)(uintptr_t)c->cache};
-    cudaGraphExec_t& graph = v->graph[mode];
-    if (graph && std::memcmp(key, v->graph_key[mode], sizeof(key)) == 0) return;
+    const int slot = graph_slot(v, mode);
+    cudaGraphExec_t& graph = v->graph[slot];
+    if (graph && std::memcmp(key, v->graph_key[slot], sizeof(key)) == 0) return;
     if (graph) {
         cudaGraphExecDestroy(graph);
         graph = nullptr;
@@ -666,7 +690,7 @@ static void vol_ensure_graph(bcmc_vol* v, int mode, uint2* out = nullptr)
     // captured launches did not run: count them per replay instead
     v->graph_kernels = g_kernel_launches.load() - before;
     g_kernel_launches.fetch_sub(v->graph_kernels);
-    std::memcpy(v->graph_key[mode], key, sizeof(key));
+    std::memcpy(v->graph_key[slot], key, sizeof(key));
 }
 
 // One query: into the volume's vertex buffer (host_out null), or straight
@@ -687,7 +711,7 @@ static bcmc_status vol_query(bcmc_vol* v, float iso, bcmc_perf* perf, uint32_t* 
             vol_ensure_graph(v, mode, host_out);
             lru_epoch_tick(c, s);
             *v->h_in = QueryInputs{iso, c->capacity, out_cap, 0u, ctx->debug_drop_tile};
-            BCMC_CUDA(cudaGraphLaunch(v->graph[mode], s));
+            BCMC_CUDA(cudaGraphLaunch(v->graph[graph_slot(v, mode)], s));
             count_launches(v->graph_kernels);
             BCMC_CUDA(cudaStreamSynchronize(s));
             if (c->h_q->error) {
@@ -785,6 +809,81 @@ bcmc_status bcmc_compute_surface_host(bcmc_vol* v, float iso, void* host_vertice
         return fail(v->ctx, BCMC_E_ARG, "the host buffer must be page-locked (cudaMallocHost or cudaHostRegister)");
     }
     return vol_query(v, iso, nullptr, num_vertices, static_cast<uint2*>(at.devicePointer), capacity);
+}
+
+// Makes ring buffer r the volume's vertex buffer.
+static void vol_select_verts(bcmc_vol* v, int r)
+{
+    if (r == v->cur) return;
+    v->ring[v->cur] = v->verts;
+    v->ring_cap[v->cur] = v->vert_capacity;
+    v->verts = v->ring[r];
+    v->vert_capacity = v->ring_cap[r];
+    v->cur = r;
+}
+
+bcmc_status bcmc_compute_surfaces_host(bcmc_vol* v, const float* isovalues, uint32_t n, void* host_vertices,
+                                       uint64_t capacity, uint32_t* num_vertices)
+{
+    if (!v || (n && (!isovalues || !host_vertices || !num_vertices || capacity == 0)) ||
+        reinterpret_cast<uintptr_t>(host_vertices) % 8 != 0)
+        return BCMC_E_ARG;
+    if (n == 0) return BCMC_OK;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, host_vertices) != cudaSuccess || at.type != cudaMemoryTypeHost) {
+        cudaGetLastError();
+        return fail(v->ctx, BCMC_E_ARG, "the host buffer must be page-locked (cudaMallocHost or cudaHostRegister)");
+    }
+    for (uint32_t i = 0; i < n; ++i) num_vertices[i] = 0;
+    bcmc_ctx* ctx = v->ctx;
+    uint2* const host = static_cast<uint2*>(host_vertices);
+    bool pending[kVertRing] = {};
+    const bcmc_status st = guarded(ctx, [&]() -> bcmc_status {
+        if (!v->copy) {
+            BCMC_CUDA(cudaStreamCreateWithFlags(&v->copy, cudaStreamNonBlocking));
+            for (auto& e : v->copy_ev) BCMC_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        }
+        uint64_t used = 0;
+        for (uint32_t i = 0; i < n; ++i) {
+            const int b = (int)(i % kVertRing);  // ring buffer 0 is the volume's vertex buffer
+            vol_select_verts(v, b);
+            uint32_t largest = 0;
+            for (int r = 0; r < kVertRing; ++r)
+                if (r != b) largest = std::max(largest, v->ring_cap[r]);
+            if (v->vert_capacity < largest) {
+                // every buffer at the largest size; the transfer from this one ends first
+                if (pending[b]) BCMC_CUDA(cudaEventSynchronize(v->copy_ev[b]));
+                pending[b] = false;
+                dev_free(ctx, v->verts, (size_t)v->vert_capacity * 8);
+                v->verts = nullptr;
+                v->vert_capacity = 0;
+                v->verts = (uint2*)dev_alloc(ctx, (size_t)largest * 8);
+                v->vert_capacity = largest;
+            }
+            // the query writes this buffer only after its previous transfer
+            if (pending[b]) BCMC_CUDA(cudaStreamWaitEvent(ctx->stream, v->copy_ev[b], 0));
+            uint32_t nv = 0;
+            const bcmc_status q = vol_query(v, isovalues[i], nullptr, &nv, nullptr, 0);
+            if (q != BCMC_OK) return q;
+            num_vertices[i] = nv;
+            if (nv > capacity - used)
+                return fail(ctx, BCMC_E_LIMIT, "the host buffer holds " + std::to_string(capacity) +
+                                                    " vertices; query " + std::to_string(i) + " needs " +
+                                                    std::to_string(used + nv));
+            if (nv) {
+                // the query has completed on the library's stream (vol_query waits for it)
+                BCMC_CUDA(cudaMemcpyAsync(host + used, v->verts, (size_t)nv * 8, cudaMemcpyDeviceToHost, v->copy));
+                BCMC_CUDA(cudaEventRecord(v->copy_ev[b], v->copy));
+                pending[b] = true;
+            }
+            used += nv;
+        }
+        return BCMC_OK;
+    });
+    // every transfer has ended when the call returns, also on failure
+    if (v->copy && cudaStreamSynchronize(v->copy) != cudaSuccess && st == BCMC_OK)
+        return fail(ctx, BCMC_E_CUDA, "vertex transfer failed");
+    return st;
 }
 
 bcmc_status bcmc_vertices(bcmc_vol* v, const void** d_vertices, uint64_t* bytes)
