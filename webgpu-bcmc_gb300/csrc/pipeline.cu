@@ -563,6 +563,10 @@ constexpr int kMcPerSm = 6;               // resident CTAs per SM (the grid: one
 //     are spread over the CTA -- thread k takes vertex k of the tile, finds its
 //     cell by binary search, its edge in the precomputed corner-pair table --
 //     so lanes stay converged and stores are contiguous.
+// Ranges of at most two tiles (small queries) skip the barrier: each CTA
+// emits its own range's tiles of blocks with vertices.  On the 256^3 CT-like
+// sweep the barrier and the tile claims cost 6-10 us on queries of under
+// 30,000 active blocks and the balance saves up to 48 us on the largest.
 // Output order = the reference's: active-block order, cell order, table order.
 // kHost: the vertices go to page-locked host memory (a.host_verts); its own
 // instantiation keeps the device path's emit loop free of the alignment shift.
@@ -580,7 +584,8 @@ __global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McAr
     __shared__ uint32_t s_slot[kMcBlocks][8];
     __shared__ uint32_t s_act[kMcBlocks];
     __shared__ uint32_t s_warp[kMcThreads / 32 + 1];
-    __shared__ uint32_t s_stop, s_with, s_pv, s_pb, s_cta_v, s_cta_b, s_rank;
+    __shared__ uint32_t s_idx[kMcBlocks];
+    __shared__ uint32_t s_stop, s_with, s_pv, s_pb, s_cta_v, s_cta_b, s_rank, s_cursor;
     __shared__ uint32_t s_gdesc[64];  // ghost_desc of each ghost voxel
     __shared__ uint8_t s_nb_off[8];
 
@@ -602,6 +607,7 @@ __global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McAr
     if (t < 16) reinterpret_cast<uint4*>(s_cnt)[t] = reinterpret_cast<const uint4*>(c_tri.count)[t];
     if (t == 0) {
         s_cta_v = s_cta_b = 0;
+        s_cursor = start;
     }
     if (t < 61) s_gdesc[t] = ghost_desc(c_ghost[t]);
     if (t < 32) {
@@ -816,6 +822,65 @@ __global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McAr
     uint32_t pv = s_pv, pb = s_pb;
     const bool fits = (uint64_t)pv + s_cta_v <= cap;
     if (!fits && t == 0) atomicOr(&q->vert_overflow, 1u);
+    if (range <= 2u * kMcBlocks) {
+        // short ranges (small queries): each CTA emits its own range, tiles of
+        // its next 16 blocks that have vertices (a warp ballot over the counts
+        // skips the others); the imbalance costs less here than the barrier
+        if (!fits) return;
+        const uint32_t lane = t & 31u;
+        for (;;) {
+            __syncthreads();
+            if (t < 32) {
+                uint32_t cur = s_cursor, filled = 0;
+                while (filled < kMcBlocks && cur < end) {
+                    const uint32_t i = cur + lane;
+                    const uint32_t c = i < end ? a.block_counts[i] : 0u;
+                    const uint32_t m = __ballot_sync(0xffffffffu, c != 0u);
+                    const uint32_t nz = __popc(m), take = min(nz, kMcBlocks - filled);
+                    const uint32_t r = __popc(m & ((1u << lane) - 1u));
+                    if (c != 0u && r < take) s_idx[filled + r] = i;
+                    if (take < nz) {
+                        uint32_t mm = m;
+                        for (uint32_t k = 0; k < take; ++k) mm &= mm - 1u;
+                        cur += (uint32_t)__ffs(mm) - 1u;
+                    } else {
+                        cur += 32u;
+                    }
+                    filled += take;
+                }
+                __syncwarp();
+                if (lane < kMcBlocks) s_id[lane] = lane < filled ? __ldg(a.active_ids + s_idx[lane]) : 0xffffffffu;
+                if (lane == 0) {
+                    s_stop = filled;
+                    s_cursor = min(cur, end);
+                }
+            }
+            __syncthreads();
+            const uint32_t n_sel = s_stop;
+            if (n_sel == 0) break;
+            const uint32_t dims = load_tile();
+            uint32_t nv[4], cs4;
+            const uint32_t mysum = count_cells(dims, nv, cs4);
+            uint32_t tile_v;
+            uint32_t run = cta_exclusive_scan<kMcThreads>(mysum, s_warp, &tile_v);
+            *reinterpret_cast<uint32_t*>(&s_case[4u * t]) = cs4;
+#pragma unroll
+            for (uint32_t x = 0; x < 4; ++x) {
+                s_off[4u * t + x] = run;
+                run += nv[x];
+            }
+            if (t == 0) s_off[kMcCells] = tile_v;
+            __syncthreads();
+            if (t < n_sel) {
+                a.with_verts[pb + t] = s_idx[t];
+                a.vert_offsets[pb + t] = pv + s_off[64 * t];
+            }
+            emit_tile(pv, tile_v);
+            pv += tile_v;
+            pb += n_sel;
+        }
+        return;
+    }
     // the range's blocks with vertices: their list entries and vertex offsets
     if (fits)
         for (uint32_t b0 = start; b0 < end; b0 += kMcThreads) {
