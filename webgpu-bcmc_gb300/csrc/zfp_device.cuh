@@ -204,7 +204,7 @@ __device__ __forceinline__ uint32_t zfp_parse_planes(ZfpWindow& rd, uint32_t bud
 //   bits 8-15 which of those became significant (bit i: the i-th passed)
 //   bit 16    the plane ended
 //   bit 17    the state after the last bit consumed
-__host__ __device__ __forceinline__ uint32_t zfp_gt_entry(uint32_t idx)
+__host__ __device__ constexpr uint32_t zfp_gt_entry(uint32_t idx)
 {
     uint32_t s = (idx >> 8) & 1u, dn = 0, mask = 0, c = 0, end = 0;
     while (c < 8u) {
@@ -228,11 +228,25 @@ __host__ __device__ __forceinline__ uint32_t zfp_gt_entry(uint32_t idx)
 }
 
 constexpr uint32_t kZfpGtWords = 512;
+struct ZfpGtTable {
+    uint32_t v[kZfpGtWords];
+};
+constexpr ZfpGtTable zfp_make_gt()
+{
+    ZfpGtTable t{};
+    for (uint32_t i = 0; i < kZfpGtWords; ++i) t.v[i] = zfp_gt_entry(i);
+    return t;
+}
+// built at compile time; a CTA copies it into shared memory (zfp_gt_fill)
+static __device__ const ZfpGtTable g_zfp_gt = zfp_make_gt();
+static_assert(zfp_make_gt().v[0] == (1u | (1u << 16)), "state 0, bit 0 clear: the plane ends after one bit");
+static_assert(zfp_make_gt().v[256] == (8u | (8u << 4) | (1u << 17)), "state 1, eight zeros: a run continues");
 
-// The CTA's threads fill the table; the caller synchronises before use.
+// The CTA's threads copy the table into shared memory; the caller
+// synchronises before use.
 __device__ __forceinline__ void zfp_gt_fill(uint32_t* gt)
 {
-    for (uint32_t i = threadIdx.x; i < kZfpGtWords; i += blockDim.x) gt[i] = zfp_gt_entry(i);
+    for (uint32_t i = threadIdx.x; i < kZfpGtWords; i += blockDim.x) gt[i] = g_zfp_gt.v[i];
 }
 
 // zfp_parse_planes with the group tests taken 8 bits per table step: a step
