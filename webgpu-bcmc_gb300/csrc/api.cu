@@ -141,6 +141,9 @@ struct bcmc_lru {
     uint32_t* sort_bv = nullptr;
     uint32_t* sort_ck = nullptr;
     uint32_t* sort_cv = nullptr;
+    // age bins: joint histogram and dense ranks (k_slots' one-pass sort plan)
+    uint32_t* age_hist = nullptr;
+    uint8_t* age_rank = nullptr;
     uint64_t* status = nullptr;
     size_t status_words = 0;
     uint64_t* st_active_a = nullptr;
@@ -156,6 +159,13 @@ struct bcmc_lru {
 };
 
 static size_t slot_array_bytes(uint32_t cap) { return (size_t)cap * 4u; }
+
+// k_slots leaves the age histogram zero after every update; it is cleared
+// here when an update may not have finished (a wait gave up)
+static void lru_clear_key16(bcmc_lru* c, cudaStream_t s)
+{
+    BCMC_CUDA(cudaMemsetAsync(c->age_hist, 0, (size_t)kAgeBins * 4, s));
+}
 
 static void lru_alloc_slots(bcmc_lru* c, uint32_t cap)
 {
@@ -276,7 +286,10 @@ static bcmc_lru* lru_new(bcmc_ctx* ctx, uint32_t initial_size, uint32_t element_
         c->st_mc_b = c->st_mc_v + wm;
         c->q = (QueryState*)dev_alloc(ctx, sizeof(QueryState));
         BCMC_CUDA(cudaMallocHost(&c->h_q, sizeof(QueryState)));
+        c->age_hist = (uint32_t*)dev_alloc(ctx, (size_t)kAgeBins * 4);
+        c->age_rank = (uint8_t*)dev_alloc(ctx, (size_t)kAgeBins);
         cudaStream_t s = ctx->stream;
+        lru_clear_key16(c, s);
         BCMC_CUDA(cudaMemsetAsync(c->status, 0, c->status_words * 8, s));
         BCMC_CUDA(cudaMemsetAsync(c->q, 0, sizeof(QueryState), s));
         BCMC_CUDA(cudaMemcpyAsync(&c->q->cache_size, &c->cache_size, 4, cudaMemcpyHostToDevice, s));
@@ -311,6 +324,8 @@ static void lru_delete(bcmc_lru* c)
     dev_free(ctx, c->item_slots, (size_t)c->aligned_total * 4);
     dev_free(ctx, c->new_ids, (size_t)(c->total ? c->total : 1) * 4);
     dev_free(ctx, c->status, c->status_words * 8);
+    dev_free(ctx, c->age_hist, (size_t)kAgeBins * 4);
+    dev_free(ctx, c->age_rank, (size_t)kAgeBins);
     dev_free(ctx, c->q, sizeof(QueryState));
     if (c->h_q) cudaFreeHost(c->h_q);
     delete c;
@@ -327,6 +342,7 @@ static SortBuffers lru_sort_buffers(bcmc_lru* c)
     b.c_keys = c->sort_ck;
     b.c_vals = c->sort_cv;
     b.status = c->st_sort;
+    b.age_rank = c->age_rank;
     return b;
 }
 
@@ -335,7 +351,8 @@ static void lru_enqueue_update(bcmc_lru* c, cudaStream_t s, const uint32_t* need
                                uint32_t max_bits)
 {
     bcmc_ctx* ctx = c->ctx;
-    SlotArgs sa{needed, c->slot_age, c->slot_avail, c->slot_item, c->avail_ids, c->avail_keys, c->st_slots, 0u, 1u};
+    SlotArgs sa{needed,    c->slot_age, c->slot_avail, c->slot_item, c->avail_ids, c->avail_keys, c->st_slots, 0u, 1u,
+                c->age_hist, c->age_rank};
     slots_launch(ctx, c->q, sa, c->capacity, s);
     sort_launch(ctx, c->q, &c->q->num_avail, c->capacity, lru_sort_buffers(c), 1, s, /*plan_ready=*/1);
     AssignArgs aa{c->new_ids, c->sort_bv,   c->sort_cv, c->slot_age, c->slot_avail, c->slot_item,
@@ -629,7 +646,8 @@ static void vol_enqueue_query(bcmc_vol* v, cudaStream_t s, float iso, int from_s
                   v->total, v->active_ids, c->new_ids, c->st_active_a, c->st_active_n};
     McArgs ma{v->active, v->active_ids, c->item_slots, reinterpret_cast<const float*>(c->cache), nb, grid,
               v->with_verts, v->vert_offsets, v->block_counts, out, c->st_mc_v, c->st_mc_b, out != v->verts ? 1u : 0u};
-    SlotArgs sa{v->active, c->slot_age, c->slot_avail, c->slot_item, c->avail_ids, c->avail_keys, c->st_slots, 1u, 1u};
+    SlotArgs sa{v->active,  c->slot_age, c->slot_avail, c->slot_item, c->avail_ids, c->avail_keys, c->st_slots, 1u, 1u,
+                c->age_hist, c->age_rank};
     AssignArgs as{c->new_ids, c->sort_bv, c->sort_cv, c->slot_age, c->slot_avail, c->slot_item,
                   c->item_slots, v->words, v->max_bits, reinterpret_cast<float*>(c->cache), v->stage, v->stage_blocks};
     DecodeArgs da{c->new_ids, v->words, v->max_bits, v->stage, v->stage_blocks};
@@ -719,6 +737,7 @@ static bcmc_status vol_query(bcmc_vol* v, float iso, bcmc_perf* perf, uint32_t* 
                 // over the logical size the query reached
                 const uint32_t site = c->h_q->error;
                 c->cache_size = std::min(std::max(c->cache_size, c->h_q->cache_size), c->capacity);
+                lru_clear_key16(c, s);
                 lru_reset_impl(c);
                 return fail(ctx, BCMC_E_TIMEOUT, "device wait timed out (site " + std::to_string(site) + ")");
             }
@@ -1002,7 +1021,10 @@ bcmc_status bcmc_lru_update(bcmc_lru* c, const uint32_t* d_item_needed, uint32_t
             active_launch(ctx, c->q, aa, s);
             lru_enqueue_update(c, s, d_item_needed, nullptr, 0);
             lru_read_state(c, s);
-            if (c->h_q->error) return fail(ctx, BCMC_E_TIMEOUT, "device wait timed out");
+            if (c->h_q->error) {
+                lru_clear_key16(c, s);
+                return fail(ctx, BCMC_E_TIMEOUT, "device wait timed out");
+            }
             if (c->h_q->grow_needed) {
                 if (attempt > 2) return fail(ctx, BCMC_E_STATE, "cache growth did not converge");
                 lru_grow_capacity(c, c->h_q->grow_needed);

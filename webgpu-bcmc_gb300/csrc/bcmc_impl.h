@@ -99,6 +99,8 @@ struct SortBuffers {
     uint32_t* c_keys;
     uint32_t* c_vals;
     uint64_t* status;  // kSortTileStatus words per tile (256 per tile)
+    // the LRU's age sort: dense rank of each age bin (age_bin; sort_key16 == 2)
+    const uint8_t* age_rank = nullptr;
 };
 // plan_ready: the keys' producer already made the pass plan and bucket
 // offsets in q (sort_plan), so the histogram kernel is not launched.

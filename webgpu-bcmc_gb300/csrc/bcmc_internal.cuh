@@ -62,8 +62,8 @@ struct QueryState {
     uint32_t sort_run[4];     // 1 if the digit pass runs
     uint32_t sort_first;      // index of the first pass that runs (4 = none)
     uint32_t sort_final;      // buffer holding the sorted values
-    uint32_t sort_key16;      // 1: the passes sort the 16-bit age keys (age_key16)
-    uint32_t sort_wide;       // set by k_slots when an available slot's age has no 16-bit key
+    uint32_t sort_key16;      // 1: the passes sort the 16-bit age keys (age_key16); 2: their dense ranks (one pass)
+    uint32_t sort_wide;       // k_slots: bit 0 an available slot's age has no 16-bit key, bit 1 none in an age bin
     uint32_t sort_hist[4][256];
     uint32_t sort_hist16[2][256];  // k_slots: digit histograms of the 16-bit age keys
     // test hook (bcmc_debug_drop_tile): 0, or t + 1 when tile t of the active
@@ -89,6 +89,15 @@ __device__ __forceinline__ bool lb_dropped(const QueryState* q, uint32_t tile)
 // can run two 8-bit digit passes instead of three with the same order and ties.
 __device__ __forceinline__ bool age_has_key16(uint32_t age) { return age < 32768u || age - 100000u < 32768u; }
 __device__ __forceinline__ uint32_t age_key16(uint32_t age) { return age < 32768u ? age : 32768u + (age - 100000u); }
+// Ages below 256 within their class (a count of updates, or 100000 + a count):
+// bin (class, low byte), in the order of age_key16.  kAgeBins marks any other age.
+constexpr uint32_t kAgeBins = 512;
+__device__ __forceinline__ uint32_t age_bin(uint32_t age)
+{
+    if (age < 256u) return age;
+    if (age - 100000u < 256u) return 256u + (age - 100000u);
+    return kAgeBins;
+}
 
 // ---------------------------------------------------------------------------
 // Decoupled look-back status words: [epoch:30 | flag:2][value:32].

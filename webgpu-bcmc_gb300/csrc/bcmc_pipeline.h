@@ -35,6 +35,12 @@ struct SlotArgs {
     // keys) and make the sort's pass plan in the last CTA, so the sort that
     // follows runs without its histogram kernel
     uint32_t plan;
+    // the joint histogram of the 16-bit age keys whose age is below 256 in
+    // its class (kAgeBins bins: class, low byte), zero between updates, and
+    // the dense rank of each bin, for a one-pass sort when every key is such
+    // and at most 256 bins are used
+    uint32_t* age_hist;
+    uint8_t* age_rank;
 };
 
 struct AssignArgs {

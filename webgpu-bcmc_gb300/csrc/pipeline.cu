@@ -349,15 +349,19 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
     __shared__ uint32_t s_warp[kActThreads / 32 + 1];
     __shared__ uint32_t s_tile, s_prefix;
     __shared__ uint32_t s_hist[6][256];  // ~age digits 0-3, then the 16-bit keys' digits 0-1
+    __shared__ uint32_t s_bins[kAgeBins];  // age bins (age_bin)
     __shared__ bool s_last;
     if ((a.skip_when_inactive && q->num_active == 0) || q->grow_needed) return;
     const uint32_t old = q->old_cache_size, nsz = q->new_cache_size;
     const bool compact = q->num_new > 0;
     const bool hist = compact && a.plan != 0u;
     const uint32_t lane = threadIdx.x & 31u;
-    uint32_t wide = 0;  // an age without a 16-bit key
-    if (hist)
+    uint32_t wide = 0;     // an age without a 16-bit key
+    uint32_t binless = 0;  // an age outside the age bins
+    if (hist) {
         for (int i = threadIdx.x; i < 1536; i += kActThreads) (&s_hist[0][0])[i] = 0;
+        for (int i = threadIdx.x; i < (int)kAgeBins; i += kActThreads) s_bins[i] = 0;
+    }
     const uint32_t ntiles = div_up(nsz, kSlotTile);
     const uint32_t epoch = q->epoch;
     for (;;) {
@@ -416,7 +420,13 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
                 }
                 if (hist) {  // one shared atomic per distinct digit and warp
                     const uint32_t k = ~age, k16 = ~age_key16(age);
-                    if (fl[j] && !age_has_key16(age)) wide = 1;
+                    const bool has16 = fl[j] && age_has_key16(age);
+                    if (fl[j] && !has16) wide = 1;
+                    // the joint histogram of the age bins (one shared atomic per distinct bin and warp)
+                    const uint32_t bin = fl[j] ? age_bin(age) : kAgeBins + 1u;
+                    if (bin == kAgeBins) binless = 1;
+                    const uint32_t bp = __match_any_sync(0xffffffffu, bin);
+                    if (bin < kAgeBins && lane == (uint32_t)__ffs(bp) - 1u) atomicAdd(&s_bins[bin], (uint32_t)__popc(bp));
 #pragma unroll
                     for (int d = 0; d < 6; ++d) {
                         const uint32_t digit = fl[j] ? ((d < 4 ? k : k16) >> (8 * (d & 3))) & 255u : 256u;
@@ -437,16 +447,50 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
         const uint32_t c = (&s_hist[0][0])[i];
         if (c) atomicAdd(gh + i, c);
     }
+    for (int i = threadIdx.x; i < (int)kAgeBins; i += kActThreads)
+        if (s_bins[i]) atomicAdd(a.age_hist + i, s_bins[i]);
     if (__syncthreads_or(wide) && threadIdx.x == 0) atomicOr(&q->sort_wide, 1u);
+    if (__syncthreads_or(binless) && threadIdx.x == 0) atomicOr(&q->sort_wide, 2u);
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) s_last = atomicAdd(&q->tiles_sort_hist, 1u) == gridDim.x - 1u;
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    const bool key16 = *reinterpret_cast<volatile uint32_t*>(&q->sort_wide) == 0u;
-    if (threadIdx.x == 0) q->sort_key16 = key16 ? 1u : 0u;
-    if (key16) sort_plan(q, q->num_avail, s_warp, &q->sort_hist16[0][0], 2);
+    const uint32_t flags = *reinterpret_cast<volatile uint32_t*>(&q->sort_wide);
+    const bool key16 = (flags & 1u) == 0u;
+    // the age bins in use (two per thread, in age order) and how many
+    uint32_t cnt[2], used = 0;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        cnt[k] = __ldcg(a.age_hist + 2u * threadIdx.x + k);
+        used += cnt[k] ? 1u : 0u;
+    }
+    uint32_t distinct;
+    const uint32_t below = cta_exclusive_scan<kActThreads>(used, s_warp, &distinct);
+    // every age in a bin and at most 256 bins used: one sort pass on the bins'
+    // dense ranks, older ages (higher bins) ranked first
+    const bool dense = flags == 0u && distinct <= 256u;
+    uint32_t* rank_hist = &q->sort_hist16[0][0];  // reused for the ranks' histogram
+    if (dense) {
+        rank_hist[threadIdx.x] = 0u;
+        __syncthreads();
+        uint32_t p = below;
+#pragma unroll
+        for (int k = 0; k < 2; ++k)
+            if (cnt[k]) {
+                const uint32_t rank = distinct - 1u - p++;
+                a.age_rank[2u * threadIdx.x + k] = (uint8_t)rank;
+                rank_hist[rank] = cnt[k];
+            }
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) a.age_hist[2u * threadIdx.x + k] = 0u;  // zero again for the next update
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) q->sort_key16 = dense ? 2u : (key16 ? 1u : 0u);
+    if (dense) sort_plan(q, q->num_avail, s_warp, rank_hist, 1);
+    else if (key16) sort_plan(q, q->num_avail, s_warp, &q->sort_hist16[0][0], 2);
     else sort_plan(q, q->num_avail, s_warp, &q->sort_hist[0][0], 4);
 }
 

@@ -21,8 +21,11 @@
 //
 // The LRU's age sort skips the histogram kernel: k_slots, which compacts the
 // ages, accumulates the histograms and makes the plan (sort_plan).  When every
-// age has a 16-bit key (age_key16) the plan sorts on that key (sort_key16), so
-// the first pass maps each age through it and two digit passes suffice.
+// age has a 16-bit key (age_key16) the plan sorts on that key (sort_key16 1),
+// so the first pass maps each age through it and two digit passes suffice;
+// when every age lies in an age bin (age_bin) and at most 256 bins are used,
+// on the bins' dense ranks (sort_key16 2, older ages ranked first, from a
+// table k_slots builds): one pass.
 #include "bcmc_impl.h"
 
 namespace bcmc {
@@ -98,7 +101,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(QueryState* q, const
     uint32_t* __restrict__ kd = src == 1 ? b.c_keys : b.b_keys;
     uint32_t* __restrict__ vd = src == 1 ? b.c_vals : b.b_vals;
     const bool gather = src == 0;
-    const bool key16 = q->sort_key16 != 0u;
+    const uint32_t kmode = q->sort_key16;  // 0: the keys, 1: 16-bit age keys, 2: their dense ranks
     const uint32_t shift = 8u * (uint32_t)pass;
     const uint32_t epoch = q->epoch * 4u + (uint32_t)pass;
     const uint32_t ntiles = div_up(n, kSortTile);
@@ -123,8 +126,12 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(QueryState* q, const
             if (qi < n) {
                 const uint32_t p = gather ? tie_perm(qi, n, reverse) : qi;
                 uint32_t k = ks[p];
-                if (gather && key16) k = age_key16(k);
-                if (gather && reverse) k = ~k;
+                if (gather && kmode == 1u) k = age_key16(k);
+                if (gather && kmode == 2u) {
+                    k = b.age_rank[age_bin(k)];  // ascending rank = descending age: no complement
+                } else if (gather && reverse) {
+                    k = ~k;
+                }
                 key[j] = k;
                 val[j] = vs[p];
             }
