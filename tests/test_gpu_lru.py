@@ -20,8 +20,12 @@ def _compare(c_gpu, c_ref, total):
     assert np.array_equal(g["item"], r["item"])
 
 
+# The age sort's plans are all exercised: one pass on the ranks of the age bins
+# (ages below 256 within their class), two passes on 16-bit keys (ages of a
+# new cache, 2 + slot, up to 32767; or ages past 255 after 300 updates), four
+# passes on 32-bit keys (a new cache of more than 32766 slots).
 @pytest.mark.parametrize("total,initial,steps", [(300, 20, 40), (5000, 64, 30), (70000, 3500, 12),
-                                                 (262144, 13107, 6)])
+                                                 (262144, 13107, 6), (2000, 300, 300), (80000, 40000, 4)])
 def test_lru_sequence_matches_oracle(ctx, oracle, total, initial, steps):
     rs = np.random.default_rng(total)
     g = bcmc.LRUCache(ctx, None, None, initial, 256, total)

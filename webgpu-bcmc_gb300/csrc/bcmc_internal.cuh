@@ -72,7 +72,8 @@ struct QueryState {
     // k_mc's grid barrier (CTAs arrived) and its emit tiles' counter
     uint32_t mc_arrived;
     uint32_t tiles_emit;
-    uint32_t pad[5];
+    uint32_t sort_arrived;  // k_sort's grid barriers between digit passes
+    uint32_t pad[4];
 };
 
 // The test hook's check: this tile publishes nothing, so the tiles after it

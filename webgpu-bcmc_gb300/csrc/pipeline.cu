@@ -63,6 +63,7 @@ __global__ void k_query_begin(QueryState* q, float iso, int mc_only, uint32_t ca
             q->isovalue = iso;
             q->tiles_active = q->tiles_slots = q->tiles_sort_hist = 0;
             for (int i = 0; i < 4; ++i) q->tiles_sort[i] = 0;
+            q->sort_arrived = 0;
             q->num_active = q->num_new = q->num_avail = 0;
             q->grow_needed = 0;
             // the sort plan of zero keys (k_slots replaces it when it sorts)

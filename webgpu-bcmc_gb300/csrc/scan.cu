@@ -20,6 +20,7 @@ __global__ void k_prim_begin(QueryState* q)
         q->epoch += 1;
         q->tiles_active = q->tiles_slots = q->tiles_mc = q->tiles_sort_hist = 0;
         for (int i = 0; i < 4; ++i) q->tiles_sort[i] = 0;
+        q->sort_arrived = 0;
         q->error = 0;
         q->num_with_verts = q->num_verts = 0;
         q->grow_needed = 0;

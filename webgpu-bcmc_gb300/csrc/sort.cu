@@ -14,7 +14,8 @@
 //
 // Kernels: a histogram/plan kernel (all four 8-bit digit histograms in one
 // read, exclusive bucket offsets, and which digit passes can be skipped because
-// every key shares the digit), then one onesweep pass per digit: tiles of 4096
+// every key shares the digit), then one cooperative kernel that runs the onesweep
+// pass of each digit the plan keeps, grid barriers between them: tiles of 4096
 // keys are ranked with warp match/popc, each tile publishes its 256 digit
 // counts through decoupled look-back, and keys are scattered via shared memory
 // so that global writes come out in runs.
@@ -82,8 +83,11 @@ __global__ void __launch_bounds__(256) k_sort_hist(QueryState* q, const uint32_t
     sort_plan(q, n, warp_sums, &q->sort_hist[0][0], 4);
 }
 
-__global__ void __launch_bounds__(kSortThreads) k_sort_pass(QueryState* q, const uint32_t* d_n, uint32_t n_host,
-                                                            SortBuffers b, int reverse, int pass)
+// All the digit passes of the plan in one cooperative launch: the passes
+// that run are separated by grid barriers (each reads what the one before it
+// scattered, so its key and value loads bypass L1), the others cost nothing.
+__global__ void __launch_bounds__(kSortThreads, 2) k_sort(QueryState* q, const uint32_t* d_n, uint32_t n_host,
+                                                       SortBuffers b, int reverse)
 {
     __shared__ uint32_t s_keys[kSortTile];
     __shared__ uint32_t s_vals[kSortTile];
@@ -93,101 +97,124 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(QueryState* q, const
     __shared__ uint32_t s_warp_sums[kSortThreads / 32 + 1];
     __shared__ uint32_t s_tile;
 
-    if (!q->sort_run[pass]) return;
     const uint32_t n = d_n ? *d_n : n_host;
-    const uint32_t src = q->sort_src[pass];
-    const uint32_t* __restrict__ ks = src == 0 ? b.in_keys : (src == 1 ? b.b_keys : b.c_keys);
-    const uint32_t* __restrict__ vs = src == 0 ? b.in_vals : (src == 1 ? b.b_vals : b.c_vals);
-    uint32_t* __restrict__ kd = src == 1 ? b.c_keys : b.b_keys;
-    uint32_t* __restrict__ vd = src == 1 ? b.c_vals : b.b_vals;
-    const bool gather = src == 0;
-    const uint32_t kmode = q->sort_key16;  // 0: the keys, 1: 16-bit age keys, 2: their dense ranks
-    const uint32_t shift = 8u * (uint32_t)pass;
-    const uint32_t epoch = q->epoch * 4u + (uint32_t)pass;
-    const uint32_t ntiles = div_up(n, kSortTile);
-    const uint32_t* bucket = q->sort_hist[pass];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t lt_mask = (1u << lane) - 1u;
-
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(&q->tiles_sort[pass], 1u);
-        for (int i = threadIdx.x; i < (kSortThreads / 32) * 256; i += kSortThreads) (&s_whist[0][0])[i] = 0;
-        __syncthreads();
-        const uint32_t tile = s_tile;
-        if (tile >= ntiles) break;
-
-        uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
-        const uint32_t base = tile * kSortTile + (uint32_t)warp * (32u * kSortItems);
-#pragma unroll
-        for (int j = 0; j < kSortItems; ++j) {
-            const uint32_t qi = base + 32u * j + lane;
-            key[j] = 0;
-            val[j] = 0;
-            if (qi < n) {
-                const uint32_t p = gather ? tie_perm(qi, n, reverse) : qi;
-                uint32_t k = ks[p];
-                if (gather && kmode == 1u) k = age_key16(k);
-                if (gather && kmode == 2u) {
-                    k = b.age_rank[age_bin(k)];  // ascending rank = descending age: no complement
-                } else if (gather && reverse) {
-                    k = ~k;
+    uint32_t barriers = 0;  // thread 0's count of grid barriers passed
+    bool ran = false;
+    for (int pass = 0; pass < 4; ++pass) {
+        if (!q->sort_run[pass]) continue;
+        if (ran) {
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                __threadfence();
+                ++barriers;
+                atomicAdd(&q->sort_arrived, 1u);
+                uint32_t spins = 0;
+                while (*reinterpret_cast<volatile uint32_t*>(&q->sort_arrived) < barriers * gridDim.x) {
+                    if (++spins > kSpinLimit) {
+                        atomicCAS(&q->error, 0u, 28u);
+                        break;
+                    }
+                    if (spins > 8) __nanosleep(100);
                 }
-                key[j] = k;
-                val[j] = vs[p];
+                __threadfence();
             }
+            __syncthreads();
         }
+        ran = true;
+        const uint32_t src = q->sort_src[pass];
+        const uint32_t* __restrict__ ks = src == 0 ? b.in_keys : (src == 1 ? b.b_keys : b.c_keys);
+        const uint32_t* __restrict__ vs = src == 0 ? b.in_vals : (src == 1 ? b.b_vals : b.c_vals);
+        uint32_t* __restrict__ kd = src == 1 ? b.c_keys : b.b_keys;
+        uint32_t* __restrict__ vd = src == 1 ? b.c_vals : b.b_vals;
+        const bool gather = src == 0;
+        const uint32_t kmode = q->sort_key16;  // 0: the keys, 1: 16-bit age keys, 2: their dense ranks
+        const uint32_t shift = 8u * (uint32_t)pass;
+        const uint32_t epoch = q->epoch * 4u + (uint32_t)pass;
+        const uint32_t ntiles = div_up(n, kSortTile);
+        const uint32_t* bucket = q->sort_hist[pass];
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const uint32_t lt_mask = (1u << lane) - 1u;
+
+        for (;;) {
+            if (threadIdx.x == 0) s_tile = atomicAdd(&q->tiles_sort[pass], 1u);
+            for (int i = threadIdx.x; i < (kSortThreads / 32) * 256; i += kSortThreads) (&s_whist[0][0])[i] = 0;
+            __syncthreads();
+            const uint32_t tile = s_tile;
+            if (tile >= ntiles) break;
+
+            uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+            const uint32_t base = tile * kSortTile + (uint32_t)warp * (32u * kSortItems);
 #pragma unroll
-        for (int j = 0; j < kSortItems; ++j) {
-            const uint32_t qi = base + 32u * j + lane;
-            const uint32_t digit = qi < n ? (key[j] >> shift) & 255u : 256u;
-            const uint32_t peers = __match_any_sync(0xffffffffu, digit);
-            const uint32_t cnt = digit < 256u ? s_whist[warp][digit] : 0u;
-            __syncwarp();
-            if (digit < 256u && lane == __ffs(peers) - 1) s_whist[warp][digit] = (uint16_t)(cnt + __popc(peers));
-            __syncwarp();
-            rank[j] = cnt + __popc(peers & lt_mask);
-        }
-        __syncthreads();
-        // thread t owns digit t: warp-exclusive offsets and the tile count
-        const uint32_t t = threadIdx.x;
-        uint32_t run = 0;
-        if (t < 256) {
+            for (int j = 0; j < kSortItems; ++j) {
+                const uint32_t qi = base + 32u * j + lane;
+                key[j] = 0;
+                val[j] = 0;
+                if (qi < n) {
+                    const uint32_t p = gather ? tie_perm(qi, n, reverse) : qi;
+                    uint32_t k = __ldcg(ks + p);
+                    if (gather && kmode == 1u) k = age_key16(k);
+                    if (gather && kmode == 2u) {
+                        k = b.age_rank[age_bin(k)];  // ascending rank = descending age: no complement
+                    } else if (gather && reverse) {
+                        k = ~k;
+                    }
+                    key[j] = k;
+                    val[j] = __ldcg(vs + p);
+                }
+            }
 #pragma unroll
-            for (int w = 0; w < kSortThreads / 32; ++w) {
-                const uint32_t c = s_whist[w][t];
-                s_whist[w][t] = (uint16_t)run;
-                run += c;
+            for (int j = 0; j < kSortItems; ++j) {
+                const uint32_t qi = base + 32u * j + lane;
+                const uint32_t digit = qi < n ? (key[j] >> shift) & 255u : 256u;
+                const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+                const uint32_t cnt = digit < 256u ? s_whist[warp][digit] : 0u;
+                __syncwarp();
+                if (digit < 256u && lane == __ffs(peers) - 1) s_whist[warp][digit] = (uint16_t)(cnt + __popc(peers));
+                __syncwarp();
+                rank[j] = cnt + __popc(peers & lt_mask);
             }
-        }
-        uint32_t tile_total;
-        const uint32_t start = cta_exclusive_scan<kSortThreads>(run, s_warp_sums, &tile_total);
-        if (t < 256) {
-            s_start[t] = start;
-            const uint32_t excl = lookback_exclusive_w8(b.status + t, tile, run, epoch, &q->error, 20u + pass, 256u);
-            s_gbase[t] = bucket[t] + excl - start;
-        }
-        __syncthreads();
+            __syncthreads();
+            // thread t owns digit t: warp-exclusive offsets and the tile count
+            const uint32_t t = threadIdx.x;
+            uint32_t run = 0;
+            if (t < 256) {
 #pragma unroll
-        for (int j = 0; j < kSortItems; ++j) {
-            const uint32_t qi = base + 32u * j + lane;
-            if (qi < n) {
-                const uint32_t d = (key[j] >> shift) & 255u;
-                const uint32_t pos = s_start[d] + s_whist[warp][d] + rank[j];
-                s_keys[pos] = key[j];
-                s_vals[pos] = val[j];
+                for (int w = 0; w < kSortThreads / 32; ++w) {
+                    const uint32_t c = s_whist[w][t];
+                    s_whist[w][t] = (uint16_t)run;
+                    run += c;
+                }
             }
-        }
-        __syncthreads();
-        const uint32_t count = min((uint32_t)kSortTile, n - tile * kSortTile);
-        for (uint32_t i = threadIdx.x; i < count; i += kSortThreads) {
-            const uint32_t k = s_keys[i];
-            const uint32_t pos = s_gbase[(k >> shift) & 255u] + i;
-            if (pos < n) {  // always true unless a look-back wait timed out
-                kd[pos] = k;
-                vd[pos] = s_vals[i];
+            uint32_t tile_total;
+            const uint32_t start = cta_exclusive_scan<kSortThreads>(run, s_warp_sums, &tile_total);
+            if (t < 256) {
+                s_start[t] = start;
+                const uint32_t excl = lookback_exclusive_w8(b.status + t, tile, run, epoch, &q->error, 20u + pass, 256u);
+                s_gbase[t] = bucket[t] + excl - start;
             }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < kSortItems; ++j) {
+                const uint32_t qi = base + 32u * j + lane;
+                if (qi < n) {
+                    const uint32_t d = (key[j] >> shift) & 255u;
+                    const uint32_t pos = s_start[d] + s_whist[warp][d] + rank[j];
+                    s_keys[pos] = key[j];
+                    s_vals[pos] = val[j];
+                }
+            }
+            __syncthreads();
+            const uint32_t count = min((uint32_t)kSortTile, n - tile * kSortTile);
+            for (uint32_t i = threadIdx.x; i < count; i += kSortThreads) {
+                const uint32_t k = s_keys[i];
+                const uint32_t pos = s_gbase[(k >> shift) & 255u] + i;
+                if (pos < n) {  // always true unless a look-back wait timed out
+                    kd[pos] = k;
+                    vd[pos] = s_vals[i];
+                }
+            }
+            __syncthreads();
         }
-        __syncthreads();
     }
 }
 
@@ -207,10 +234,21 @@ __global__ void k_sort_writeback(QueryState* q, const uint32_t* d_n, uint32_t n_
 
 size_t sort_status_words(uint32_t n_max) { return (size_t)div_up(n_max ? n_max : 1, kSortTile) * 256u; }
 
+// CTAs of k_sort resident per SM: the bound of its cooperative grid
+static uint32_t sort_per_sm()
+{
+    static const uint32_t n = [] {
+        int r = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_sort, kSortThreads, 0) != cudaSuccess || r < 1) r = 1;
+        return (uint32_t)r;
+    }();
+    return n;
+}
+
 int sort_grid(bcmc_ctx* ctx, uint32_t n_max)
 {
     const uint32_t tiles = div_up(n_max ? n_max : 1, kSortTile);
-    const uint32_t resident = (uint32_t)ctx->num_sms * 3u;
+    const uint32_t resident = (uint32_t)ctx->num_sms * sort_per_sm();
     return (int)(tiles < resident ? tiles : resident);
 }
 
@@ -222,11 +260,19 @@ void sort_launch(bcmc_ctx* ctx, QueryState* q, const uint32_t* d_n, uint32_t n_m
         k_sort_hist<<<hist_grid, 256, 0, s>>>(q, d_n, n_max, bufs.in_keys, reverse);
         count_launches(1);
     }
-    const int grid = sort_grid(ctx, n_max);
-    for (int pass = 0; pass < 4; ++pass)
-        k_sort_pass<<<grid, kSortThreads, 0, s>>>(q, d_n, n_max, bufs, reverse, pass);
-    count_launches(4);
-    BCMC_CUDA(cudaGetLastError());
+    // cooperative: the grid barriers between digit passes need every CTA resident
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(sort_grid(ctx, n_max));
+    cfg.blockDim = dim3(kSortThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeCooperative;
+    attr.val.cooperative = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    BCMC_CUDA(cudaLaunchKernelEx(&cfg, k_sort, q, d_n, n_max, bufs, reverse));
+    count_launches(1);
 }
 
 void sort_writeback(bcmc_ctx* ctx, QueryState* q, const uint32_t* d_n, uint32_t n_max,
