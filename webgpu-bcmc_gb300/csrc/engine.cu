@@ -301,12 +301,10 @@ __global__ void __launch_bounds__(kEngThreads) k_bactive(BatchArgs a)
 // at the largest rate of the resident volumes (`max_rate` u64 words per block).
 
 template <int kThreads>
-__global__ void __launch_bounds__(kThreads) k_bdecode(BatchArgs a, uint32_t max_rate)
+__global__ void __launch_bounds__(kThreads, 640 / kThreads) k_bdecode(BatchArgs a, uint32_t max_rate)
 {
     extern __shared__ __align__(16) uint32_t s_words[];
     uint32_t* pl = zfp_stage_planes(s_words, kThreads, max_rate);
-    uint32_t* gt = zfp_stage_gt(s_words, kThreads, max_rate);
-    zfp_gt_fill(gt);
     if (threadIdx.x < 4) s_words[kThreads * 2u * max_rate + threadIdx.x] = 0u;
     const uint32_t n = a.st->num_decode;
     for (uint32_t i0 = blockIdx.x * kThreads; i0 < n; i0 += gridDim.x * kThreads) {
@@ -330,7 +328,7 @@ __global__ void __launch_bounds__(kThreads) k_bdecode(BatchArgs a, uint32_t max_
         if (i >= n) continue;
         const EngVolDev& V = a.vols[v];
         float out[64];
-        zfp_decode_staged(s_words + threadIdx.x * 2u * max_rate, V.max_bits, pl, out, gt);
+        zfp_decode_staged(s_words + threadIdx.x * 2u * max_rate, V.max_bits, pl, out);
         float4* d4 = reinterpret_cast<float4*>(a.cache + (uint64_t)slot * 64u);
 #pragma unroll
         for (int k = 0; k < 16; ++k) d4[k] = make_float4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
@@ -342,24 +340,22 @@ __global__ void __launch_bounds__(kThreads) k_bdecode(BatchArgs a, uint32_t max_
 
 // The autotuner's decode probe: k_bdecode's inner loop into a scratch buffer.
 template <int kThreads>
-__global__ void __launch_bounds__(kThreads) k_decode_probe(const uint64_t* __restrict__ words, uint32_t rate,
+__global__ void __launch_bounds__(kThreads, 640 / kThreads) k_decode_probe(const uint64_t* __restrict__ words, uint32_t rate,
                                                            uint32_t n, float* __restrict__ scratch)
 {
     extern __shared__ __align__(16) uint32_t s_words[];
     uint32_t* pl = zfp_stage_planes(s_words, kThreads, rate);
-    uint32_t* gt = zfp_stage_gt(s_words, kThreads, rate);
-    zfp_gt_fill(gt);
+    const uint32_t wb = threadIdx.x & ~31u;
     for (uint32_t i0 = blockIdx.x * kThreads; i0 < n; i0 += gridDim.x * kThreads) {
         const uint32_t nb = n - i0 < (uint32_t)kThreads ? n - i0 : (uint32_t)kThreads;
         __syncthreads();
         zfp_stage_run(words, i0, nb, rate, s_words);
         __syncthreads();
-        if (threadIdx.x >= nb) continue;
+        if (wb >= nb) continue;
+        const bool mine = threadIdx.x < nb;
         float out[64];
-        zfp_decode_staged(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, out, gt);
-        float4* d4 = reinterpret_cast<float4*>(scratch + (uint64_t)(i0 + threadIdx.x) * 64u);
-#pragma unroll
-        for (int k = 0; k < 16; ++k) d4[k] = make_float4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
+        if (mine) zfp_decode_staged(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, out);
+        zfp_store_warp(pl, out, mine, scratch + (uint64_t)(i0 + wb) * 64u, nb - wb);
     }
 }
 

@@ -557,27 +557,25 @@ __global__ void __launch_bounds__(kAssignThreads) k_assign(QueryState* q, Assign
 // ---------------------------------------------------------------------------
 constexpr int kDecodeNewThreads = 128;
 
-__global__ void __launch_bounds__(kDecodeNewThreads) k_decode_new(const QueryState* q, DecodeArgs a)
+__global__ void __launch_bounds__(kDecodeNewThreads, 5) k_decode_new(const QueryState* q, DecodeArgs a)
 {
     if (q->num_active == 0 || q->grow_needed) return;
     const uint32_t n = q->num_new < a.stage_blocks ? q->num_new : a.stage_blocks;
     extern __shared__ __align__(16) uint32_t s_words[];
     const uint32_t rate = a.max_bits / 64u;
     uint32_t* pl = zfp_stage_planes(s_words, kDecodeNewThreads, rate);
-    uint32_t* gt = zfp_stage_gt(s_words, kDecodeNewThreads, rate);
-    zfp_gt_fill(gt);
     if (threadIdx.x < 4) s_words[kDecodeNewThreads * 2u * rate + threadIdx.x] = 0u;
+    const uint32_t wb = threadIdx.x & ~31u;
     for (uint32_t i0 = blockIdx.x * kDecodeNewThreads; i0 < n; i0 += gridDim.x * kDecodeNewThreads) {
         const uint32_t i = i0 + threadIdx.x;
         __syncthreads();
         if (i < n) zfp_stage_block(a.words, a.new_ids[i], rate, s_words);
         __syncthreads();
-        if (i >= n) continue;
+        if (i0 + wb >= n) continue;  // the whole warp
+        const bool mine = i < n;
         float v[64];
-        zfp_decode_staged(s_words + threadIdx.x * 2u * rate, a.max_bits, pl, v, gt);
-        float4* d4 = reinterpret_cast<float4*>(a.stage + (uint64_t)i * 64u);
-#pragma unroll
-        for (int k = 0; k < 16; ++k) d4[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+        if (mine) zfp_decode_staged(s_words + threadIdx.x * 2u * rate, a.max_bits, pl, v);
+        zfp_store_warp(pl, v, mine, a.stage + (uint64_t)(i0 + wb) * 64u, n - (i0 + wb));
     }
 }
 

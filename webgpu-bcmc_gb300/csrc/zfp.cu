@@ -10,7 +10,7 @@ namespace bcmc {
 // from there (zfp_decode_staged).  Loop bounds are uniform across the CTA
 // (the staging is followed by a barrier).
 constexpr int kDecThreads = 128;
-constexpr int kDeposit = 0;  // 8x8 bit-transposed deposit
+constexpr int kDecPerSm = 5;  // 96 registers: measured faster than 4 CTAs per SM at 128
 
 __device__ __forceinline__ uint32_t* stage_words() { extern __shared__ __align__(16) uint32_t s_dyn[]; return s_dyn; }
 
@@ -24,14 +24,12 @@ __device__ __forceinline__ void store_block(float* __restrict__ dst, const float
 // zfp_compute_block_range.comp:19-61: min/max over the voxels of each block
 // that lie inside the volume (partial blocks at the +x/+y/+z faces are
 // clipped), starting from (1e20, -1e20).
-__global__ void __launch_bounds__(kDecThreads) k_block_ranges(const uint64_t* __restrict__ words, uint3 dims, uint3 nb,
+__global__ void __launch_bounds__(kDecThreads, kDecPerSm) k_block_ranges(const uint64_t* __restrict__ words, uint3 dims, uint3 nb,
                                                               uint32_t rate, uint64_t ranged,
                                                               float2* __restrict__ ranges)
 {
     uint32_t* s_words = stage_words();
     uint32_t* pl = zfp_stage_planes(s_words, kDecThreads, rate);
-    uint32_t* gt = zfp_stage_gt(s_words, kDecThreads, rate);
-    zfp_gt_fill(gt);
     const uint64_t nblocks = (uint64_t)nb.x * nb.y * nb.z;
     for (uint64_t b0 = (uint64_t)blockIdx.x * kDecThreads; b0 < nblocks; b0 += (uint64_t)gridDim.x * kDecThreads) {
         const uint32_t n = (uint32_t)(nblocks - b0 < (uint64_t)kDecThreads ? nblocks - b0 : (uint64_t)kDecThreads);
@@ -45,7 +43,7 @@ __global__ void __launch_bounds__(kDecThreads) k_block_ranges(const uint64_t* __
             continue;
         }
         float v[64];
-        zfp_decode_staged<kDeposit>(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, v, gt);
+        zfp_decode_staged(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, v);
         const uint32_t bx = (uint32_t)(b % nb.x), by = (uint32_t)((b / nb.x) % nb.y),
                        bz = (uint32_t)(b / ((uint64_t)nb.x * nb.y));
         const uint32_t px = min(dims.x - 4u * bx, 4u), py = min(dims.y - 4u * by, 4u),
@@ -68,15 +66,13 @@ __global__ void __launch_bounds__(kDecThreads) k_block_ranges(const uint64_t* __
 }
 
 // zfp_decompress_block.comp:29-39: decode ids[i] into its cache slot.
-__global__ void __launch_bounds__(kDecThreads) k_decode_blocks(const uint64_t* __restrict__ words, uint32_t rate,
+__global__ void __launch_bounds__(kDecThreads, kDecPerSm) k_decode_blocks(const uint64_t* __restrict__ words, uint32_t rate,
                                                                const uint32_t* __restrict__ ids, uint32_t n,
                                                                const int32_t* __restrict__ item_slots,
                                                                float* __restrict__ cache)
 {
     uint32_t* s_words = stage_words();
     uint32_t* pl = zfp_stage_planes(s_words, kDecThreads, rate);
-    uint32_t* gt = zfp_stage_gt(s_words, kDecThreads, rate);
-    zfp_gt_fill(gt);
     if (threadIdx.x < 4) s_words[kDecThreads * 2u * rate + threadIdx.x] = 0u;
     for (uint32_t i0 = blockIdx.x * kDecThreads; i0 < n; i0 += gridDim.x * kDecThreads) {
         const uint32_t i = i0 + threadIdx.x;
@@ -91,27 +87,27 @@ __global__ void __launch_bounds__(kDecThreads) k_decode_blocks(const uint64_t* _
         __syncthreads();
         if (slot < 0) continue;  // not cached: nothing to decode into
         float v[64];
-        zfp_decode_staged<kDeposit>(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, v, gt);
+        zfp_decode_staged(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, v);
         store_block(cache + (uint64_t)slot * 64u, v);
     }
 }
 
-__global__ void __launch_bounds__(kDecThreads) k_decode_volume(const uint64_t* __restrict__ words, uint64_t nblocks,
+__global__ void __launch_bounds__(kDecThreads, kDecPerSm) k_decode_volume(const uint64_t* __restrict__ words, uint64_t nblocks,
                                                                uint32_t rate, float* __restrict__ out)
 {
     uint32_t* s_words = stage_words();
     uint32_t* pl = zfp_stage_planes(s_words, kDecThreads, rate);
-    uint32_t* gt = zfp_stage_gt(s_words, kDecThreads, rate);
-    zfp_gt_fill(gt);
+    const uint32_t wb = threadIdx.x & ~31u;  // the warp's first block in the run
     for (uint64_t b0 = (uint64_t)blockIdx.x * kDecThreads; b0 < nblocks; b0 += (uint64_t)gridDim.x * kDecThreads) {
         const uint32_t n = (uint32_t)(nblocks - b0 < (uint64_t)kDecThreads ? nblocks - b0 : (uint64_t)kDecThreads);
         __syncthreads();
         zfp_stage_run(words, b0, n, rate, s_words);
         __syncthreads();
-        if (threadIdx.x >= n) continue;
+        if (wb >= n) continue;  // the whole warp
+        const bool mine = threadIdx.x < n;
         float v[64];
-        zfp_decode_staged<kDeposit>(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, v, gt);
-        store_block(out + (b0 + threadIdx.x) * 64u, v);
+        if (mine) zfp_decode_staged(s_words + threadIdx.x * 2u * rate, 64u * rate, pl, v);
+        zfp_store_warp(pl, v, mine, out + (b0 + wb) * 64u, n - wb);
     }
 }
 

@@ -8,11 +8,11 @@
 // 2^(emax-30) (:378-382).  Bit offsets are 64-bit (the reference multiplies
 // block_index*max_bits in 32 bits, :199, which wraps past 2^32 bits).
 //
-// The GB300 decoder stages each block's words in shared memory and reads them
-// through a 64-bit window of 32-bit funnel shifts; the group tests are taken 8
-// bits per step through a 512-entry state table in shared memory (or a unary
-// run per find-first-set where there is no shared memory), and the bit planes
-// become coefficients through 8x8 bit transposes (see "Staged decoder").
+// The GB300 decoder stages each block's words in shared memory, parses them
+// one group test per loop step through a 64-bit window with both outcomes
+// computed by selects (lanes stay converged), and turns the bit planes into
+// coefficients with three delta-swap stages over 8-plane chunks (see "Staged
+// decoder").
 #pragma once
 
 #include <stdint.h>
@@ -84,342 +84,193 @@ __device__ __forceinline__ float zfp_inv_weight(int32_t emax)
 // memory (coalesced loads by the CTA for runs of consecutive blocks, or one
 // block per thread), then parsed there.
 //
-// The parse reads the words through a 32-bit window (a funnel shift of two
-// words), takes each plane's raw bits at once and its group tests 8 bits per
-// table step (zfp_parse_planes_gt) or one unary run per find-first-set
-// (zfp_parse_planes), and writes each plane's 64-bit mask to a per-thread
-// scratch; the coefficients are then built from 8-plane chunks with 8x8 bit
-// transposes (kDeposit 0) or shifted in plane by plane (kDeposit 1).  On the
-// 512^3 spectral field at rate 2 (8 planes, 11 group tests and 72 group-test
-// bits per block on average) the table parse takes 268 us against 303 us for
-// the find-first-set parse; a parse flattened into one loop of uniform steps
-// (raw chunk, table step or single bit, branch-free or not), so that lanes do
-// not wait for each other at plane boundaries, measured 296-299 us.
+// Parse (zfp_parse_planes): one loop step per group-test read.  A step loads
+// a 64-bit window at the bit position (three words, two funnel shifts) and
+// computes both outcomes with selects: a 1 (the run of zeros after it found
+// with one find-first-set, clamped by the bit budget and by coefficient 63,
+// decode_ints' two limits) or a 0, which ends the plane and takes the next
+// plane's raw bits from the same window.  Only the plane store and the loop
+// exit branch, so a warp's lanes stay converged although their blocks take
+// different numbers of steps.  A block's leading empty planes (single 0 group
+// tests while nothing is significant) are skipped at once.  On the 512^3
+// spectral field at rate 2 (about 19 steps per block) this took the full
+// decode from 0.390 ms (8-bit group-test table steps, a bit-by-bit tail near
+// the limits, branches per outcome) to 0.257 ms; the branching form of the
+// same step measured 0.333 ms.
+//
+// Deposit (zfp_planes_deposit): the plane masks go to a per-thread row of
+// shared memory; each 8-plane chunk is read back as 8 rows of 64 bits and all
+// eight 8x8 byte columns are transposed at once by three delta-swap stages,
+// after which byte g of row k is coefficient 8g + k's bits of those planes.
 // ---------------------------------------------------------------------------
 
-// Bit window over 32-bit words (LSB first): the 32 bits at the current
-// position are one funnel shift of the two words around it.  The window reads
-// one word past the last bit it consumes, so a block is followed by at least
-// one readable word (staged blocks get padding).
-struct ZfpWindow {
-    const uint32_t* p;  // next word to load
-    uint32_t lo, hi, sh;
-    __device__ __forceinline__ void init(const uint32_t* w)
-    {
-        lo = w[0];
-        hi = w[1];
-        p = w + 2;
-        sh = 0;
-    }
-    __device__ __forceinline__ uint32_t peek() const { return __funnelshift_r(lo, hi, sh); }
-    __device__ __forceinline__ void skip(uint32_t c)  // c <= 32
-    {
-        sh += c;
-        if (sh >= 32u) {
-            sh -= 32u;
-            lo = hi;
-            hi = *p++;
-        }
-    }
-};
-
-__device__ __forceinline__ uint32_t zfp_mask32(uint32_t m) { return m >= 32u ? 0xffffffffu : (1u << m) - 1u; }
-
-// decode_ints' bit planes (zfp_decompress.comp:265-294) as masks: plane 31 - r
-// at pl[2r] (coefficients 0..31) and pl[2r + 1] (32..63).  Returns the number
-// of planes decoded.  Per plane: the raw bits of the n coefficients already
-// significant, then group tests, each a 1 followed by the run of zeros before
-// the next significant coefficient (one find-first-set in the common case) or
-// a 0 that ends the plane.
-__device__ __forceinline__ uint32_t zfp_parse_planes(ZfpWindow& rd, uint32_t budget, uint32_t* pl)
+// PTX shifts clamp the count: a shift by 32 or more gives 0 (the host
+// branch states the same for host builds of this header)
+__device__ __forceinline__ uint32_t zfp_shl(uint32_t x, uint32_t s)
 {
-    uint32_t bits = budget, n = 0, r = 0;
-    for (; r < 32u && bits != 0; ++r) {
-        const uint32_t m = n < bits ? n : bits;
-        bits -= m;
-        uint32_t xlo, xhi = 0;
-        if (m <= 32u) {
-            xlo = rd.peek() & zfp_mask32(m);
-            rd.skip(m);
-        } else {
-            xlo = rd.peek();
-            rd.skip(32);
-            xhi = rd.peek() & zfp_mask32(m - 32u);
-            rd.skip(m - 32u);
+#ifdef __CUDA_ARCH__
+    uint32_t r;
+    asm("shl.b32 %0, %1, %2;" : "=r"(r) : "r"(x), "r"(s));
+    return r;
+#else
+    return s >= 32u ? 0u : x << s;
+#endif
+}
+__device__ __forceinline__ uint32_t zfp_shr(uint32_t x, uint32_t s)
+{
+#ifdef __CUDA_ARCH__
+    uint32_t r;
+    asm("shr.b32 %0, %1, %2;" : "=r"(r) : "r"(x), "r"(s));
+    return r;
+#else
+    return s >= 32u ? 0u : x >> s;
+#endif
+}
+
+// decode_ints' bit planes (zfp_decompress.comp:265-294) as masks.  `w`: the
+// block's words (LSB first), readable for two words past the block; `pos`:
+// the first bit after the header.  Plane r (bit 31 - r of the coefficients)
+// goes to pl[2(r - r0)] (coefficients 0..31) and pl[2(r - r0) + 1] (32..63),
+// where *r0 is the number of leading empty planes, which are not stored.
+// Returns the number of planes decoded, r0 included.
+//
+// A 64-bit window suffices: a run after a group test needs bits 1..63 (one
+// that would reach bit 64 is cut at 63 coefficients first), raw bits after a
+// group test number at most 63 (n < 64 there), and 64 raw bits are read only
+// where no group test is (n = 64).
+__device__ __forceinline__ uint32_t zfp_parse_planes(const uint32_t* w, uint32_t pos, uint32_t budget, uint32_t* pl,
+                                                     uint32_t* r0p)
+{
+    uint32_t bits = budget, n = 0, xlo = 0, xhi = 0, a0, a1;
+    a0 = __funnelshift_r(w[pos >> 5], w[(pos >> 5) + 1], pos & 31u);
+    const uint32_t r0 = min(a0 ? (uint32_t)__ffs(a0) - 1u : 32u, bits);
+    pos += r0;
+    bits -= r0;
+    *r0p = r0;
+    uint32_t r = r0;
+    if (r == 32u || bits == 0u) return r;
+    pl -= 2u * r0;
+    for (;;) {
+        const uint32_t i = pos >> 5, sh = pos & 31u;
+        const uint32_t w0 = w[i], w1 = w[i + 1], w2 = w[i + 2];
+        a0 = __funnelshift_r(w0, w1, sh);
+        a1 = __funnelshift_r(w1, w2, sh);
+        const uint32_t b0 = __funnelshift_r(a0, a1, 1), b1 = a1 >> 1;  // window bits 1..63
+        const bool gtr = n < 64u && bits != 0u;  // a group test is read
+        const bool one = gtr && (a0 & 1u);
+        // a 1: t zeros before the next one (63: none within the window)
+        const uint32_t t = b0 ? (uint32_t)__ffs(b0) - 1u : (b1 ? (uint32_t)__ffs(b1) + 31u : 63u);
+        const uint32_t lim = min(63u - n, bits - 1u);
+        const uint32_t z = min(t, lim), hit = t < lim ? 1u : 0u;
+        const uint32_t nt = n + z;  // the coefficient that becomes significant
+        // a 0 (or no read): the plane ends; the next plane's raw bits follow
+        const uint32_t o = gtr ? 1u : 0u, be = bits - o, m = min(n, be);
+        if (!one) {
+            pl[2 * r] = xlo;
+            pl[2 * r + 1] = xhi;
+            ++r;
+            if (r == 32u || be == 0u) break;
         }
-        while (n < 64u && bits != 0) {
-            const uint32_t W = rd.peek();
-            --bits;
-            if (!(W & 1u)) {
-                rd.skip(1);
-                break;
-            }
-            const uint32_t limit = min(63u - n, bits);
-            const uint32_t Z = W >> 1;
-            const uint32_t tz = (uint32_t)__ffs(Z) - 1u;  // 0xffffffff when Z == 0
-            uint32_t z;
-            if (Z != 0u && tz < limit) {  // the next one is within this window
-                rd.skip(tz + 2u);
-                bits -= tz + 1u;
-                z = tz;
-            } else {  // a longer run, or one that reaches the limit
-                rd.skip(1);
-                z = 0;
-                bool hit = false;
-                while (z < limit) {
-                    const uint32_t V = rd.peek();
-                    const uint32_t rem = limit - z;
-                    const uint32_t t = (uint32_t)__ffs(V) - 1u;
-                    if (V != 0u && t < rem) {
-                        rd.skip(t + 1u);
-                        z += t;
-                        hit = true;
-                        break;
-                    }
-                    const uint32_t step = rem < 32u ? rem : 32u;
-                    rd.skip(step);
-                    z += step;
-                }
-                bits -= z + (hit ? 1u : 0u);
-            }
-            n += z;
-            if (n < 32u) xlo |= 1u << n;
-            else xhi |= 1u << (n - 32u);
-            ++n;
-        }
-        pl[2 * r] = xlo;
-        pl[2 * r + 1] = xhi;
+        const uint32_t c0 = gtr ? b0 : a0, c1 = gtr ? b1 : a1;
+        const uint32_t rlo = c0 & (zfp_shl(1u, m) - 1u), rhi = c1 & zfp_shr(0xffffffffu, 64u - m);
+        const uint32_t tlo = xlo | zfp_shl(1u, nt), thi = xhi | zfp_shl(1u, nt - 32u);
+        xlo = one ? tlo : rlo;
+        xhi = one ? thi : rhi;
+        const uint32_t adv = one ? 1u + z + hit : o + m;
+        pos += adv;
+        bits -= adv;
+        n = one ? nt + 1u : n;
     }
     return r;
 }
 
-// Group-test step table.  A plane's group tests read as a two-state machine
-// over its bits: in state 0 the next bit is a group test (0 ends the plane,
-// 1 enters state 1); in state 1 each bit is the next coefficient's (1: it
-// becomes significant, back to state 0).  Entry (state << 8 | b) is what the
-// 8 bits b do from `state`, as long as neither the bit budget nor coefficient
-// 63 (whose run decode_ints does not read) falls among them:
-//   bits 0-3  bits consumed (1..8; fewer when the plane ends)
-//   bits 4-7  coefficients passed (0..8)
-//   bits 8-15 which of those became significant (bit i: the i-th passed)
-//   bit 16    the plane ended
-//   bit 17    the state after the last bit consumed
-__host__ __device__ constexpr uint32_t zfp_gt_entry(uint32_t idx)
+// delta swap: the bits of a at (mask << s) exchange with the bits of b at mask
+__device__ __forceinline__ void zfp_dswap(uint32_t& a, uint32_t& b, uint32_t s, uint32_t mask)
 {
-    uint32_t s = (idx >> 8) & 1u, dn = 0, mask = 0, c = 0, end = 0;
-    while (c < 8u) {
-        const uint32_t b = (idx >> c) & 1u;
-        ++c;
-        if (s == 0u) {
-            if (!b) {
-                end = 1;
-                break;
-            }
-            s = 1;
-        } else {
-            if (b) {
-                mask |= 1u << dn;
-                s = 0;
-            }
-            ++dn;
-        }
+    const uint32_t t = ((a >> s) ^ b) & mask;
+    b ^= t;
+    a ^= t << s;
+}
+
+// Rows of stored planes 8c .. 8c + 7 (row j = stored plane 8c + 7 - j, zero
+// past `np`), transposed: byte g of row k is then coefficient 8g + k's bits
+// of those planes, the first at bit 7.
+__device__ __forceinline__ void zfp_chunk(const uint32_t* pl, uint32_t c, uint32_t np, uint32_t* L, uint32_t* H)
+{
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const uint4 v = reinterpret_cast<const uint4*>(pl + 16u * c)[q];
+        const uint32_t p0 = 8u * c + 2u * (uint32_t)q;
+        L[7 - 2 * q] = p0 < np ? v.x : 0u;
+        H[7 - 2 * q] = p0 < np ? v.y : 0u;
+        L[6 - 2 * q] = p0 + 1u < np ? v.z : 0u;
+        H[6 - 2 * q] = p0 + 1u < np ? v.w : 0u;
     }
-    return c | (dn << 4) | (mask << 8) | (end << 16) | (s << 17);
-}
-
-constexpr uint32_t kZfpGtWords = 512;
-struct ZfpGtTable {
-    uint32_t v[kZfpGtWords];
-};
-constexpr ZfpGtTable zfp_make_gt()
-{
-    ZfpGtTable t{};
-    for (uint32_t i = 0; i < kZfpGtWords; ++i) t.v[i] = zfp_gt_entry(i);
-    return t;
-}
-// built at compile time; a CTA copies it into shared memory (zfp_gt_fill)
-static __device__ const ZfpGtTable g_zfp_gt = zfp_make_gt();
-static_assert(zfp_make_gt().v[0] == (1u | (1u << 16)), "state 0, bit 0 clear: the plane ends after one bit");
-static_assert(zfp_make_gt().v[256] == (8u | (8u << 4) | (1u << 17)), "state 1, eight zeros: a run continues");
-
-// The CTA's threads copy the table into shared memory; the caller
-// synchronises before use.
-__device__ __forceinline__ void zfp_gt_fill(uint32_t* gt)
-{
-    for (uint32_t i = threadIdx.x; i < kZfpGtWords; i += blockDim.x) gt[i] = g_zfp_gt.v[i];
-}
-
-// zfp_parse_planes with the group tests taken 8 bits per table step: a step
-// is taken when it consumes no more bits than the budget has left and passes
-// coefficients below 63 only (each of its reads then happens in decode_ints
-// too); otherwise, and for the plane's remaining bits, one bit at a time with
-// decode_ints' limits (at coefficient 63 or an empty budget a run ends
-// without a read and marks the coefficient).
-__device__ __forceinline__ uint32_t zfp_parse_planes_gt(ZfpWindow& rd, uint32_t budget, uint32_t* pl,
-                                                        const uint32_t* gt)
-{
-    uint32_t bits = budget, n = 0, r = 0;
-    for (; r < 32u && bits != 0; ++r) {
-        const uint32_t m = n < bits ? n : bits;
-        bits -= m;
-        uint64_t x;
-        if (m <= 32u) {
-            x = rd.peek() & zfp_mask32(m);
-            rd.skip(m);
-        } else {
-            x = rd.peek();
-            rd.skip(32);
-            x |= (uint64_t)(rd.peek() & zfp_mask32(m - 32u)) << 32;
-            rd.skip(m - 32u);
-        }
-        uint32_t s = 0;
-        bool ended = false;
-        for (;;) {
-            const uint32_t e = gt[(s << 8) | (rd.peek() & 255u)];
-            const uint32_t c = e & 15u, dn = (e >> 4) & 15u;
-            if (c > bits || n + dn > 63u) break;
-            rd.skip(c);
-            bits -= c;
-            x |= (uint64_t)((e >> 8) & 255u) << n;
-            n += dn;
-            s = (e >> 17) & 1u;
-            if (e & 0x10000u) {
-                ended = true;
-                break;
-            }
-        }
-        if (!ended) {
-            for (;;) {
-                if (s == 0u) {
-                    if (n >= 64u || bits == 0u) break;
-                    --bits;
-                    const uint32_t b = rd.peek() & 1u;
-                    rd.skip(1);
-                    if (!b) break;
-                    s = 1;
-                } else {
-                    if (n < 63u && bits != 0u) {
-                        --bits;
-                        const uint32_t b = rd.peek() & 1u;
-                        rd.skip(1);
-                        if (!b) {
-                            ++n;
-                            continue;
-                        }
-                    }
-                    x |= 1ull << n;
-                    ++n;
-                    s = 0;
-                }
-            }
-        }
-        pl[2 * r] = (uint32_t)x;
-        pl[2 * r + 1] = (uint32_t)(x >> 32);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        zfp_dswap(L[j], L[j + 4], 4, 0x0F0F0F0Fu);
+        zfp_dswap(H[j], H[j + 4], 4, 0x0F0F0F0Fu);
     }
-    return r;
-}
-
-// 8x8 bit transpose of the 64-bit matrix (hi:lo), row = byte, column = bit
-// (three delta swaps)
-__device__ __forceinline__ void zfp_transpose8(uint32_t& lo, uint32_t& hi)
-{
-    uint32_t t;
-    t = (lo ^ (lo >> 7)) & 0x00AA00AAu;
-    lo ^= t ^ (t << 7);
-    t = (hi ^ (hi >> 7)) & 0x00AA00AAu;
-    hi ^= t ^ (t << 7);
-    t = (lo ^ (lo >> 14)) & 0x0000CCCCu;
-    lo ^= t ^ (t << 14);
-    t = (hi ^ (hi >> 14)) & 0x0000CCCCu;
-    hi ^= t ^ (t << 14);
-    t = (lo ^ __funnelshift_r(lo, hi, 28)) & 0xF0F0F0F0u;
-    lo ^= t;
-    hi ^= t >> 4;
-}
-
-// Coefficients (stream order) from the plane masks: each 8-plane chunk is cut
-// into eight 8x8 bit matrices (byte g of planes 8c..8c+7), transposed, and
-// each result byte is coefficient 8g + i's bits of those planes.
-__device__ __forceinline__ void zfp_planes_transposed(const uint32_t* pl, uint32_t planes, uint32_t* u)
-{
 #pragma unroll
-    for (int i = 0; i < 64; ++i) u[i] = 0;
-    for (uint32_t c = 0; c * 8u < planes; ++c) {
-        uint32_t w[16];  // planes 8c .. 8c+7: lo, hi
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const uint4 v = reinterpret_cast<const uint4*>(pl + 16u * c)[q];
-            w[4 * q] = v.x;
-            w[4 * q + 1] = v.y;
-            w[4 * q + 2] = v.z;
-            w[4 * q + 3] = v.w;
+    for (int j = 0; j < 8; ++j)
+        if ((j & 2) == 0) {
+            zfp_dswap(L[j], L[j + 2], 2, 0x33333333u);
+            zfp_dswap(H[j], H[j + 2], 2, 0x33333333u);
         }
 #pragma unroll
-        for (int r = 0; r < 8; ++r)
-            if (8u * c + (uint32_t)r >= planes) w[2 * r] = w[2 * r + 1] = 0u;
-        const uint32_t rs = 8u * c;  // bit j of a result byte is plane 24 - 8c + j: (byte << 24) >> 8c
-#pragma unroll
-        for (int g = 0; g < 8; ++g) {
-            const int h = g >> 2;
-            const uint32_t sb = (uint32_t)(g & 3);
-            const uint32_t sel = sb | ((sb + 4u) << 4);
-            // matrix byte j = byte g of plane 7 - j (lo word: planes 7..4, hi word: planes 3..0)
-            const uint32_t a = __byte_perm(w[14 + h], w[12 + h], sel);
-            const uint32_t b = __byte_perm(w[10 + h], w[8 + h], sel);
-            const uint32_t d = __byte_perm(w[6 + h], w[4 + h], sel);
-            const uint32_t e = __byte_perm(w[2 + h], w[0 + h], sel);
-            uint32_t lo = __byte_perm(a, b, 0x5410u), hi = __byte_perm(d, e, 0x5410u);
-            zfp_transpose8(lo, hi);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                u[8 * g + i] |= __byte_perm(lo, 0u, 0x0444u | ((uint32_t)i << 12)) >> rs;
-                u[8 * g + 4 + i] |= __byte_perm(hi, 0u, 0x0444u | ((uint32_t)i << 12)) >> rs;
-            }
-        }
+    for (int j = 0; j < 8; j += 2) {
+        zfp_dswap(L[j], L[j + 1], 1, 0x55555555u);
+        zfp_dswap(H[j], H[j + 1], 1, 0x55555555u);
     }
 }
 
-// The same by shifting each plane into the 64 accumulators.
-__device__ __forceinline__ void zfp_planes_shifted(const uint32_t* pl, uint32_t planes, uint32_t* u)
+// Coefficients (stream order) from the stored planes r0 .. planes - 1: chunk
+// c's byte of a coefficient goes to bits 31 - r0 - 8c down to 24 - r0 - 8c.
+__device__ __forceinline__ void zfp_planes_deposit(const uint32_t* pl, uint32_t planes, uint32_t r0, uint32_t* u)
 {
+    const uint32_t np = planes - r0;
+    {
+        uint32_t L[8], H[8];
+        zfp_chunk(pl, 0u, np, L, H);
 #pragma unroll
-    for (int i = 0; i < 64; ++i) u[i] = 0;
-    for (uint32_t r = 0; r < planes; ++r) {
-        const uint32_t lo = pl[2 * r], hi = pl[2 * r + 1];
+        for (int k = 0; k < 8; ++k)
 #pragma unroll
-        for (int i = 0; i < 32; ++i) u[i] = (u[i] << 1) | ((lo >> i) & 1u);
-#pragma unroll
-        for (int i = 0; i < 32; ++i) u[32 + i] = (u[32 + i] << 1) | ((hi >> i) & 1u);
+            for (int g = 0; g < 4; ++g) {
+                u[8 * g + k] = __byte_perm(L[k], 0u, 0x0444u | ((uint32_t)g << 12)) >> r0;
+                u[8 * (g + 4) + k] = __byte_perm(H[k], 0u, 0x0444u | ((uint32_t)g << 12)) >> r0;
+            }
     }
-    const uint32_t rest = 32u - planes;
+    for (uint32_t c = 1; c * 8u < np; ++c) {
+        uint32_t L[8], H[8];
+        zfp_chunk(pl, c, np, L, H);
+        const uint32_t rs = 8u * c + r0;
 #pragma unroll
-    for (int i = 0; i < 64; ++i) u[i] = rest >= 32u ? 0u : u[i] << rest;
+        for (int k = 0; k < 8; ++k)
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+                u[8 * g + k] |= __byte_perm(L[k], 0u, 0x0444u | ((uint32_t)g << 12)) >> rs;
+                u[8 * (g + 4) + k] |= __byte_perm(H[k], 0u, 0x0444u | ((uint32_t)g << 12)) >> rs;
+            }
+    }
 }
 
 // One block from its words `w` (2 * rate 32-bit words, 64 * rate bits; staged
-// in shared memory, or in place in global memory), readable for one word past
-// the block.  `pl` is the thread's plane scratch: 64 words, 16-byte aligned
-// (in shared memory, or a thread-local array).  `gt`: the CTA's group-test
-// step table (zfp_gt_fill), or null for the find-first-set parse (decoders
-// without shared memory).
-template <int kDeposit = 0>
-__device__ __forceinline__ void zfp_decode_staged(const uint32_t* w, uint32_t max_bits, uint32_t* pl, float* out,
-                                                  const uint32_t* gt = nullptr)
+// in shared memory, or in place in global memory), readable for two words
+// past the block.  `pl` is the thread's plane scratch: 64 words, 16-byte
+// aligned (a row of shared memory, or a thread-local array).
+__device__ __forceinline__ void zfp_decode_staged(const uint32_t* w, uint32_t max_bits, uint32_t* pl, float* out)
 {
-    ZfpWindow rd;
-    rd.init(w);
-    const uint32_t h = rd.peek();
+    const uint32_t h = w[0];
     if (!(h & 1u)) {
 #pragma unroll
         for (int i = 0; i < 64; ++i) out[i] = 0.0f;
         return;
     }
     const int32_t emax = (int32_t)((h >> 1) & 255u) - 127;
-    rd.skip(9);
+    uint32_t r0;
+    const uint32_t planes = zfp_parse_planes(w, 9u, max_bits - 9u, pl, &r0);
     uint32_t u[64];
-    const uint32_t planes = gt ? zfp_parse_planes_gt(rd, max_bits - 9u, pl, gt) : zfp_parse_planes(rd, max_bits - 9u, pl);
-    if (kDeposit == 0) zfp_planes_transposed(pl, planes, u);
-    else zfp_planes_shifted(pl, planes, u);
+    zfp_planes_deposit(pl, planes, r0, u);
     int32_t v[64];
     uint32_t un[64];
     BCMC_ZFP_GATHER(un, u)
@@ -432,9 +283,10 @@ __device__ __forceinline__ void zfp_decode_staged(const uint32_t* w, uint32_t ma
 }
 
 // Shared memory of a staged decode CTA of `threads` threads at `rate`: the
-// staged words (2 * rate per block, 4 words of padding), 68 words of plane
-// scratch per thread (64 used; 68 keeps the threads' 16-byte rows apart) and
-// the group-test step table.
+// staged words (2 * rate per block, 4 words of padding) and 68 words of plane
+// scratch per thread (64 used; 68 keeps the threads' 16-byte rows on
+// different banks).  A thread's row also holds its decoded block for the
+// warp's coalesced store (zfp_store_warp).
 constexpr uint32_t kZfpPlaneWords = 68;
 __host__ __device__ __forceinline__ uint32_t zfp_stage_words(uint32_t threads, uint32_t rate)
 {
@@ -442,15 +294,37 @@ __host__ __device__ __forceinline__ uint32_t zfp_stage_words(uint32_t threads, u
 }
 __host__ __device__ __forceinline__ size_t zfp_stage_smem(uint32_t threads, uint32_t rate)
 {
-    return ((size_t)zfp_stage_words(threads, rate) + (size_t)threads * kZfpPlaneWords + kZfpGtWords) * 4u;
+    return ((size_t)zfp_stage_words(threads, rate) + (size_t)threads * kZfpPlaneWords) * 4u;
 }
 __device__ __forceinline__ uint32_t* zfp_stage_planes(uint32_t* s_words, uint32_t threads, uint32_t rate)
 {
     return s_words + zfp_stage_words(threads, rate) + threadIdx.x * kZfpPlaneWords;
 }
-__device__ __forceinline__ uint32_t* zfp_stage_gt(uint32_t* s_words, uint32_t threads, uint32_t rate)
+
+// The warp's decoded blocks to out[k * 64 ..] for the warp's k-th block,
+// k < count, with coalesced 16-byte stores: each thread writes its block into
+// its own row (`row`, from zfp_stage_planes), then the warp stores two blocks
+// per instruction.  Every lane of the warp calls it (a lane without a block
+// passes nothing to write: `v` is not read when has_block is false).
+__device__ __forceinline__ void zfp_store_warp(uint32_t* row, const float* v, bool has_block, float* out,
+                                               uint32_t count)
 {
-    return s_words + zfp_stage_words(threads, rate) + threads * kZfpPlaneWords;
+    if (has_block) {
+        float4* r4 = reinterpret_cast<float4*>(row);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) r4[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+    }
+    __syncwarp();
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t* row0 = row - lane * kZfpPlaneWords;
+#pragma unroll
+    for (uint32_t k = 0; k < 16; ++k) {
+        const uint32_t blk = 2u * k + (lane >> 4);
+        if (blk < count)
+            reinterpret_cast<float4*>(out + (uint64_t)blk * 64u)[lane & 15u] =
+                *reinterpret_cast<const float4*>(row0 + blk * kZfpPlaneWords + 4u * (lane & 15u));
+    }
+    __syncwarp();
 }
 
 // Copies the words of blocks b0 .. b0+nb-1 (consecutive) to s_words with
