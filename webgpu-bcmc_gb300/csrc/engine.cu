@@ -397,10 +397,12 @@ __global__ void __launch_bounds__(16 * kBmcBlocks, kBmcThreadsPerSm / (16 * kBmc
     const uint32_t rank = s_rank;
     const uint32_t range = div_up(div_up(A, G), kBmcBlocks) * kBmcBlocks;
     const uint32_t start = min(A, rank * range), end = min(A, start + range);
+    // ranks 0 .. worked - 1 own entries; the others take part in no look-back
+    const uint32_t worked = div_up(A, range);
     for (uint32_t i = t; i < 256u; i += kBmcThreads)
         reinterpret_cast<uint4*>(&s_te[0][0])[i] = reinterpret_cast<const uint4*>(&c_tri.corners[0][0])[i];
     if (t < 16) reinterpret_cast<uint4*>(s_cnt)[t] = reinterpret_cast<const uint4*>(c_tri.count)[t];
-    if (t == 0) s_cta_v = s_cta_b = 0;
+    if (t == 0) s_cta_v = s_cta_b = s_pv = s_pb = 0;
     if (t < 61) s_gdesc[t] = ghost_desc(c_ghost[t]);
     if (t < 32) {
         uint32_t w = 0, ws = 0;
@@ -555,7 +557,7 @@ __global__ void __launch_bounds__(16 * kBmcBlocks, kBmcThreadsPerSm / (16 * kBmc
         }
     }
     __syncthreads();
-    if (t < 64) {
+    if (t < 64 && rank < worked) {
         if (t < 32) {
             const uint32_t p = warp_lookback(a.status_v, rank, s_cta_v, epoch, &st->error, 61u);
             if (t == 0) s_pv = p;
@@ -563,7 +565,7 @@ __global__ void __launch_bounds__(16 * kBmcBlocks, kBmcThreadsPerSm / (16 * kBmc
             const uint32_t p = warp_lookback(a.status_b, rank, s_cta_b, epoch, &st->error, 64u);
             if (t == 32) {
                 s_pb = p;
-                if (rank == G - 1) st->with_verts = p + s_cta_b;
+                if (rank == worked - 1) st->with_verts = p + s_cta_b;
             }
         }
     }

@@ -646,10 +646,14 @@ __global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McAr
     const uint32_t rank = s_rank;
     const uint32_t range = div_up(div_up(A, G), kMcBlocks) * kMcBlocks;
     const uint32_t start = min(A, rank * range), end = min(A, start + range);
+    // ranks 0 .. worked - 1 own blocks; the others take part in no look-back
+    // (the walk of the last rank, past every predecessor, would end the kernel)
+    const uint32_t worked = div_up(A, range);
     reinterpret_cast<uint4*>(&s_te[0][0])[t] = reinterpret_cast<const uint4*>(&c_tri.corners[0][0])[t];
     if (t < 16) reinterpret_cast<uint4*>(s_cnt)[t] = reinterpret_cast<const uint4*>(c_tri.count)[t];
     if (t == 0) {
         s_cta_v = s_cta_b = 0;
+        s_pv = s_pb = 0;
         s_cursor = start;
     }
     if (t < 61) s_gdesc[t] = ghost_desc(c_ghost[t]);
@@ -846,18 +850,18 @@ __global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McAr
         }
     }
     __syncthreads();
-    if (t < 64) {
+    if (t < 64 && rank < worked) {
         if (t < 32) {
             const uint32_t p = warp_lookback(a.status_v, rank, s_cta_v, epoch, &q->error, 40u);
             if (t == 0) {
                 s_pv = p;
-                if (rank == G - 1) q->num_verts = p + s_cta_v;
+                if (rank == worked - 1) q->num_verts = p + s_cta_v;
             }
         } else {
             const uint32_t p = warp_lookback(a.status_b, rank, s_cta_b, epoch, &q->error, 41u);
             if (t == 32) {
                 s_pb = p;
-                if (rank == G - 1) q->num_with_verts = p + s_cta_b;
+                if (rank == worked - 1) q->num_with_verts = p + s_cta_b;
             }
         }
     }
