@@ -619,7 +619,8 @@ __global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McAr
     __shared__ float s_vol[kMcBlocks][128];
     __shared__ uint8_t s_rm[kMcBlocks][32];  // corner-row masks of each block (count_cells)
     __shared__ uint32_t s_pair[32], s_pair_sw[32];  // 5-bit row mask -> per-cell corner pairs
-    __shared__ __align__(16) uint8_t s_te[256][16];
+    __shared__ __align__(16) uint16_t s_te[256][16];  // c_tri_edges
+    __shared__ __align__(16) uint32_t s_cp[64 * 8];    // c_corner_pack
     __shared__ __align__(16) uint8_t s_cnt[256];
     __shared__ __align__(16) uint8_t s_case[kMcCells];
     __shared__ uint32_t s_off[kMcCells + 1];
@@ -649,7 +650,9 @@ __global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McAr
     // ranks 0 .. worked - 1 own blocks; the others take part in no look-back
     // (the walk of the last rank, past every predecessor, would end the kernel)
     const uint32_t worked = div_up(A, range);
-    reinterpret_cast<uint4*>(&s_te[0][0])[t] = reinterpret_cast<const uint4*>(&c_tri.corners[0][0])[t];
+    for (uint32_t i = t; i < 512u; i += kMcThreads)
+        reinterpret_cast<uint4*>(&s_te[0][0])[i] = reinterpret_cast<const uint4*>(&c_tri_edges.e[0][0])[i];
+    if (t < 128) reinterpret_cast<uint4*>(s_cp)[t] = reinterpret_cast<const uint4*>(&c_corner_pack.p[0][0])[t];
     if (t < 16) reinterpret_cast<uint4*>(s_cnt)[t] = reinterpret_cast<const uint4*>(c_tri.count)[t];
     if (t == 0) {
         s_cta_v = s_cta_b = 0;
@@ -784,36 +787,9 @@ __global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McAr
 #pragma unroll
             for (uint32_t step = kMcCells / 2; step; step >>= 1)
                 if (s_off[cell + step] <= k) cell += step;
-            const uint32_t ed = s_te[s_case[cell]][k - s_off[cell]];
-            const uint32_t jb = cell >> 6, cc = cell & 63u;
-            const uint32_t x = cc & 3u, y = (cc >> 2) & 3u, z = cc >> 4;
-            const uint32_t o0 = ed & 7u, o1 = ed >> 3;
-            const uint32_t ax = o0 & 1u, ay = (o0 >> 1) & 1u, az = o0 >> 2;
-            const uint32_t bx = o1 & 1u, by = (o1 >> 1) & 1u, bz = o1 >> 2;
-            const float fa = s_vol[jb][(x + ax) + 5u * ((y + ay) + 5u * (z + az))];
-            const float fb = s_vol[jb][(x + bx) + 5u * ((y + by) + 5u * (z + bz))];
-            // lerp_verts (compute_block_vertices.comp:62-74)
-            float tt = 0.0f;
-            if (!(fabsf(__fsub_rn(fa, fb)) < 0.001f)) tt = __fdiv_rn(__fsub_rn(iso, fa), __fsub_rn(fb, fa));
-            uint32_t qx, qy, qz;
-            if (isfinite(tt)) {
-                // edges are axis aligned: along the two fixed axes
-                // a + tt*0 + v + 0.5 is exactly a + v + 0.5, which
-                // quantizes to floor((a + v) * 255.75); only the edge's
-                // own axis needs the f32 arithmetic
-                const uint32_t d = (o0 ^ o1) >> 1;  // 0, 1, 2 = x, y, z
-                const uint32_t ad = (o0 >> d) & 1u, vd = d == 0 ? x : (d == 1 ? y : z);
-                const float pd = __fadd_rn(__fadd_rn(ad ? __fsub_rn(1.0f, tt) : tt, (float)vd), 0.5f);
-                const uint32_t qd = quantize(pd);
-                qx = d == 0 ? qd : (((ax + x) * 1023u) >> 2);
-                qy = d == 1 ? qd : (((ay + y) * 1023u) >> 2);
-                qz = d == 2 ? qd : (((az + z) * 1023u) >> 2);
-            } else {
-                qx = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)ax, __fmul_rn(tt, (float)((int)bx - (int)ax))), (float)x), 0.5f));
-                qy = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)ay, __fmul_rn(tt, (float)((int)by - (int)ay))), (float)y), 0.5f));
-                qz = quantize(__fadd_rn(__fadd_rn(__fadd_rn((float)az, __fmul_rn(tt, (float)((int)bz - (int)az))), (float)z), 0.5f));
-            }
-            out[k] = make_uint2((qx << 20) | (qy << 10) | qz, s_id[jb]);
+            const uint32_t jb = cell >> 6;
+            out[k] = make_uint2(mc_vertex(s_te[s_case[cell]][k - s_off[cell]], cell & 63u, s_vol[jb], s_cp, iso),
+                                s_id[jb]);
         };
         if constexpr (kHost) {
             // into host memory, j = k + shift puts each warp's 32 stores in
