@@ -586,6 +586,7 @@ constexpr int kMcBlocks = 16;
 constexpr int kMcThreads = 256;
 constexpr int kMcCells = 64 * kMcBlocks;  // 4 consecutive cells per thread
 constexpr int kMcPerSm = 6;               // resident CTAs per SM (the grid: one launch, all resident)
+constexpr int kMcMaskWords = kMcCells * 15 / 32;  // a tile holds at most 15 vertices per cell
 
 // Marching cubes over the active blocks, one cooperative launch (every CTA
 // resident).  Each CTA owns one contiguous range of active blocks:
@@ -623,7 +624,10 @@ __global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McAr
     __shared__ __align__(16) uint32_t s_cp[64 * 8];    // c_corner_pack
     __shared__ __align__(16) uint8_t s_cnt[256];
     __shared__ __align__(16) uint8_t s_case[kMcCells];
-    __shared__ uint32_t s_off[kMcCells + 1];
+    __shared__ uint32_t s_cells[kMcCells];          // the tile's cells with vertices in order: cell | first vertex << 16
+    __shared__ uint32_t s_vmask[kMcMaskWords];      // bit k: vertex k of the tile is its cell's first
+    __shared__ uint16_t s_vbase[kMcMaskWords];      // cells with vertices starting before vertex 32w
+    __shared__ uint32_t s_boff[kMcBlocks];          // each block's first vertex in the tile
     __shared__ uint32_t s_id[kMcBlocks];
     __shared__ uint32_t s_slot[kMcBlocks][8];
     __shared__ uint32_t s_act[kMcBlocks];
@@ -778,17 +782,46 @@ __global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McAr
         return sum;
     };
 
-    // the vertices of the tile in shared memory (s_vol, s_case, s_off, s_id),
-    // vertex k of the tile to out[k], out = a.verts + pv
+    // a tile's cases and counts into the emit's tables: one CTA scan gives each
+    // thread's first vertex and first rank among the cells with vertices; each
+    // such cell sets its start bit, takes its place in s_cells and, for the one
+    // 32-vertex word whose first vertex falls in its range (it has at most 15),
+    // records the cells starting before that word (s_vmask is zeroed when the
+    // tile is claimed).  Returns the tile's vertex count; ends with a barrier.
+    auto prep_tile = [&](const uint32_t* nv, const uint32_t cs4, const uint32_t mysum) -> uint32_t {
+        const uint32_t ne = (nv[0] != 0u) + (nv[1] != 0u) + (nv[2] != 0u) + (nv[3] != 0u);
+        uint32_t tot;
+        const uint32_t ex = cta_exclusive_scan<kMcThreads>(mysum | (ne << 16), s_warp, &tot);
+        uint32_t run = ex & 0xffffu, rank = ex >> 16;
+        *reinterpret_cast<uint32_t*>(&s_case[4u * t]) = cs4;
+        if ((t & 15u) == 0u) s_boff[t >> 4] = run;
+        if (t == 0) s_vbase[0] = 0;
+#pragma unroll
+        for (uint32_t x = 0; x < 4; ++x) {
+            if (nv[x]) {
+                atomicOr(&s_vmask[run >> 5], 1u << (run & 31u));
+                s_cells[rank] = (4u * t + x) | (run << 16);
+                const uint32_t w = (run + nv[x]) >> 5;
+                if ((w << 5) > run && w < (uint32_t)kMcMaskWords) s_vbase[w] = (uint16_t)(rank + 1u);
+                ++rank;
+            }
+            run += nv[x];
+        }
+        __syncthreads();
+        return tot & 0xffffu;
+    };
+
+    // the vertices of the tile in shared memory (s_vol, s_case, s_cells,
+    // s_vmask, s_vbase, s_id), vertex k of the tile to out[k], out = a.verts + pv
     auto emit_tile = [&](const uint32_t pv, const uint32_t tile_v) {
         uint2* out = a.verts + pv;
         const auto emit = [&](const uint32_t k) {
-            uint32_t cell = 0;
-#pragma unroll
-            for (uint32_t step = kMcCells / 2; step; step >>= 1)
-                if (s_off[cell + step] <= k) cell += step;
-            const uint32_t jb = cell >> 6;
-            out[k] = make_uint2(mc_vertex(s_te[s_case[cell]][k - s_off[cell]], cell & 63u, s_vol[jb], s_cp, iso),
+            // vertex k's cell: the last cell starting at or before k, counted
+            // through the start bits of k's word
+            const uint32_t w = k >> 5;
+            const uint32_t r = s_vbase[w] + (uint32_t)__popc(s_vmask[w] & (0xffffffffu >> (31u - (k & 31u)))) - 1u;
+            const uint32_t e = s_cells[r], cell = e & 0xffffu, jb = cell >> 6;
+            out[k] = make_uint2(mc_vertex(s_te[s_case[cell]][k - (e >> 16)], cell & 63u, s_vol[jb], s_cp, iso),
                                 s_id[jb]);
         };
         if constexpr (kHost) {
@@ -853,6 +886,7 @@ __global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McAr
         const uint32_t lane = t & 31u;
         for (;;) {
             __syncthreads();
+            for (uint32_t i = t; i < (uint32_t)kMcMaskWords; i += kMcThreads) s_vmask[i] = 0u;
             if (t < 32) {
                 uint32_t cur = s_cursor, filled = 0;
                 while (filled < kMcBlocks && cur < end) {
@@ -884,19 +918,10 @@ __global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McAr
             const uint32_t dims = load_tile();
             uint32_t nv[4], cs4;
             const uint32_t mysum = count_cells(dims, nv, cs4);
-            uint32_t tile_v;
-            uint32_t run = cta_exclusive_scan<kMcThreads>(mysum, s_warp, &tile_v);
-            *reinterpret_cast<uint32_t*>(&s_case[4u * t]) = cs4;
-#pragma unroll
-            for (uint32_t x = 0; x < 4; ++x) {
-                s_off[4u * t + x] = run;
-                run += nv[x];
-            }
-            if (t == 0) s_off[kMcCells] = tile_v;
-            __syncthreads();
+            const uint32_t tile_v = prep_tile(nv, cs4, mysum);
             if (t < n_sel) {
                 a.with_verts[pb + t] = s_idx[t];
-                a.vert_offsets[pb + t] = pv + s_off[64 * t];
+                a.vert_offsets[pb + t] = pv + s_boff[t];
             }
             emit_tile(pv, tile_v);
             pv += tile_v;
@@ -943,6 +968,7 @@ __global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McAr
     for (;;) {
         __syncthreads();
         if (t == 0) s_rank = atomicAdd(&q->tiles_emit, 1u);
+        for (uint32_t i = t; i < (uint32_t)kMcMaskWords; i += kMcThreads) s_vmask[i] = 0u;
         __syncthreads();
         const uint32_t tile = s_rank;
         if (tile >= ntiles) break;
@@ -954,16 +980,7 @@ __global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McAr
         const uint32_t dims = load_tile();
         uint32_t nv[4], cs4;
         const uint32_t mysum = count_cells(dims, nv, cs4);
-        uint32_t tile_v;
-        uint32_t run = cta_exclusive_scan<kMcThreads>(mysum, s_warp, &tile_v);
-        *reinterpret_cast<uint32_t*>(&s_case[4u * t]) = cs4;
-#pragma unroll
-        for (uint32_t x = 0; x < 4; ++x) {
-            s_off[4u * t + x] = run;
-            run += nv[x];
-        }
-        if (t == 0) s_off[kMcCells] = tile_v;
-        __syncthreads();
+        const uint32_t tile_v = prep_tile(nv, cs4, mysum);
         emit_tile(s_pv, tile_v);
     }
 }
