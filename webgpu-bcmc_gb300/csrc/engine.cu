@@ -374,7 +374,10 @@ __global__ void __launch_bounds__(16 * kBmcBlocks, kBmcThreadsPerSm / (16 * kBmc
     __shared__ __align__(16) uint32_t s_cp[64 * 8];    // c_corner_pack
     __shared__ __align__(16) uint8_t s_cnt[256];
     __shared__ __align__(16) uint8_t s_case[kBmcCells];
-    __shared__ uint32_t s_off[kBmcCells + 1];
+    constexpr int kMaskWords = kBmcCells * 15 / 32;  // a tile holds at most 15 vertices per cell
+    __shared__ uint32_t s_cells[kBmcCells];    // the tile's cells with vertices in order: cell | first vertex << 16
+    __shared__ uint32_t s_vmask[kMaskWords];   // bit k: vertex k of the tile is its cell's first
+    __shared__ uint16_t s_vbase[kMaskWords];   // cells with vertices starting before vertex 32w
     __shared__ uint32_t s_id[kBmcBlocks];
     __shared__ uint32_t s_qi[kBmcBlocks];
     __shared__ float s_iso[kBmcBlocks];
@@ -617,6 +620,7 @@ __global__ void __launch_bounds__(16 * kBmcBlocks, kBmcThreadsPerSm / (16 * kBmc
     for (;;) {
         __syncthreads();
         if (t == 0) s_rank = atomicAdd(&st->tiles_emit, 1u);
+        for (uint32_t i = t; i < (uint32_t)kMaskWords; i += kBmcThreads) s_vmask[i] = 0u;
         __syncthreads();
         const uint32_t tile = s_rank;
         if (tile >= ntiles) break;
@@ -637,24 +641,35 @@ __global__ void __launch_bounds__(16 * kBmcBlocks, kBmcThreadsPerSm / (16 * kBmc
         const uint32_t dims = load_tile();
         uint32_t nv[4], cs4;
         const uint32_t mysum = count_cells(dims, nv, cs4);
-        uint32_t tile_v;
-        uint32_t run = cta_exclusive_scan<kBmcThreads>(mysum, s_warp, &tile_v);
+        // the emit's tables (as k_mc's prep_tile): each cell with vertices sets
+        // its start bit, takes its place in s_cells and records, for the one
+        // 32-vertex word whose first vertex falls in its range, the cells
+        // starting before that word
+        const uint32_t ne = (nv[0] != 0u) + (nv[1] != 0u) + (nv[2] != 0u) + (nv[3] != 0u);
+        uint32_t tot;
+        const uint32_t ex = cta_exclusive_scan<kBmcThreads>(mysum | (ne << 16), s_warp, &tot);
+        const uint32_t tile_v = tot & 0xffffu;
+        uint32_t run = ex & 0xffffu, rank = ex >> 16;
         *reinterpret_cast<uint32_t*>(&s_case[4u * t]) = cs4;
+        if (t == 0) s_vbase[0] = 0;
 #pragma unroll
         for (uint32_t x = 0; x < 4; ++x) {
-            s_off[4u * t + x] = run;
+            if (nv[x]) {
+                atomicOr(&s_vmask[run >> 5], 1u << (run & 31u));
+                s_cells[rank] = (4u * t + x) | (run << 16);
+                const uint32_t w = (run + nv[x]) >> 5;
+                if ((w << 5) > run && w < (uint32_t)kMaskWords) s_vbase[w] = (uint16_t)(rank + 1u);
+                ++rank;
+            }
             run += nv[x];
         }
-        if (t == 0) s_off[kBmcCells] = tile_v;
         __syncthreads();
         uint2* out = a.verts + vbase + s_pv;
         for (uint32_t k = t; k < tile_v; k += kBmcThreads) {
-            uint32_t cell = 0;
-#pragma unroll
-            for (uint32_t step = kBmcCells / 2; step; step >>= 1)
-                if (s_off[cell + step] <= k) cell += step;
-            const uint32_t jb = cell >> 6;
-            out[k] = make_uint2(mc_vertex(s_te[s_case[cell]][k - s_off[cell]], cell & 63u, s_vol[jb], s_cp, s_iso[jb]),
+            const uint32_t w = k >> 5;
+            const uint32_t r = s_vbase[w] + (uint32_t)__popc(s_vmask[w] & (0xffffffffu >> (31u - (k & 31u)))) - 1u;
+            const uint32_t e = s_cells[r], cell = e & 0xffffu, jb = cell >> 6;
+            out[k] = make_uint2(mc_vertex(s_te[s_case[cell]][k - (e >> 16)], cell & 63u, s_vol[jb], s_cp, s_iso[jb]),
                                 s_id[jb]);
         }
     }
