@@ -367,7 +367,9 @@ __global__ void __launch_bounds__(16 * kBmcBlocks, kBmcThreadsPerSm / (16 * kBmc
 {
     constexpr int kBmcThreads = 16 * kBmcBlocks;
     constexpr int kBmcCells = 64 * kBmcBlocks;
-    __shared__ float s_vol[kBmcBlocks][128];
+    // a block's 5^3 grid; rows 144 floats apart (16 mod 32 banks), so the two
+    // blocks of a warp read their corner rows on complementary banks
+    __shared__ float s_vol[kBmcBlocks][144];
     __shared__ uint8_t s_rm[kBmcBlocks][32];  // corner-row masks of each block (count_cells)
     __shared__ uint32_t s_pair[32], s_pair_sw[32];  // 5-bit row mask -> per-cell corner pairs
     __shared__ __align__(16) uint16_t s_te[256][16];  // c_tri_edges

@@ -617,7 +617,9 @@ constexpr int kMcMaskWords = kMcCells * 15 / 32;  // a tile holds at most 15 ver
 template <bool kHost>
 __global__ void __launch_bounds__(kMcThreads, kMcPerSm) k_mc(QueryState* q, McArgs a)
 {
-    __shared__ float s_vol[kMcBlocks][128];
+    // a block's 5^3 grid; rows 144 floats apart (16 mod 32 banks), so the two
+    // blocks of a warp read their corner rows on complementary banks
+    __shared__ float s_vol[kMcBlocks][144];
     __shared__ uint8_t s_rm[kMcBlocks][32];  // corner-row masks of each block (count_cells)
     __shared__ uint32_t s_pair[32], s_pair_sw[32];  // 5-bit row mask -> per-cell corner pairs
     __shared__ __align__(16) uint16_t s_te[256][16];  // c_tri_edges
