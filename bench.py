@@ -621,8 +621,9 @@ def served_bench() -> dict:
 
 
 # DRAM bytes (read + write) per launch of k_mc on this workload, from one ncu
-# capture (mean over the 16-isovalue sweep): a profile constant, reported as such
-NCU_TRAFFIC = {"k_mc": 42.037e6}
+# capture of 16 consecutive launches (dram__bytes_read.sum + dram__bytes_write.sum,
+# mean over one 16-isovalue sweep): a profile constant, reported as such
+NCU_TRAFFIC = {"k_mc": 42.979e6}
 
 
 def algorithmic_bytes(stage: str, st: dict, rate: int, total_blocks: int) -> float:
