@@ -483,11 +483,17 @@ def batched_bench(reps: int = 5) -> dict:
 
 SERVED = dict(workload="1024x1024x1080 uint16-range value noise (~60% background blocks, 17,694,720 blocks) "
                        "+ 256^3 value noise, 320^3 blobs, 384^3 spectral, 512^3 value noise; ZFP rate 4; Poisson "
-                       "arrivals, volume weighted by size, isovalue uniform in its range; 40 GB slot pool",
+                       "arrivals, volume weighted by size, isovalue uniform in its range; 40 GB slot pool; server batches of "
+                       "one request, two in flight",
               big=(1024, 1024, 1080),
               others=[("ct_like", (256, 256, 256)), ("blobs", (320, 320, 320)), ("turbulence", (384, 384, 384)),
                       ("ct_like", (512, 512, 512))],
-              rate=4, pool_bytes=40 << 30, seed=5, rates=(100.0, 200.0, 300.0, 400.0, 500.0, 600.0), seconds=2.5)
+              rate=4, pool_bytes=40 << 30, seed=5, rates=(100.0, 200.0, 300.0, 400.0, 500.0, 600.0), seconds=4.0,
+              # one request per batch, two in flight: a query of this mix averages 87 M vertices,
+              # enough to fill the GPU on its own, so batching would only make each request wait
+              # for its batch-mates (measured: equal-p99 ratios 0.7-1.0 at up to 256 per batch,
+              # 1.1-1.9 at one)
+              server_max_batch=1)
 
 
 def served_bench() -> dict:
@@ -556,7 +562,7 @@ def served_bench() -> dict:
     while warm:  # warm-up: first decodes, graphs, buffer growth
         _, m = eng.run_admit(warm)
         warm = warm[m:]
-    srv = bcmc.Server(eng, max_batch=256)
+    srv = bcmc.Server(eng, max_batch=SERVED["server_max_batch"])
     sweeps = []
     try:
         for r in SERVED["rates"]:
