@@ -24,7 +24,7 @@ Lines printed (one JSON line on rank 0):
           with the oracle on the walk's first 8 queries beside it
   batched / served / render_ms  the batched engine, the continuous-batching
           server and the render pass, each summarised; their full records
-          (per-rate sweeps, autotune choices) go to gpurun_out/bench_detail.json
+          (per-rate sweeps, autotune choices) go to the detail file (DETAIL)
 
 `--impl reference` times the CPU restatement of the reference pipeline (the
 reference itself is WebGPU/JavaScript and has no CPU path) on the same config.

@@ -1,7 +1,6 @@
-"""A bounded device wait that runs out (SURVEY's failure-detection plan: every
-decoupled look-back has a spin limit and reports an error status; the
-reference only raises alerts, js/lru_cache.js:315-317,
-js/exclusive_scan.js:117-119).
+"""A bounded device wait that runs out.  Every decoupled look-back has a spin
+limit and reports an error status when it runs out (the reference only raises
+alerts, js/lru_cache.js:315-317, js/exclusive_scan.js:117-119).
 
 bcmc_debug_drop_tile makes one tile publish no look-back status, so the tiles
 after it wait on a status word that nothing sets.  Their spin limit ends the
