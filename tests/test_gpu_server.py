@@ -140,3 +140,31 @@ def test_overlapped_batches_match_plain_path(ctx, volumes):
         assert st["batches"] < len(reqs)
     finally:
         srv.close()
+
+
+def test_single_request_batches_overlap_and_match_plain_path(ctx, volumes):
+    """max_batch=1 (the setting for mixes whose queries each fill the GPU):
+    every request is its own batch, the next one is launched while the one
+    before it is still on the device, and every result equals the plain
+    path's."""
+    reqs = _isos(volumes, 60, seed=9)
+    plain = []
+    mcs = {}
+    for v, iso in reqs:
+        if v not in mcs:
+            mcs[v] = bcmc.CompressedMarchingCubes(ctx)
+            mcs[v].setCompressedVolume(volumes[v]["stream"], volumes[v]["rate"], volumes[v]["dims"])
+        mcs[v].computeSurface(iso)
+        plain.append(mcs[v].copyVertices().copy())
+    eng, srv = _server(ctx, volumes, max_batch=1)
+    try:
+        tickets = [srv.submit(v, iso, max_vertices=len(plain[i]) + 8) for i, (v, iso) in enumerate(reqs)]
+        for i, t in enumerate(tickets):
+            n, nact, lat, verts = srv.wait(t)
+            assert n == len(plain[i]), i
+            assert np.array_equal(verts, plain[i]), i
+        st = eng.stats()
+        assert st["batches"] == len(reqs), st
+        assert st["overlapped_batches"] > 0, st
+    finally:
+        srv.close()
