@@ -73,7 +73,10 @@ struct QueryState {
     uint32_t mc_arrived;
     uint32_t tiles_emit;
     uint32_t sort_arrived;  // k_sort's grid barriers between digit passes
-    uint32_t pad[4];
+    // the last age sort's plan was the one-pass one (k_slots then accumulates the
+    // age bins alone); kept across queries, zero when the state is created
+    uint32_t sort_prev_dense;
+    uint32_t pad[3];
 };
 
 // The test hook's check: this tile publishes nothing, so the tiles after it

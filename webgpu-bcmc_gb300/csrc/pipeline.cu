@@ -358,11 +358,16 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
     const uint32_t old = q->old_cache_size, nsz = q->new_cache_size;
     const bool compact = q->num_new > 0;
     const bool hist = compact && a.plan != 0u;
+    // the six digit histograms of the sort keys are needed unless the plan is
+    // the one-pass one on the age bins; expect that when the last update's was
+    // (a misprediction is repaired by the last CTA below)
+    const bool digits = hist && q->sort_prev_dense == 0u;
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t wide = 0;     // an age without a 16-bit key
     uint32_t binless = 0;  // an age outside the age bins
     if (hist) {
-        for (int i = threadIdx.x; i < 1536; i += kActThreads) (&s_hist[0][0])[i] = 0;
+        if (digits)
+            for (int i = threadIdx.x; i < 1536; i += kActThreads) (&s_hist[0][0])[i] = 0;
         for (int i = threadIdx.x; i < (int)kAgeBins; i += kActThreads) s_bins[i] = 0;
     }
     const uint32_t ntiles = div_up(nsz, kSlotTile);
@@ -430,12 +435,14 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
                     if (bin == kAgeBins) binless = 1;
                     const uint32_t bp = __match_any_sync(0xffffffffu, bin);
                     if (bin < kAgeBins && lane == (uint32_t)__ffs(bp) - 1u) atomicAdd(&s_bins[bin], (uint32_t)__popc(bp));
+                    if (digits) {
 #pragma unroll
-                    for (int d = 0; d < 6; ++d) {
-                        const uint32_t digit = fl[j] ? ((d < 4 ? k : k16) >> (8 * (d & 3))) & 255u : 256u;
-                        const uint32_t peers = __match_any_sync(0xffffffffu, digit);
-                        if (fl[j] && lane == (uint32_t)__ffs(peers) - 1u)
-                            atomicAdd(&s_hist[d][digit], (uint32_t)__popc(peers));
+                        for (int d = 0; d < 6; ++d) {
+                            const uint32_t digit = fl[j] ? ((d < 4 ? k : k16) >> (8 * (d & 3))) & 255u : 256u;
+                            const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+                            if (fl[j] && lane == (uint32_t)__ffs(peers) - 1u)
+                                atomicAdd(&s_hist[d][digit], (uint32_t)__popc(peers));
+                        }
                     }
                 }
             }
@@ -446,10 +453,11 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
     // this CTA's histograms into q->sort_hist; the last CTA to finish makes
     // the sort's pass plan (what k_sort_hist's last CTA does)
     uint32_t* gh = &q->sort_hist[0][0];  // sort_hist16 follows it
-    for (int i = threadIdx.x; i < 1536; i += kActThreads) {
-        const uint32_t c = (&s_hist[0][0])[i];
-        if (c) atomicAdd(gh + i, c);
-    }
+    if (digits)
+        for (int i = threadIdx.x; i < 1536; i += kActThreads) {
+            const uint32_t c = (&s_hist[0][0])[i];
+            if (c) atomicAdd(gh + i, c);
+        }
     for (int i = threadIdx.x; i < (int)kAgeBins; i += kActThreads)
         if (s_bins[i]) atomicAdd(a.age_hist + i, s_bins[i]);
     if (__syncthreads_or(wide) && threadIdx.x == 0) atomicOr(&q->sort_wide, 1u);
@@ -489,9 +497,34 @@ __global__ void __launch_bounds__(kActThreads) k_slots(QueryState* q, SlotArgs a
     }
 #pragma unroll
     for (int k = 0; k < 2; ++k) a.age_hist[2u * threadIdx.x + k] = 0u;  // zero again for the next update
+    if (!dense && !digits) {
+        // the one-pass plan was expected and does not apply: the digit
+        // histograms from the compacted keys, by this CTA alone (the CTAs
+        // accumulated none, so q->sort_hist is still zero)
+        const uint32_t n = q->num_avail;
+        for (int i = threadIdx.x; i < 1536; i += kActThreads) (&s_hist[0][0])[i] = 0;
+        __syncthreads();
+        for (uint32_t i0 = 0; i0 < n; i0 += kActThreads) {
+            const uint32_t i = i0 + threadIdx.x;
+            const bool v = i < n;
+            const uint32_t age = v ? __ldcg(a.avail_keys + i) : 0u;
+            const uint32_t k = ~age, k16 = ~age_key16(age);
+#pragma unroll
+            for (int d = 0; d < 6; ++d) {
+                const uint32_t digit = v ? ((d < 4 ? k : k16) >> (8 * (d & 3))) & 255u : 256u;
+                const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+                if (v && lane == (uint32_t)__ffs(peers) - 1u) atomicAdd(&s_hist[d][digit], (uint32_t)__popc(peers));
+            }
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < 1536; i += kActThreads) gh[i] = (&s_hist[0][0])[i];
+    }
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) q->sort_key16 = dense ? 2u : (key16 ? 1u : 0u);
+    if (threadIdx.x == 0) {
+        q->sort_key16 = dense ? 2u : (key16 ? 1u : 0u);
+        q->sort_prev_dense = dense ? 1u : 0u;
+    }
     if (dense) sort_plan(q, q->num_avail, s_warp, rank_hist, 1);
     else if (key16) sort_plan(q, q->num_avail, s_warp, &q->sort_hist16[0][0], 2);
     else sort_plan(q, q->num_avail, s_warp, &q->sort_hist[0][0], 4);
