@@ -1,7 +1,9 @@
 // Host definitions of the CUDA keywords and intrinsics that the device ZFP
-// decoder (webgpu-bcmc_gb300/csrc/zfp_device.cuh) uses, so that the same
-// header compiles as host C++ for the CPU test of its parse and deposit
-// (test infrastructure only; the product builds the header with nvcc).
+// decoder (webgpu-bcmc_gb300/csrc/zfp_device.cuh) and the marching-cubes
+// vertex code (mc_vertex.cuh) use, so that the same headers compile as host
+// C++ for their CPU tests (test infrastructure only; the product builds the
+// headers with nvcc).  Build with -ffp-contract=off: each float operation
+// below then rounds on its own, as the device intrinsics do.
 #pragma once
 #include <stdint.h>
 #include <string.h>
@@ -52,6 +54,14 @@ static inline float __int_as_float(int32_t i)
 }
 static inline float __int2float_rn(int32_t i) { return (float)i; }
 static inline float __fmul_rn(float a, float b) { return a * b; }
+static inline float __fadd_rn(float a, float b) { return a + b; }
+static inline float __fsub_rn(float a, float b) { return a - b; }
+static inline float __fdiv_rn(float a, float b) { return a / b; }
+// round toward zero, saturating (NaN -> 0)
+static inline uint32_t __float2uint_rz(float f)
+{
+    return !(f > 0.0f) ? 0u : (f >= 4294967296.0f ? 0xffffffffu : (uint32_t)f);
+}
 template <class T>
 static inline T __ldg(const T* p) { return *p; }
 static inline void __syncwarp(unsigned = 0xffffffffu) {}

@@ -26,8 +26,8 @@ def host_decoder():
     if cxx is None:
         pytest.skip("no host C++ compiler")
     os.makedirs(BUILD, exist_ok=True)
-    src = os.path.join(HERE, "host_decoder", "decoder_host.cpp")
-    cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-I", os.path.join(HERE, "host_decoder"),
+    src = os.path.join(HERE, "host_device", "decoder_host.cpp")
+    cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-I", os.path.join(HERE, "host_device"),
            "-I", os.path.join(ROOT, "webgpu-bcmc_gb300", "csrc"), src, "-o", LIB]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
