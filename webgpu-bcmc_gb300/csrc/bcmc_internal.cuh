@@ -135,51 +135,6 @@ __device__ __forceinline__ uint64_t lb_load(const uint64_t* p)
     return v;
 }
 
-__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p)
-{
-    uint32_t v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// Single-thread look-back over tiles [0, tile) of one counter whose status
-// word for tile i sits at status[i * stride].  Publishes the tile's aggregate
-// (tile > 0), accumulates predecessors until an inclusive prefix is found,
-// then publishes its own inclusive prefix.  Returns the exclusive prefix.  A
-// wait that exceeds kSpinLimit records `site` in *err and stops the walk, so
-// the kernel always finishes (the host reports BCMC_E_TIMEOUT).
-__device__ __forceinline__ uint32_t lookback_exclusive(uint64_t* status, uint32_t tile,
-                                                       uint32_t aggregate, uint32_t epoch,
-                                                       uint32_t* err, uint32_t site,
-                                                       uint32_t stride = 1)
-{
-    if (tile == 0) {
-        lb_store(status, lb_pack(epoch, kFlagPrefix, aggregate));
-        return 0;
-    }
-    lb_store(status + (uint64_t)tile * stride, lb_pack(epoch, kFlagAggregate, aggregate));
-    uint32_t exclusive = 0;
-    int64_t t = (int64_t)tile - 1;
-    uint32_t spins = 0;
-    while (t >= 0) {
-        const uint64_t s = lb_load(status + (uint64_t)t * stride);
-        const uint32_t hi = (uint32_t)(s >> 32);
-        if ((hi >> 2) != epoch || (hi & 3u) == 0) {
-            if (++spins > kSpinLimit) {
-                atomicCAS(err, 0u, site);
-                break;
-            }
-            if (spins > 32) __nanosleep(100);
-            continue;
-        }
-        exclusive += (uint32_t)s;
-        if ((hi & 3u) == kFlagPrefix) break;
-        --t;
-    }
-    lb_store(status + (uint64_t)tile * stride, lb_pack(epoch, kFlagPrefix, exclusive + aggregate));
-    return exclusive;
-}
-
 // Warp-cooperative look-back, called by all 32 lanes of one warp: each round
 // reads the status words of 32 * kPer predecessors at once (a round trip to
 // L2 costs microseconds when hundreds of tiles poll, so callers with many
