@@ -638,10 +638,12 @@ constexpr int kMcMaskWords = kMcCells * 15 / 32;  // a tile holds at most 15 ver
 //   emit: tiles of 16 consecutive list entries, claimed from a counter by
 //     whichever CTA is free -- vertex counts differ between ranges by up to
 //     7x, so the emit work is balanced across the grid, not per range --
-//     reloaded (from L2); a CTA scan gives each cell's offset and the vertices
-//     are spread over the CTA -- thread k takes vertex k of the tile, finds its
-//     cell by binary search, its edge in the precomputed corner-pair table --
-//     so lanes stay converged and stores are contiguous.
+//     reloaded (from L2); a CTA scan gives each cell's offset and marks each
+//     cell's first vertex in a bitmask, and the vertices are spread over the
+//     CTA -- thread k takes vertex k of the tile, finds its cell from the
+//     bitmask (a population count below bit k plus the cells started before
+//     its word), its edge's two corners and axis in the (case, vertex) table
+//     -- so lanes stay converged and stores are contiguous.
 // Ranges of at most two tiles (small queries) skip the barrier: each CTA
 // emits its own range's tiles of blocks with vertices.  On the 256^3 CT-like
 // sweep the barrier and the tile claims cost 6-10 us on queries of under
