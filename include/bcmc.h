@@ -117,7 +117,9 @@ typedef struct {
 /* computeSurface(isovalue, perfTracker) -> numVertices
  * (js/compressed_marching_cubes.js:580-809).  Blocks until the vertex count is
  * known.  `perf` may be NULL (no per-stage timing); passing one adds the
- * stage-timing events to the query (some tens of microseconds). */
+ * stage-timing events to the query (some tens of microseconds).  Vertex
+ * counts are 32-bit, as the reference's: a query of 2^32 or more vertices
+ * returns BCMC_E_STATE (its mesh is not produced). */
 bcmc_status bcmc_compute_surface(bcmc_vol* vol, float isovalue, bcmc_perf* perf,
                                  uint32_t* num_vertices);
 

@@ -769,7 +769,13 @@ static bcmc_status vol_query(bcmc_vol* v, float iso, bcmc_perf* perf, uint32_t* 
             if (perf) BCMC_CUDA(cudaEventRecord(v->ev[4], s));
             lru_read_state(c, s);
             if (c->h_q->error) return fail(ctx, BCMC_E_TIMEOUT, "device wait timed out");
-            if (c->h_q->vert_overflow) return fail(ctx, BCMC_E_STATE, "vertex buffer growth failed");
+            // a query of 2^32 or more vertices lands here too: vertex counts
+            // are 32-bit (as the reference's), so the CTA whose range crosses
+            // 2^32 fails its fit check again after any growth
+            if (c->h_q->vert_overflow)
+                return fail(ctx, BCMC_E_STATE,
+                            "vertex buffer growth failed (or the query has 2^32 or more vertices, past the 32-bit "
+                            "vertex count)");
         } else if (h.num_verts > v->verts_storage) {
             v->verts_storage = h.num_verts;  // the reference's storage bookkeeping
         }
