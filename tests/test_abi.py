@@ -84,3 +84,16 @@ def test_short_stream_is_refused_before_the_kernel():
     with pytest.raises(ValueError):
         bcmc._check_stream(Fake(), 8, 2)  # 8 blocks at rate 2 need 16 words
     bcmc._check_stream(Fake(), 5, 2)
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """No CPU fallback: without the built library every entry of the host side
+    raises instead of computing anything."""
+    import bcmc
+
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "libbcmc_gb300.so"))
+    with pytest.raises(ImportError, match="no CPU fallback"):
+        _lib.load()
+    with pytest.raises(ImportError):
+        bcmc.Context(0)
