@@ -3,7 +3,9 @@ C++, against the oracle's decode (shaders/zfp_decompress.comp:195-384): every
 rate from 1 to 32 bits per value, random bit streams (dense, sparse, single
 bits, zero blocks) and encoded fields, compared bit for bit.  This covers the
 group-test parse (budget and coefficient-63 limits, 64-bit raw reads, leading
-empty planes) and the plane deposit without a GPU."""
+empty planes) and the plane deposit without a GPU.  The device encoder (the
+reference only decodes; it makes the benchmark inputs) is checked the same way
+against the oracle's encoder, stream word for word."""
 import ctypes
 import os
 import shutil
@@ -88,3 +90,52 @@ def test_encoded_fields_match_oracle(host_decoder, oracle, kind, dims, rate):
     got = host_decoder(w, nb, rate)
     ref = oracle.decode_volume(w, nb, 64 * rate)
     assert np.array_equal(_bits(got), _bits(ref))
+
+
+@pytest.fixture(scope="module")
+def host_encoder(host_decoder):
+    lib = ctypes.CDLL(LIB)  # built by host_decoder
+    lib.encode_blocks_host.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p]
+    lib.encode_blocks_host.restype = None
+
+    def encode(field, rate):
+        """field [z, y, x] with every extent a multiple of 4: its blocks
+        gathered as the encode kernel gathers them, encoded one by one."""
+        Z, Y, X = field.shape
+        blocks = np.ascontiguousarray(
+            field.reshape(Z // 4, 4, Y // 4, 4, X // 4, 4).transpose(0, 2, 4, 1, 3, 5).reshape(-1, 64),
+            dtype=np.float32)
+        nb = blocks.shape[0]
+        words = np.zeros(nb * rate, dtype=np.uint64)
+        lib.encode_blocks_host(blocks.ctypes.data, nb, rate, words.ctypes.data)
+        return words
+
+    return encode
+
+
+def _special_field(rs):
+    """Blocks of zeros, constants, denormals, huge and tiny magnitudes, mixed
+    signs and values just below a power of two, on a 16^3 grid of 64 blocks."""
+    f = rs.standard_normal((16, 16, 16)).astype(np.float32)
+    f *= np.float32(10.0) ** rs.integers(-30, 30, size=f.shape).astype(np.float32)
+    b = f.reshape(4, 4, 4, 4, 4, 4)  # [bz, z, by, y, bx, x] views of blocks
+    b[0, :, 0, :, 0, :] = 0.0
+    b[0, :, 0, :, 1, :] = 3.0
+    b[0, :, 0, :, 2, :] = np.float32(1e-40) * rs.standard_normal((4, 4, 4)).astype(np.float32)
+    b[0, :, 0, :, 3, :] = np.float32(np.nextafter(np.float32(2.0), np.float32(0.0)))
+    b[1, :, 0, :, 0, :] = np.float32(3.0e38) * np.sign(rs.standard_normal((4, 4, 4))).astype(np.float32)
+    b[1, :, 0, :, 1, :] = -np.float32(1.0)
+    b[1, :, 0, 0, 1, 0] = np.float32(1.0)
+    return f
+
+
+@pytest.mark.parametrize("rate", [1, 2, 4, 8, 16, 32])
+def test_device_encoder_matches_oracle_encoder(host_encoder, oracle, rate):
+    rs = np.random.default_rng(77 + rate)
+    fields = [D.make_field("turbulence", (32, 32, 32), 3), D.make_field("ct_like", (32, 32, 32), 4),
+              D.make_field("blobs", (32, 32, 32), 5), _special_field(rs)]
+    for f in fields:
+        nb = f.size // 64
+        got = host_encoder(f, rate)
+        ref = oracle.zfp_encode(f, rate)[: nb * rate]
+        assert np.array_equal(got, ref)
