@@ -97,3 +97,44 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
         _lib.load()
     with pytest.raises(ImportError):
         bcmc.Context(0)
+
+
+_NULL_CALLS = r"""
+import ctypes as C, json, sys
+from bcmc import _lib
+L = _lib.load()
+ints = (C.c_uint8, C.c_int, C.c_int32, C.c_uint32, C.c_int64, C.c_uint64, C.c_size_t)
+for name in sorted(_lib.SIGNATURES):
+    rt, args = _lib.SIGNATURES[name]
+    vals = [0.0 if a in (C.c_float, C.c_double) else (0 if a in ints else None) for a in args]
+    print(name, flush=True)  # the last name printed is the culprit if the call crashes
+    r = getattr(L, name)(*vals)
+    print(json.dumps({"name": name, "r": r if r is None or isinstance(r, int) else str(r)}), flush=True)
+"""
+
+
+def test_every_entry_point_refuses_null_arguments(lib_built):
+    """Each entry point of include/bcmc.h, called with null pointers and zero
+    sizes, returns an error status (or, for the size helpers, zero) instead of
+    dereferencing anything; no device is needed for that."""
+    import subprocess
+    import sys
+    import json
+
+    pkg = os.path.dirname(os.path.dirname(_lib.__file__))
+    r = subprocess.run([sys.executable, "-c", _NULL_CALLS], cwd=pkg, capture_output=True, text=True, timeout=120,
+                       env=dict(os.environ, PYTHONPATH=pkg))
+    lines = r.stdout.splitlines()
+    assert r.returncode == 0, (lines[-1:] if lines else None, r.stderr[-2000:])
+    got = {d["name"]: d["r"] for d in (json.loads(l) for l in lines if l.startswith("{"))}
+    assert sorted(got) == sorted(_lib.SIGNATURES)
+    status = {n for n, (rt, _) in _lib.SIGNATURES.items() if rt is C.c_int}
+    assert len(status) >= 40
+    for n in status - {"bcmc_scan_exclusive_u32_noalloc"}:
+        assert got[n] == 1, (n, got[n])  # BCMC_E_ARG
+    # n = 0 with null pointers is a valid empty scan: OK with a device, a
+    # set-up error (BCMC_E_CUDA) without one
+    assert got["bcmc_scan_exclusive_u32_noalloc"] in (0, 3)
+    for n in ("bcmc_scan_aligned_size", "bcmc_sort_aligned_size", "bcmc_zfp_stream_words"):
+        assert got[n] == 0, n
+    assert got["bcmc_ctx_stream"] is None
