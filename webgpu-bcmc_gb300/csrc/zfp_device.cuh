@@ -232,12 +232,16 @@ __device__ __forceinline__ void zfp_planes_deposit(const uint32_t* pl, uint32_t 
     {
         uint32_t L[8], H[8];
         zfp_chunk(pl, 0u, np, L, H);
+        // r0 is 32 only for a block whose 32 planes are all empty: np is 0,
+        // every row is zero, and the shift (kept below 32, as C++ requires)
+        // moves nothing
+        const uint32_t s0 = r0 & 31u;
 #pragma unroll
         for (int k = 0; k < 8; ++k)
 #pragma unroll
             for (int g = 0; g < 4; ++g) {
-                u[8 * g + k] = __byte_perm(L[k], 0u, 0x0444u | ((uint32_t)g << 12)) >> r0;
-                u[8 * (g + 4) + k] = __byte_perm(H[k], 0u, 0x0444u | ((uint32_t)g << 12)) >> r0;
+                u[8 * g + k] = __byte_perm(L[k], 0u, 0x0444u | ((uint32_t)g << 12)) >> s0;
+                u[8 * (g + 4) + k] = __byte_perm(H[k], 0u, 0x0444u | ((uint32_t)g << 12)) >> s0;
             }
     }
     for (uint32_t c = 1; c * 8u < np; ++c) {
