@@ -17,7 +17,11 @@ import subprocess
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-_LIB_PATH = os.path.join(_HERE, "_build", "libbcmc_oracle.so")
+# BCMC_ORACLE_SANITIZE=1 selects the AddressSanitizer + UBSan build (`make
+# asan`); the Python process must then preload libasan and libubsan
+# (LD_PRELOAD), since the interpreter is not built with them
+_SANITIZE = os.environ.get("BCMC_ORACLE_SANITIZE") == "1"
+_LIB_PATH = os.path.join(_HERE, "_build", "libbcmc_oracle_asan.so" if _SANITIZE else "libbcmc_oracle.so")
 _lib = None
 
 u32p = C.POINTER(C.c_uint32)
@@ -28,7 +32,7 @@ f32p = C.POINTER(C.c_float)
 
 def build() -> str:
     """Compile the oracle with its Makefile (gcc, OpenMP)."""
-    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    subprocess.run(["make", "-s", "-C", _HERE] + (["asan"] if _SANITIZE else []), check=True)
     return _LIB_PATH
 
 

@@ -8,6 +8,7 @@ reference only decodes; it makes the benchmark inputs) is checked the same way
 against the oracle's encoder, stream word for word."""
 import ctypes
 import os
+import shlex
 import shutil
 import subprocess
 
@@ -31,6 +32,7 @@ def host_decoder():
     src = os.path.join(HERE, "host_device", "decoder_host.cpp")
     cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-I", os.path.join(HERE, "host_device"),
            "-I", os.path.join(ROOT, "webgpu-bcmc_gb300", "csrc"), src, "-o", LIB]
+    cmd += shlex.split(os.environ.get("BCMC_HOST_CXXFLAGS", ""))  # e.g. sanitizers
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     lib = ctypes.CDLL(LIB)

@@ -8,6 +8,7 @@ values, bit for bit.  Ties (a corner equal to the isovalue), near-equal
 corners (the 0.001 test) and values far from the isovalue are included."""
 import ctypes
 import os
+import shlex
 import shutil
 import subprocess
 
@@ -35,6 +36,7 @@ def host_mc():
     src = os.path.join(HERE, "host_device", "mc_vertex_host.cpp")
     cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-I", os.path.join(HERE, "host_device"),
            "-I", os.path.join(ROOT, "webgpu-bcmc_gb300", "csrc"), src, "-o", LIB]
+    cmd += shlex.split(os.environ.get("BCMC_HOST_CXXFLAGS", ""))  # e.g. sanitizers
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     lib = ctypes.CDLL(LIB)
