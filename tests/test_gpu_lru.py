@@ -61,3 +61,45 @@ def test_lru_ties_after_reset(ctx, oracle):
     n, ids = g.update(to_dev(needed))
     assert np.array_equal(ids.numpy(), r.update(needed))
     _compare(g, r, total)
+
+
+def _one_pass_plan(ages):
+    """The age sort's one-pass plan applies when every available age lies in
+    an age bin (below 256 within its class: an update count, or 100000 plus
+    one) and at most 256 bins are in use."""
+    ages = ages.astype(np.int64)
+    in_bin = (ages < 256) | ((ages >= 100000) & (ages - 100000 < 256))
+    if not np.all(in_bin):
+        return False
+    return len(np.unique(np.where(ages < 256, ages, 256 + ages - 100000))) <= 256
+
+
+def test_lru_plan_change_from_one_pass_to_keys(ctx, oracle):
+    """The cache update expects the sort plan of the update before it: it
+    accumulates only the age bins while that plan was the one-pass one, and
+    its last CTA builds the keys' digit histograms itself when the plan
+    changes.  After a reset (every slot at age 100000), one new item per
+    update keeps the one-pass plan until the untouched slots' ages leave the
+    bins after 256 updates; the slot state must match the oracle's throughout."""
+    total, initial = 2000, 1000
+    g = bcmc.LRUCache(ctx, None, None, initial, 256, total)
+    r = oracle.LRUCache(initial, total)
+    g.reset()
+    r.reset()
+    prev_one_pass, changes = False, []
+    for step in range(270):
+        needed = np.zeros(total, np.uint32)
+        needed[step] = 1
+        st = r.state()
+        age, item = st["age"][: r.cache_size], st["item"][: r.cache_size]
+        keep = (item >= 0) & (needed[np.maximum(item, 0)] != 0)
+        one_pass = _one_pass_plan(np.where(keep, 0, age.astype(np.int64) + 1)[~keep])
+        if prev_one_pass and not one_pass:
+            changes.append(step)
+        prev_one_pass = one_pass
+        n_gpu, ids = g.update(to_dev(needed))
+        ref_ids = r.update(needed)
+        assert n_gpu == len(ref_ids) == 1, step
+        assert np.array_equal(ids.numpy(), ref_ids), step
+        _compare(g, r, total)
+    assert changes == [255]
