@@ -136,6 +136,12 @@ def test_surface_straight_to_host(ctx, oracle):
         assert np.array_equal(a.lruCache.state()["item_slots"], b.lruCache.state()["item_slots"])
     with pytest.raises(bcmc.BcmcError):
         b.vertexBuffer  # noqa: B018 -- the last query went to host memory
+    # a buffer 8-byte aligned but off every 256-byte boundary (the kernel
+    # aligns each warp's stores to 256-byte windows of the host buffer)
+    for off in (1, 5, 31):
+        n = a.computeSurface(0.42)
+        m = b.computeSurfaceToHost(0.42, pinned[off:])
+        assert m == n and np.array_equal(pinned[off:off + m], a.copyVertices()), off
     n = a.computeSurface(0.5)
     small = pinned[:10]
     with pytest.raises(bcmc.BcmcError):
