@@ -99,6 +99,50 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
         bcmc.Context(0)
 
 
+_C_HOST = r"""
+#include <stdio.h>
+#include "bcmc.h"
+int main(void)
+{
+    bcmc_opts opts;
+    bcmc_ctx* ctx = NULL;
+    const uint32_t dims[3] = {13, 7, 9};
+    bcmc_opts_default(&opts);
+    bcmc_status st = bcmc_ctx_create(&opts, &ctx);
+    printf("%d %u %u %llu\n", (int)st, bcmc_scan_aligned_size(1000), bcmc_sort_aligned_size(1000),
+           (unsigned long long)bcmc_zfp_stream_words(dims, 4));
+    if (st == BCMC_OK) bcmc_ctx_destroy(ctx);
+    return 0;
+}
+"""
+
+
+def test_header_is_c99_and_links_from_c(lib_built, tmp_path):
+    """A C host (a cgo or FFI binding compiles the header as C) builds against
+    include/bcmc.h with -std=c99 -pedantic and warnings as errors, links the
+    library and calls it."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "host.c"
+    src.write_text(_C_HOST)
+    exe = tmp_path / "host"
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.dirname(_lib.HEADER),
+                        str(src), "-L", libdir, "-lbcmc_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    st, scan, sort, words = (int(x) for x in r.stdout.split())
+    assert st in (0, 3)  # a context on a GPU machine, BCMC_E_CUDA without one
+    assert (scan, sort) == (1024, 1024)
+    assert words == (4 * 2 * 3) * 4 + 1  # 24 blocks of 4 u64 words, one pad word
+
+
 _NULL_CALLS = r"""
 import ctypes as C, json, sys
 from bcmc import _lib
