@@ -455,7 +455,9 @@ void bcmc_server_destroy(bcmc_server* srv);
 bcmc_status bcmc_server_submit(bcmc_server* srv, uint32_t volume, float isovalue, void* host_vertices,
                                uint64_t host_capacity, uint64_t* ticket);
 /* Blocks until the request completes.  result->vertex_offset is 0 (batch
- * buffers are reused); latency_ms = completion - submission, wall clock. */
+ * buffers are reused); latency_ms = completion - submission, wall clock.
+ * Each ticket is waited for once: a ticket never issued or already waited
+ * for returns BCMC_E_ARG at once. */
 bcmc_status bcmc_server_wait(bcmc_server* srv, uint64_t ticket, bcmc_query_result* result,
                              double* latency_ms);
 /* Open-loop load: `requests` arrivals with exponential inter-arrival times at

@@ -168,3 +168,20 @@ def test_single_request_batches_overlap_and_match_plain_path(ctx, volumes):
         assert st["overlapped_batches"] > 0, st
     finally:
         srv.close()
+
+
+def test_each_ticket_is_waited_for_once(ctx, volumes):
+    """A ticket already waited for, or never issued, is refused at once
+    instead of blocking its caller; the server keeps serving."""
+    eng, srv = _server(ctx, volumes, max_batch=4)
+    try:
+        (v, iso), = _isos(volumes, 1, seed=11)
+        t = srv.submit(v, iso)
+        n = srv.wait(t)[0]
+        with pytest.raises(bcmc.BcmcError):
+            srv.wait(t)
+        with pytest.raises(bcmc.BcmcError):
+            srv.wait(t + 1000)
+        assert srv.wait(srv.submit(v, iso))[0] == n
+    finally:
+        srv.close()

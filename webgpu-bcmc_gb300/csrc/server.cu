@@ -25,6 +25,7 @@
 #include <random>
 #include <thread>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "bcmc_impl.h"
@@ -57,6 +58,7 @@ struct bcmc_server {
     std::condition_variable cv_work, cv_done;
     std::deque<Request> pending;
     std::unordered_map<uint64_t, Done> done;
+    std::unordered_set<uint64_t> unclaimed;  // submitted, not yet waited for
     uint64_t next_ticket = 1;
     bool stop = false;
     bool lane_done[2] = {false, false};  // set by the completion callback
@@ -232,6 +234,7 @@ extern "C" bcmc_status bcmc_server_submit(bcmc_server* s, uint32_t volume, float
         std::lock_guard<std::mutex> lk(s->mu);
         if (s->stop) return BCMC_E_STATE;
         *ticket = s->next_ticket++;
+        s->unclaimed.insert(*ticket);
         s->pending.push_back(Request{*ticket, volume, isovalue, host_vertices, host_capacity, Clock::now()});
     }
     s->cv_work.notify_one();
@@ -243,7 +246,9 @@ extern "C" bcmc_status bcmc_server_wait(bcmc_server* s, uint64_t ticket, bcmc_qu
 {
     if (!s || !ticket) return BCMC_E_ARG;
     std::unique_lock<std::mutex> lk(s->mu);
-    if (ticket >= s->next_ticket) return BCMC_E_ARG;
+    // each ticket is waited for once: one never issued or already claimed
+    // (whose result is gone) would otherwise block for ever
+    if (s->unclaimed.erase(ticket) == 0) return BCMC_E_ARG;
     s->cv_done.wait(lk, [&] { return s->done.count(ticket) != 0; });
     const Done d = s->done[ticket];
     s->done.erase(ticket);
