@@ -451,7 +451,8 @@ bcmc_status bcmc_server_create(bcmc_engine* eng, const bcmc_server_opts* opts, b
 void bcmc_server_destroy(bcmc_server* srv);
 /* Queues one request.  When host_vertices is not NULL the request's vertices
  * (8 bytes each, at most host_capacity of them) are copied there before the
- * request completes. */
+ * request completes.  A volume id the engine does not hold returns
+ * BCMC_E_ARG at once (nothing is queued). */
 bcmc_status bcmc_server_submit(bcmc_server* srv, uint32_t volume, float isovalue, void* host_vertices,
                                uint64_t host_capacity, uint64_t* ticket);
 /* Blocks until the request completes.  result->vertex_offset is 0 (batch

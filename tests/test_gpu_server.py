@@ -182,6 +182,8 @@ def test_each_ticket_is_waited_for_once(ctx, volumes):
             srv.wait(t)
         with pytest.raises(bcmc.BcmcError):
             srv.wait(t + 1000)
+        with pytest.raises(bcmc.BcmcError):  # an unknown volume is refused at submission
+            srv.submit(len(volumes), iso)
         assert srv.wait(srv.submit(v, iso))[0] == n
     finally:
         srv.close()

@@ -80,6 +80,7 @@ bcmc_status engine_copy_lane_vertices(bcmc_engine* e, int k, uint64_t first, uin
 // Waits for everything the engine queued, host callbacks included.
 void engine_drain(bcmc_engine* e);
 uint32_t engine_max_batch(bcmc_engine* e);
+uint32_t engine_num_volumes(bcmc_engine* e);
 uint64_t engine_vertex_budget(bcmc_engine* e);
 bcmc_ctx* engine_ctx(bcmc_engine* e);
 

@@ -1862,6 +1862,7 @@ void engine_drain(bcmc_engine* e)
 }
 
 uint32_t engine_max_batch(bcmc_engine* e) { return e->max_batch; }
+uint32_t engine_num_volumes(bcmc_engine* e) { return (uint32_t)e->vols.size(); }
 
 int engine_device(bcmc_engine* e) { return e->ctx->device; }
 uint64_t engine_vertex_budget(bcmc_engine* e) { return e->opts.vertex_budget; }

@@ -230,6 +230,8 @@ extern "C" bcmc_status bcmc_server_submit(bcmc_server* s, uint32_t volume, float
                                           uint64_t host_capacity, uint64_t* ticket)
 {
     if (!s || !ticket || (host_vertices && !host_capacity)) return BCMC_E_ARG;
+    // an unknown volume is refused here: in a batch it would fail its batch-mates too
+    if (volume >= bcmc::engine_num_volumes(s->eng)) return BCMC_E_ARG;
     {
         std::lock_guard<std::mutex> lk(s->mu);
         if (s->stop) return BCMC_E_STATE;
