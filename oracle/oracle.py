@@ -1,8 +1,8 @@
 """ctypes front end of the CPU oracle (oracle/bcmc_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: tests/, ``__graft_entry__.smoke()`` and the CPU
-baseline leg of ``bench.py`` load this module as the checker.  The product
-library never imports it.
+baseline leg of ``bench.py`` load this module, to check the CUDA results
+against it and to time it.  The product library never imports it.
 
 The oracle restates Twinklebear/webgpu-bcmc's compute shaders and JavaScript
 orchestration (citations live in bcmc_oracle.c) and adds a fixed-rate ZFP
